@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 sDEM hot path: particle-steps/s on the 1M-sphere
+polydisperse Hertz bed.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Our arm: one DEMSystem per GPU (replicas: each rank advances its own
+independent bed, no collective on the data path), W untimed steps, then K
+timed steps (CUDA events on the library's stream, barrier + synchronize on both
+sides, max over ranks).  The bed (~300 MB of state) is larger than L2, so no
+flush is needed between steps.  e2e: the same metric through the C ABI with
+host buffers: upload of the state, K host-synchronous sdem_step(h,1) calls
+each followed by a counters read-back, download of the state.
+
+--impl reference: the CPU restatement of the reference's algorithm (the
+reference's Fortran+MPI build cannot be compiled here or on the GPU host: no
+Fortran compiler, no MPI) on all host cores, one process per x-slab of the same
+bed (domain decomposition without halo), rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s, 1M Hertz spheres"
+UNIT = "particle-steps/s"
+WORKLOAD = "hertz_poly_1m"
+MEASURED_FP64_TFLOPS = 1.198   # DFMA-chain probe on this machine's GB300 (2 flops per DFMA)
+
+
+def make_case(n: int, seed: int):
+    from sdem_gb300 import beds
+    return beds.hertz_poly_case(n=n, seed=seed)
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the oracle on x-slabs of the bed, one process per core
+# ---------------------------------------------------------------------------
+def _slab_worker(args):
+    path, k, nslab, steps, warm, budget_s = args
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import OracleSystem
+    from sdem_gb300 import beds
+    meta = json.load(open(os.path.join(path, "meta.json")))
+    P = {name: np.load(os.path.join(path, name + ".npy"), mmap_mode="r")
+         for name in ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta", "rotVel", "rotAcc")}
+    x = P["posR"][:, 0]
+    lo, hi = meta["xmin"] + (meta["xmax"] - meta["xmin"]) * k / nslab, \
+        meta["xmin"] + (meta["xmax"] - meta["xmin"]) * (k + 1) / nslab
+    sel = np.nonzero((x >= lo) & (x < hi))[0]
+    parts = beds.Particles(*(np.ascontiguousarray(P[name][sel]) for name in
+                             ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta", "rotVel", "rotAcc")))
+    import pickle
+    case = pickle.load(open(os.path.join(path, "case.pkl"), "rb"))
+    case = beds.Case(case.name, case.opts, case.tables, case.walls, parts)
+    o = OracleSystem(case, max_gid=meta["max_gid"])
+    if warm:
+        o.step(warm)
+    if steps is None:   # calibrate a bounded sample
+        t0 = time.perf_counter()
+        o.step(1)
+        t1 = time.perf_counter() - t0
+        steps = int(max(2, min(400, budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    o.step(steps)
+    el = time.perf_counter() - t0
+    return len(sel), steps, el, o.counters()["pp"]
+
+
+def cpu_leg(case, steps, warm, budget_s=1.5, procs=None):
+    """Oracle over all host cores: returns (particle-steps/s, cores, sample text)."""
+    procs = procs or os.cpu_count() or 1
+    from oracle.oracle import load as load_oracle
+    load_oracle()   # build once before the workers start
+    tmp = tempfile.mkdtemp(prefix="sdem_bench_")
+    p = case.particles
+    for name in ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta", "rotVel", "rotAcc"):
+        np.save(os.path.join(tmp, name + ".npy"), getattr(p, name))
+    import pickle
+    from sdem_gb300 import beds
+    empty = beds.Particles(*(getattr(p, name)[:0] for name in
+                             ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta", "rotVel", "rotAcc")))
+    pickle.dump(beds.Case(case.name, case.opts, case.tables, case.walls, empty), open(os.path.join(tmp, "case.pkl"), "wb"))
+    json.dump({"xmin": float(case.opts.minpoint[0]), "xmax": float(case.opts.maxpoint[0]),
+               "max_gid": int(case.max_gid)}, open(os.path.join(tmp, "meta.json"), "w"))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_slab_worker, [(tmp, k, procs, steps, warm, budget_s) for k in range(procs)])
+    n_tot = sum(r[0] for r in res)
+    work = sum(r[0] * r[1] for r in res)
+    tmax = max(r[2] for r in res)
+    ksteps = sorted(set(r[1] for r in res))
+    sample = (f"{n_tot} particles of the bed in {procs} x-slabs (one oracle process per slab, no halo), "
+              f"{ksteps[0] if len(ksteps) == 1 else ksteps} steps each, wall time of the slowest slab {tmax:.2f} s")
+    return work / tmax, procs, sample
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.path = tempfile.mktemp(prefix="clocks_", suffix=".csv")
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower().startswith("active"):
+                        reasons.add(nm)
+            except Exception:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    case = make_case(1_000_000, 2)
+    procs = os.cpu_count() or 1
+    rate, cores, sample = cpu_leg(case, steps=args.steps, warm=args.warmup, procs=procs)
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * case.particles.n / rate,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_particles": case.particles.n, "parallelism": f"{cores} processes"},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "CPU restatement of the reference (oracle/sdem_oracle.c), not the reference "
+                                       "itself: " + sample},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def our_arm(args):
+    import torch
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist = None
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def allreduce(x, op):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+        return float(t.item())
+
+    from sdem_gb300 import build
+    build.build()
+    from sdem_gb300.capi import DEMSystem
+    seed = 2 + rank
+    case = make_case(args.n, seed)
+    n = case.particles.n
+    sysm = DEMSystem(case)
+    sysm.step(args.warmup)
+    stream = torch.cuda.ExternalStream(sysm.stream())
+    K = args.steps
+    barrier()
+    torch.cuda.synchronize()
+    l0 = sysm.launch_count()
+    sysm.profile_begin(K)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        sysm.step_async(K)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    phases, nprof = sysm.profile_end()
+    launches = sysm.launch_count() - l0
+    cnt = sysm.counters()
+    ms_max = allreduce(ms, "max")
+    n_all = allreduce(float(n), "sum")
+    value = n_all * K / (ms_max * 1e-3)
+
+    # dominant kernel: the contact-force kernel (one thread per contact)
+    C = cnt["pp"]
+    dom = max(phases, key=phases.get)
+    t_force = phases["force"] / nprof * 1e-3
+    force_bytes = 80.0 * C          # per persistent contact: key, spring and VelRel_Init read + written
+    achieved = force_bytes / t_force / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = None
+    try:
+        tj = json.load(open(os.path.join(ROOT, "profiles", "force_traffic.json")))
+        traffic = tj["dram_bytes_per_contact"] * C
+    except Exception:
+        pass
+    # algorithmic FP64 operations of one Hertz contact (force law + normal vector):
+    # 127 add/sub/mul, 8 sqrt, 7 divisions, each sqrt/div counted as one operation
+    fp64_per_contact = 142
+    t_step = ms / K * 1e-3
+    step_bytes = n * 352.0 + C * 80.0 + 4.0 * 0   # per-step algorithmic bytes of the whole path
+
+    # e2e: through the C ABI with host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        sys2 = DEMSystem(case)
+        sys2.step(1)
+        st = sys2.state()
+        Ke = args.e2e_steps
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sys2.upload(st)
+        for _ in range(Ke):
+            sys2.step(1)
+            sys2.counters()
+        out = sys2.state()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        el = allreduce(el, "max")
+        h2d = sum(getattr(st, f).nbytes for f in ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta",
+                                                  "rotVel", "rotAcc"))
+        d2h = sum(getattr(out, f).nbytes for f in ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta",
+                                                   "rotVel", "rotAcc")) + Ke * 32
+        e2e = {"value": n_all * Ke / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / Ke),
+               "d2h_bytes_per_step": int(d2h / Ke), "steps": Ke,
+               "note": "upload of the state, K x (sdem_step(h,1) + sdem_counters), download of the state"}
+        sys2.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        rate, cores, sample = cpu_leg(case, steps=None, warm=0)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "CPU restatement of the reference (oracle/sdem_oracle.c): " + sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
+            "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_particles": n, "contact_model": "Hertz-Mindlin",
+                       "types": int(case.tables.n_types), "dt": case.opts.dt, "integrator": "AB2",
+                       "pp_contacts": C, "pw_contacts": cnt["pw"], "contacts_per_particle": C / n,
+                       "bed": "seeded deposited packing (seed 2+rank), see sdem_gb300.beds.hertz_poly_case",
+                       "l2": "state > L2 (no flush)", "parallelism": f"replicas x{ws}"},
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic,
+                         "algorithmic_bytes": "80 B per contact x contacts per launch",
+                         "note": "k_force is FP64-ALU bound on GB300, see fp64 below"},
+            "fp64": {"kernel": "k_force", "achieved_tflops": fp64_per_contact * C / t_force / 1e12,
+                     "peak_tflops": MEASURED_FP64_TFLOPS, "frac": fp64_per_contact * C / t_force / 1e12 /
+                     MEASURED_FP64_TFLOPS},
+            "step_roofline": {"achieved": step_bytes / t_step / 1e9, "peak": hbm, "unit": "GB/s",
+                              "frac": step_bytes / t_step / 1e9 / hbm,
+                              "algorithmic_bytes": "352 B per particle + 80 B per contact per step"},
+            "phases_ms_per_step": {k: v / nprof for k, v in phases.items()},
+            "dominant_phase": dom,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    sysm.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        our_arm(args)
+
+
+if __name__ == "__main__":
+    main()

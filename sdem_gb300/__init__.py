@@ -1,0 +1,20 @@
+"""GB300-native (sm_103a) implementation of sDEM's per-step particle hot path.
+
+Modules:
+  capi      ctypes binding of libsdem_gpu.so (include/sdem_gpu.h) + DEMSystem handle
+  props     material tables (InitPrtclProperty / clc_BnryPrtcl_Prop restated)
+  geometry  plane walls (G_add_PlaneWall restated)
+  beds      seeded synthetic beds (the workloads)
+  restart   reader/writer of the reference's restart file layout
+  build     nvcc recipe of the native library
+"""
+from . import beds, geometry, props  # noqa: F401
+
+__all__ = ["beds", "geometry", "props", "capi", "build"]
+
+
+def __getattr__(name):
+    if name in ("capi", "build", "restart"):
+        import importlib
+        return importlib.import_module(f".{name}", __name__)
+    raise AttributeError(name)

@@ -1,0 +1,291 @@
+"""Seeded synthetic beds and the cases they belong to.
+
+A Case is one complete input of the hot path: options (the &DEMOptions fields
+the path reads), material tables, plane walls and particle arrays in the
+reference's layouts.  The reference's own particle maker is clock-seeded
+(Prtcl_Variables.f90:225-227), so every bed here is generated from an explicit
+seed instead and stands in for a restart file of the reference.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field, replace
+from typing import Optional, Tuple
+
+import numpy as np
+
+from . import props
+from .geometry import WallSet, box_walls
+
+
+@dataclass
+class Options:
+    """&DEMOptions fields of the hot path (Prtcl_Parameters.f90:45-95)."""
+    dt: float = 1.0e-5
+    gravity: Tuple[float, float, float] = (0.0, -9.81, 0.0)
+    minpoint: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    maxpoint: Tuple[float, float, float] = (1.0, 1.0, 1.0)
+    periodic: Tuple[int, int, int] = (0, 0, 0)
+    cs_ratio: float = 1.0
+    cs_method: int = 1
+    cf_type: int = props.CFT_LSD
+    ct_model: int = 1
+    pi_method: int = 1
+    pri_method: int = 1
+    cntct_list_size: int = 6
+    base_wall_id: int = 10000000
+    wall_max_update_iter: int = 100
+    wall_neighbor_ratio: float = 2.0
+    quirk_ab2_rot: int = 1
+    max_contacts_per_particle: int = 0
+
+    @property
+    def tsize(self) -> int:
+        return self.pi_method
+
+    @property
+    def rsize(self) -> int:
+        return self.pri_method
+
+
+@dataclass
+class Particles:
+    id: np.ndarray        # int32 (n,)
+    ptype: np.ndarray     # int32 (n,), 1-based
+    usrmark: np.ndarray   # int32 (n,)
+    posR: np.ndarray      # (n, 4): x, y, z, radius
+    linVel: np.ndarray    # (n, tsize, 3)
+    linAcc: np.ndarray    # (n, tsize, 3)
+    theta: np.ndarray     # (n, 3)
+    rotVel: np.ndarray    # (n, rsize, 3)
+    rotAcc: np.ndarray    # (n, rsize, 3)
+
+    @property
+    def n(self) -> int:
+        return len(self.id)
+
+    def copy(self) -> "Particles":
+        return Particles(*(a.copy() for a in (self.id, self.ptype, self.usrmark, self.posR, self.linVel,
+                                               self.linAcc, self.theta, self.rotVel, self.rotAcc)))
+
+    def take(self, idx) -> "Particles":
+        return Particles(*(a[idx].copy() for a in (self.id, self.ptype, self.usrmark, self.posR, self.linVel,
+                                                    self.linAcc, self.theta, self.rotVel, self.rotAcc)))
+
+
+@dataclass
+class Case:
+    name: str
+    opts: Options
+    tables: props.Tables
+    walls: WallSet
+    particles: Particles
+    contacts: Optional[tuple] = None   # (owner_idx, partner_id, tandelta (nc,3), velrel) or None
+    note: str = ""
+
+    @property
+    def max_gid(self) -> int:
+        return int(self.particles.id.max()) if self.particles.n else 1
+
+
+def new_particles(pos: np.ndarray, ptype: np.ndarray, radius_of_type: np.ndarray, vel: np.ndarray,
+                  tsize: int, rsize: int, first_id: int = 1) -> Particles:
+    n = len(pos)
+    posR = np.zeros((n, 4))
+    posR[:, :3] = pos
+    posR[:, 3] = radius_of_type[ptype - 1]
+    linVel = np.zeros((n, tsize, 3))
+    linVel[:, :, :] = vel[:, None, :]   # every AB level starts at the initial velocity
+    return Particles(id=np.arange(first_id, first_id + n, dtype=np.int32), ptype=ptype.astype(np.int32),
+                     usrmark=np.zeros(n, dtype=np.int32), posR=posR, linVel=linVel,
+                     linAcc=np.zeros((n, tsize, 3)), theta=np.zeros((n, 3)), rotVel=np.zeros((n, rsize, 3)),
+                     rotAcc=np.zeros((n, rsize, 3)))
+
+
+# --------------------------------------------------------------------------
+# workloads
+# --------------------------------------------------------------------------
+def lsd_mono_case(n: int = 20000, seed: int = 1, box=(0.04, 0.2, 0.04), d: float = 1.0e-3,
+                  steps_dt: float = 2.0e-6, pi: int = 2, pri: int = 2) -> Case:
+    """20k monodisperse LSD spheres on a seeded jittered lattice (pitch 1.2 d,
+    jitter U(-0.1d, 0.1d) per axis, velocity U(-0.05, 0.05) m/s) in a
+    0.04 x 0.2 x 0.04 m box (gravity -y) with a floor and four side walls;
+    Adams-Bashforth 2, dt = 2e-6 s.  Restitution 0.9, friction 0.3, rolling
+    friction 0.1.  The reference's LSD has no direct k_n input: Young's modulus
+    is chosen so that its stiffness K_n*V**0.4 equals 1e4 N/m at V = 0.05 m/s."""
+    rng = np.random.default_rng(seed)
+    pitch = 1.2 * d
+    nxz = int(box[0] / pitch)
+    nzz = int(box[2] / pitch)
+    per_layer = nxz * nzz
+    layers = int(math.ceil(n / per_layer))
+    idx = np.arange(n)
+    iy, rem = np.divmod(idx, per_layer)
+    ix, iz = np.divmod(rem, nzz)
+    pos = np.stack([(ix + 0.5) * pitch + box[0] * 0.0 + (box[0] - nxz * pitch) * 0.5,
+                    (iy + 0.5) * pitch + 0.5 * (pitch - d) * 0.0,
+                    (iz + 0.5) * pitch + (box[2] - nzz * pitch) * 0.5], axis=1)
+    if layers * pitch > box[1]:
+        raise ValueError("box too short for the lattice")
+    pos = pos + rng.uniform(-0.1 * d, 0.1 * d, size=pos.shape)
+    vel = rng.uniform(-0.05, 0.05, size=(n, 3))
+    nu = 0.3
+    E = props.lsd_youngs_for_stiffness(1.0e4, 0.05, d, 2500.0, nu)
+    tables = props.build_tables(props.CFT_LSD, [d], [2500.0], [E], [nu], (0.3, 0.3, 0.1, 0.9, 0.9),
+                                [E], [nu], (0.3, 0.3, 0.1, 0.9, 0.9))
+    opts = Options(dt=steps_dt, minpoint=(0.0, 0.0, 0.0), maxpoint=tuple(box), cf_type=props.CFT_LSD,
+                   pi_method=pi, pri_method=pri)
+    parts = new_particles(pos, np.ones(n, dtype=np.int32), tables.radius, vel, opts.tsize, opts.rsize)
+    walls = box_walls(opts.minpoint, opts.maxpoint, infinite=True, base_wall_id=opts.base_wall_id)
+    return Case(f"lsd_mono_{n}", opts, tables, walls, parts,
+                note=f"LSD E={E:.6g} Pa (k_n(0.05 m/s)=1e4 N/m), nu=0.3, e=0.9, mu=0.3, mu_r=0.1")
+
+
+def hertz_poly_tables(ntypes: int = 41, d_lo: float = 0.8e-3, d_hi: float = 1.2e-3, E: float = 5.0e7,
+                      nu: float = 0.3, e_n: float = 0.8, mu: float = 0.4, mu_r: float = 0.1,
+                      density: float = 2500.0):
+    diam = np.linspace(d_lo, d_hi, ntypes) if ntypes > 1 else np.array([0.5 * (d_lo + d_hi)])
+    coefs = (mu, mu, mu_r, e_n, e_n)
+    tables = props.build_tables(props.CFT_NLIN, list(diam), [density] * ntypes, [E] * ntypes, [nu] * ntypes,
+                                coefs, [E], [nu], coefs)
+    return diam, tables
+
+
+def deposited_positions(rng, diam_of_particle: np.ndarray, box, floor_y: float, overlap: float,
+                        spacing: float, jitter: float):
+    """Layer-by-layer deposition onto a body-centred column grid.
+
+    Even layers sit on the grid (spacing/2 + i*spacing), odd layers on the grid
+    shifted by half a spacing in x and z.  Each sphere (lateral jitter
+    U(-jitter, jitter)) is lowered until it rests on the highest of the floor,
+    the spheres of the layer below and the sphere two layers below in its own
+    column, then sunk by `overlap`.  With spacing >= max diameter + 2*jitter no
+    two spheres of one layer touch.  Returns positions in placement order
+    (bottom layer first)."""
+    n = len(diam_of_particle)
+    r = 0.5 * diam_of_particle
+    pos = np.zeros((n, 3))
+    done = 0
+    layers = []   # per layer: (origin, x, z, y, r) grids with NaN where empty
+    k = 0
+    while done < n:
+        org = 0.5 * spacing + (0.5 * spacing if k % 2 else 0.0)
+        nxl = int((box[0] - org - 0.5 * spacing) / spacing) + 1
+        nzl = int((box[2] - org - 0.5 * spacing) / spacing) + 1
+        cnt = min(nxl * nzl, n - done)
+        gx, gz = np.divmod(np.arange(cnt), nzl)
+        xg = org + gx * spacing
+        zg = org + gz * spacing
+        x = xg + rng.uniform(-jitter, jitter, cnt)
+        z = zg + rng.uniform(-jitter, jitter, cnt)
+        rr = r[done:done + cnt]
+        y = floor_y + rr
+        for back in (1, 2, 3, 4):
+            if len(layers) < back:
+                continue
+            porg, px, pz, py, pr = layers[-back]
+            pnx, pnz = px.shape
+            bx = np.floor((xg - porg) / spacing + 1e-9).astype(np.int64)
+            bz = np.floor((zg - porg) / spacing + 1e-9).astype(np.int64)
+            for dxs in (-1, 0, 1, 2):
+                for dzs in (-1, 0, 1, 2):
+                    qx = bx + dxs
+                    qz = bz + dzs
+                    ok = (qx >= 0) & (qx < pnx) & (qz >= 0) & (qz < pnz)
+                    qx2 = np.clip(qx, 0, pnx - 1)
+                    qz2 = np.clip(qz, 0, pnz - 1)
+                    sy = py[qx2, qz2]
+                    sr = pr[qx2, qz2]
+                    reach = (rr + sr) ** 2 - ((x - px[qx2, qz2]) ** 2 + (z - pz[qx2, qz2]) ** 2)
+                    valid = ok & np.isfinite(sy) & (reach > 0)
+                    y = np.where(valid, np.maximum(y, sy + np.sqrt(np.where(valid, reach, 0.0))), y)
+        y = y - overlap
+        pos[done:done + cnt] = np.stack([x, y, z], axis=1)
+        grids = [np.full((nxl, nzl), np.nan) for _ in range(4)]
+        for g, v in zip(grids, (x, z, y, rr)):
+            g[gx, gz] = v
+        layers.append((org, *grids))
+        done += cnt
+        k += 1
+    if pos[:, 1].max() + r.max() > box[1]:
+        raise ValueError("deposited bed is taller than the box")
+    return pos
+
+
+def hertz_poly_case(n: int = 1_000_000, seed: int = 2, box=(0.1, 0.6, 0.1), ntypes: int = 41,
+                    dt: float = 1.0e-6, overlap: float = 1.0e-6, pi: int = 2, pri: int = 2) -> Case:
+    """Polydisperse Hertz-Mindlin bed: d uniform in [0.8, 1.2] mm realised as
+    `ntypes` discrete types (10 um steps for 41), density 2500 kg/m^3,
+    E = 5e7 Pa, nu = 0.3, restitution 0.8, friction 0.4 (rolling 0.1), in a
+    0.1 x 0.6 x 0.1 m box with a floor and four side walls, dt = 1e-6 s.
+    Positions: seeded deposition onto a body-centred column grid (spacing
+    1.3 mm, lateral jitter 0.05 mm), each sphere resting on its highest support
+    with `overlap` of sink, i.e. a packed bed just after deposition."""
+    rng = np.random.default_rng(seed)
+    diam, tables = hertz_poly_tables(ntypes)
+    ptype = rng.integers(1, ntypes + 1, size=n).astype(np.int32)
+    pos = deposited_positions(rng, diam[ptype - 1], box, 0.0, overlap, spacing=1.3e-3, jitter=0.05e-3)
+    opts = Options(dt=dt, minpoint=(0.0, 0.0, 0.0), maxpoint=tuple(box), cf_type=props.CFT_NLIN,
+                   pi_method=pi, pri_method=pri)
+    vel = np.zeros((n, 3))
+    parts = new_particles(pos, ptype, tables.radius, vel, opts.tsize, opts.rsize)
+    # the reference's index order is unrelated to space (its maker shuffles,
+    # Prtcl_Variables.f90:279-288): shuffle the same way with the seed
+    perm = rng.permutation(n)
+    parts = parts.take(perm)
+    parts.id = np.arange(1, n + 1, dtype=np.int32)
+    walls = box_walls(opts.minpoint, opts.maxpoint, infinite=True, base_wall_id=opts.base_wall_id)
+    return Case(f"hertz_poly_{n}", opts, tables, walls, parts,
+                note="Hertz E=5e7 Pa, nu=0.3, e=0.8, mu=0.4, mu_r=0.1, 41 types d=0.80..1.20 mm")
+
+
+def random_cloud_case(n: int, seed: int, box=(0.01, 0.01, 0.01), ntypes: int = 5, cf_type: int = props.CFT_NLIN,
+                      d_lo: float = 0.8e-3, d_hi: float = 1.2e-3, vmax: float = 0.3, pi: int = 2, pri: int = 2,
+                      dt: float = 1.0e-6, overlap_frac: float = 0.02, density_frac: float = 0.45,
+                      finite_walls: bool = False) -> Case:
+    """Small dense cloud for parity tests: random sequential placement that
+    accepts small overlaps (up to overlap_frac of the smaller diameter), so the
+    first step already has many contacts; random velocities U(-vmax, vmax)
+    and angular velocities."""
+    rng = np.random.default_rng(seed)
+    if cf_type == props.CFT_NLIN:
+        diam, tables = hertz_poly_tables(ntypes, d_lo, d_hi)
+    else:
+        diam = np.linspace(d_lo, d_hi, ntypes) if ntypes > 1 else np.array([d_lo])
+        E = props.lsd_youngs_for_stiffness(1.0e4, 0.05, float(diam.mean()), 2500.0, 0.3)
+        c = (0.3, 0.2, 0.1, 0.9, 0.9)
+        tables = props.build_tables(props.CFT_LSD, list(diam), [2500.0] * ntypes, [E] * ntypes, [0.3] * ntypes,
+                                    c, [E], [0.3], c)
+    ptype = rng.integers(1, ntypes + 1, size=n).astype(np.int32)
+    r = 0.5 * diam[ptype - 1]
+    pos = np.zeros((n, 3))
+    placed = 0
+    tries = 0
+    lo = np.array([0.0, 0.0, 0.0])
+    hi = np.array(box)
+    while placed < n:
+        tries += 1
+        if tries > 200 * n:
+            raise ValueError("random_cloud_case: box too small")
+        p = rng.uniform(lo + r[placed] * 0.9, hi - r[placed] * 0.9)
+        if placed:
+            dd = np.sqrt(((pos[:placed] - p) ** 2).sum(axis=1))
+            lim = r[:placed] + r[placed] - overlap_frac * 2.0 * np.minimum(r[:placed], r[placed])
+            if np.any(dd < lim):
+                continue
+        pos[placed] = p
+        placed += 1
+    vel = rng.uniform(-vmax, vmax, size=(n, 3))
+    opts = Options(dt=dt, minpoint=(0.0, 0.0, 0.0), maxpoint=tuple(box), cf_type=cf_type, pi_method=pi,
+                   pri_method=pri)
+    parts = new_particles(pos, ptype, tables.radius, vel, opts.tsize, opts.rsize)
+    parts.rotVel[:] = rng.uniform(-50.0, 50.0, size=(n, 1, 3))
+    if finite_walls:
+        walls = box_walls(opts.minpoint, opts.maxpoint, infinite=False, base_wall_id=opts.base_wall_id)
+    else:
+        walls = box_walls(opts.minpoint, opts.maxpoint, infinite=True, base_wall_id=opts.base_wall_id)
+    return Case(f"cloud_{n}_{seed}", opts, tables, walls, parts)
+
+
+def scaled(case: Case, **opt_changes) -> Case:
+    return replace(case, opts=replace(case.opts, **opt_changes))

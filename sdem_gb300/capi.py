@@ -1,0 +1,265 @@
+"""ctypes binding of libsdem_gpu.so (include/sdem_gpu.h) and a Python handle.
+
+This is the binding a Python caller (and the test suite) uses; a Fortran
+caller binds the same symbols through ISO_C_BINDING.  Loading fails loudly
+when the library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from .beds import Case, Particles
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsdem_gpu.so")
+
+SDEM_OK = 0
+ERRORS = {1: "SDEM_E_ARG", 2: "SDEM_E_CUDA", 3: "SDEM_E_CL_FULL", 4: "SDEM_E_BAD_ID", 5: "SDEM_E_NCV20",
+          6: "SDEM_E_GRID", 7: "SDEM_E_TIMEOUT", 8: "SDEM_E_CAPACITY", 9: "SDEM_E_NOMEM",
+          10: "SDEM_E_UNSUPPORTED"}
+CNT_NAMES = ("pp", "ppg", "ppfix", "pw", "cnsv", "nlocal", "iter", "next_wall_update")
+
+EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls", "sdem_upload_particles",
+            "sdem_upload_contacts", "sdem_step", "sdem_step_async", "sdem_get_stream",
+            "sdem_download_particles", "sdem_download_contacts", "sdem_check_restart_limit",
+            "sdem_download_forces", "sdem_counters", "sdem_launch_count", "sdem_profile_begin",
+            "sdem_profile_end", "sdem_profile_phase_name", "sdem_last_error", "sdem_destroy")
+
+
+class SdemCfg(C.Structure):
+    """struct sdem_cfg of include/sdem_gpu.h (field order matters)."""
+    _fields_ = [
+        ("n_capacity", C.c_int), ("max_gid", C.c_int), ("tsize", C.c_int), ("rsize", C.c_int),
+        ("cf_type", C.c_int), ("ct_model", C.c_int), ("pi_method", C.c_int), ("pri_method", C.c_int),
+        ("cs_method", C.c_int), ("cntct_list_size", C.c_int), ("base_wall_id", C.c_int),
+        ("wall_max_update_iter", C.c_int), ("periodic", C.c_int * 3), ("quirk_ab2_rot", C.c_int),
+        ("max_contacts_per_particle", C.c_int), ("dt", C.c_double), ("gravity", C.c_double * 3),
+        ("dom_min", C.c_double * 3), ("dom_max", C.c_double * 3), ("cs_ratio", C.c_double),
+        ("wall_neighbor_ratio", C.c_double),
+    ]
+
+
+class SdemError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def cfg_from_case(case: Case, n_capacity: Optional[int] = None, max_gid: Optional[int] = None) -> SdemCfg:
+    o = case.opts
+    c = SdemCfg()
+    c.n_capacity = int(n_capacity or max(case.particles.n, 1))
+    c.max_gid = int(max_gid or case.max_gid)
+    c.tsize, c.rsize = o.tsize, o.rsize
+    c.cf_type, c.ct_model = o.cf_type, o.ct_model
+    c.pi_method, c.pri_method = o.pi_method, o.pri_method
+    c.cs_method = o.cs_method
+    c.cntct_list_size = o.cntct_list_size
+    c.base_wall_id = o.base_wall_id
+    c.wall_max_update_iter = o.wall_max_update_iter
+    for k in range(3):
+        c.periodic[k] = int(o.periodic[k])
+        c.gravity[k] = o.gravity[k]
+        c.dom_min[k] = o.minpoint[k]
+        c.dom_max[k] = o.maxpoint[k]
+    c.quirk_ab2_rot = int(o.quirk_ab2_rot)
+    c.max_contacts_per_particle = int(o.max_contacts_per_particle)
+    c.dt = o.dt
+    c.cs_ratio = o.cs_ratio
+    c.wall_neighbor_ratio = o.wall_neighbor_ratio
+    return c
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Loads the sm_103a library.  Raises if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m sdem_gb300.build` "
+                           "(the GPU path has no fallback)")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int)
+    lib.sdem_default_cfg.argtypes = [C.POINTER(SdemCfg)]
+    lib.sdem_default_cfg.restype = None
+    lib.sdem_create.argtypes = [C.POINTER(SdemCfg), C.POINTER(P)]
+    lib.sdem_set_types.argtypes = [P, C.c_int, dp, dp, dp, dp, C.c_int, dp]
+    lib.sdem_set_walls.argtypes = [P, C.c_int, dp, ip]
+    lib.sdem_upload_particles.argtypes = [P, C.c_int, ip, ip, ip, dp, dp, dp, dp, dp, dp]
+    lib.sdem_upload_contacts.argtypes = [P, C.c_int, ip, ip, dp, dp]
+    lib.sdem_step.argtypes = [P, C.c_int]
+    lib.sdem_step_async.argtypes = [P, C.c_int]
+    lib.sdem_get_stream.argtypes = [P, C.POINTER(P)]
+    lib.sdem_download_particles.argtypes = [P, ip, ip, ip, ip, dp, dp, dp, dp, dp, dp]
+    lib.sdem_download_contacts.argtypes = [P, C.c_int, ip, ip, ip, dp, dp]
+    lib.sdem_check_restart_limit.argtypes = [P]
+    lib.sdem_download_forces.argtypes = [P, dp, dp]
+    lib.sdem_counters.argtypes = [P, ip]
+    lib.sdem_launch_count.argtypes = [P, C.POINTER(C.c_longlong)]
+    lib.sdem_profile_begin.argtypes = [P, C.c_int]
+    lib.sdem_profile_end.argtypes = [P, C.c_int, dp, ip]
+    lib.sdem_profile_phase_name.argtypes = [C.c_int]
+    lib.sdem_profile_phase_name.restype = C.c_char_p
+    lib.sdem_last_error.argtypes = [P]
+    lib.sdem_last_error.restype = C.c_char_p
+    lib.sdem_destroy.argtypes = [P]
+    lib.sdem_destroy.restype = None
+    for name in EXPORTED:
+        if name not in ("sdem_default_cfg", "sdem_last_error", "sdem_destroy", "sdem_profile_phase_name"):
+            getattr(lib, name).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def dptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def iptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class DEMSystem:
+    """One bed on the current GPU, driven through the C ABI."""
+
+    def __init__(self, case: Case, n_capacity: Optional[int] = None, max_gid: Optional[int] = None):
+        self.lib = load()
+        self.case = case
+        self.cfg = cfg_from_case(case, n_capacity, max_gid)
+        self.h = C.c_void_p()
+        rc = self.lib.sdem_create(C.byref(self.cfg), C.byref(self.h))
+        if rc:
+            msg = self.lib.sdem_last_error(self.h).decode() if self.h else ""
+            self.lib.sdem_destroy(self.h)
+            self.h = None
+            raise SdemError(rc, msg)
+        t = case.tables
+        self._check(self.lib.sdem_set_types(self.h, t.n_types, dptr(t.radius), dptr(t.mass), dptr(t.inertia),
+                                            dptr(t.bpp), t.n_wall_types, dptr(t.bpw)))
+        w, f = case.walls.arrays()
+        self._check(self.lib.sdem_set_walls(self.h, case.walls.n, dptr(w) if case.walls.n else None,
+                                            iptr(f) if case.walls.n else None))
+        self.upload(case.particles)
+        if case.contacts is not None:
+            self.upload_contacts(*case.contacts)
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise SdemError(rc, self.lib.sdem_last_error(self.h).decode())
+
+    def upload(self, p: Particles) -> None:
+        a = lambda x: np.ascontiguousarray(x, dtype=np.float64)
+        i = lambda x: np.ascontiguousarray(x, dtype=np.int32)
+        self._keep = (i(p.id), i(p.ptype), i(p.usrmark), a(p.posR), a(p.linVel), a(p.linAcc), a(p.theta),
+                      a(p.rotVel), a(p.rotAcc))
+        k = self._keep
+        self._check(self.lib.sdem_upload_particles(self.h, p.n, iptr(k[0]), iptr(k[1]), iptr(k[2]), dptr(k[3]),
+                                                   dptr(k[4]), dptr(k[5]), dptr(k[6]), dptr(k[7]), dptr(k[8])))
+
+    def upload_contacts(self, owner, partner, tandelta, velrel) -> None:
+        o = np.ascontiguousarray(owner, dtype=np.int32)
+        q = np.ascontiguousarray(partner, dtype=np.int32)
+        t = np.ascontiguousarray(tandelta, dtype=np.float64)
+        v = np.ascontiguousarray(velrel, dtype=np.float64)
+        self._check(self.lib.sdem_upload_contacts(self.h, len(o), iptr(o), iptr(q), dptr(t), dptr(v)))
+
+    def step(self, n: int = 1) -> None:
+        self._check(self.lib.sdem_step(self.h, int(n)))
+
+    def step_async(self, n: int = 1) -> None:
+        self._check(self.lib.sdem_step_async(self.h, int(n)))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self.lib.sdem_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def state(self) -> Particles:
+        cap = self.cfg.n_capacity
+        ts, rs = self.cfg.tsize, self.cfg.rsize
+        n = C.c_int()
+        out = Particles(np.zeros(cap, np.int32), np.zeros(cap, np.int32), np.zeros(cap, np.int32),
+                        np.zeros((cap, 4)), np.zeros((cap, ts, 3)), np.zeros((cap, ts, 3)), np.zeros((cap, 3)),
+                        np.zeros((cap, rs, 3)), np.zeros((cap, rs, 3)))
+        self._check(self.lib.sdem_download_particles(self.h, C.byref(n), iptr(out.id), iptr(out.ptype),
+                                                     iptr(out.usrmark), dptr(out.posR), dptr(out.linVel),
+                                                     dptr(out.linAcc), dptr(out.theta), dptr(out.rotVel),
+                                                     dptr(out.rotAcc)))
+        return out.take(slice(0, n.value))
+
+    def forces(self):
+        n = self.counters()["nlocal"]
+        F = np.zeros((max(n, 1), 3))
+        T = np.zeros((max(n, 1), 3))
+        self._check(self.lib.sdem_download_forces(self.h, dptr(F), dptr(T)))
+        return F[:n], T[:n]
+
+    def contacts(self):
+        nc = C.c_int()
+        self._check(self.lib.sdem_download_contacts(self.h, 0, C.byref(nc), None, None, None, None))
+        m = nc.value
+        o = np.zeros(max(m, 1), np.int32)
+        q = np.zeros(max(m, 1), np.int32)
+        t = np.zeros((max(m, 1), 3))
+        v = np.zeros(max(m, 1))
+        self._check(self.lib.sdem_download_contacts(self.h, max(m, 1), C.byref(nc), iptr(o), iptr(q), dptr(t),
+                                                    dptr(v)))
+        return o[:m], q[:m], t[:m], v[:m]
+
+    def launch_count(self) -> int:
+        n = C.c_longlong()
+        self._check(self.lib.sdem_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def profile_begin(self, max_steps: int) -> None:
+        self._check(self.lib.sdem_profile_begin(self.h, int(max_steps)))
+
+    def profile_end(self) -> tuple:
+        """-> ({phase: summed ms}, steps timed)"""
+        ms = np.zeros(32)
+        ns = C.c_int()
+        k = self.lib.sdem_profile_end(self.h, 32, dptr(ms), C.byref(ns))
+        if k <= 0:
+            raise SdemError(k, self.lib.sdem_last_error(self.h).decode())
+        names = [self.lib.sdem_profile_phase_name(i).decode() for i in range(k)]
+        return dict(zip(names, ms[:k].tolist())), ns.value
+
+    def check_restart_limit(self) -> None:
+        self._check(self.lib.sdem_check_restart_limit(self.h))
+
+    def counters(self) -> dict:
+        out = np.zeros(8, np.int32)
+        self._check(self.lib.sdem_counters(self.h, iptr(out)))
+        return dict(zip(CNT_NAMES, (int(x) for x in out)))
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.sdem_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

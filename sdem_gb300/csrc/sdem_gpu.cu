@@ -1,0 +1,1616 @@
+// sdem_gpu.cu -- GB300 (sm_103a) kernels and C ABI for sDEM's per-step
+// particle hot path.  Build: nvcc -gencode arch=compute_103a,code=sm_103a
+// -O3 -fmad=false (see sdem_gb300/build.py).
+//
+// One step (the body of DEMS_iterate, Prtcl_DEMSystem.f90:214-247) is:
+//   k_wall_refresh/k_wall_refresh_end  UpdateNearPrtclsPW (Prtcl_ContactSearchPW.f90:159-235),
+//                                      device-predicated on iter >= Next_iter_update
+//   k_bin, scan, k_scatter, k_cellorder
+//                                      NBSM_clcBoxIndex + Y/X/Z lists (Prtcl_NBS_Munjiza.f90:163-296)
+//                                      as a counting sort; within a cell particles are ordered by
+//                                      decreasing index, the order the reference's Z lists walk
+//   k_search                           LoopNBSMask + FineSearch2 (:302-473, :503-530): one thread per
+//                                      target particle, same 13-cell half shell + same-cell tail, same
+//                                      exact FP64 overlap test; contacts go to the target's row (in visit
+//                                      order) and an entry (target, slot) to the partner's in-list
+//   scan, k_gid_index                  row offsets (CSR) and per-id row tables for the next step's
+//                                      history lookup
+//   k_force                            Find_insert history lookup + ContactForce_PP
+//                                      (Prtcl_CL_and_CF.f90:142-168, 256-296, 732-756): one thread per
+//                                      contact, full warps of FP64 work
+//   k_gather_integrate                 per particle, sums its contact records in the reference's scatter
+//                                      order (a deterministic gather), then wall contacts
+//                                      (FindContactsPW, :298-319) in near-list order, clc_Acceleration
+//                                      (Prtcl_DEMSystem.f90:166-181) and Prtcl_Integrate
+//                                      (Prtcl_Integration.f90:15-88)
+//   k_delete, k_apply_moves            one-rank out-of-domain delete (Prtcl_Comm.f90:1569-1840)
+//   k_step_end                         iterNumber += 1, counters
+// RemvReleased/PreIteration have no kernel: the history of step n+1 is exactly
+// the contact records written at step n (double-buffered, keyed by particle id).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sdem_gpu.h"
+#include "dem_device.cuh"
+
+using sdem::dbl4;
+using sdem::make_dbl4;
+using sdem::r3;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxK = 64;         // row / in-list capacity limit (6-bit slot in the in-list key)
+constexpr int kKw = 4;            // wall contacts per particle
+constexpr int kMaxWalls = 64;     // near-wall mask is 64 bits
+constexpr int kOutCap = 4096;     // out-of-domain deletions per step
+constexpr int kScanTile = 4096;   // elements per scan block (1024 threads x 4)
+
+// Phases of one step, for the optional per-phase timing (sdem_profile_*).
+enum Phase { PH_WALL, PH_BIN, PH_SCAN_CELLS, PH_SCATTER, PH_CELLORDER, PH_SEARCH, PH_SCAN_ROWS, PH_GID_INDEX,
+             PH_FORCE, PH_GATHER, PH_DELETE, PH_END, kPhases };
+const char* const kPhaseNames[kPhases] = {"wall_refresh", "bin", "scan_cells", "scatter", "cellorder", "search",
+                                          "scan_rows", "gid_index", "force", "gather_integrate", "delete",
+                                          "step_end"};
+
+// ---------------------------------------------------------------------------
+// Device view of one handle, passed by value to every kernel.
+struct Dev {
+  int ncap, n_launch;
+  int* n;  // device particle count (changes on deletion)
+  int max_gid, K, Kin, ccap;
+  int tsize, rsize, pi, pri, quirk;
+  sdem::LawCfg law;
+  double3 g;
+  double cell, x0, y0, z0;
+  int nx, ny, nz;
+  long long ncell;
+  double3 dmin, dmax;
+  // tables
+  int nT, nWT;
+  const double *radius, *mass, *inertia, *bpp, *bpw;
+  int nw;
+  const double* walls;
+  const int* wflags;
+  double dx1, dx2, max_wall_vel;
+  int wall_max_update_iter;
+  // particle state
+  int *gid, *ptype, *usrmark;
+  dbl4* posr;
+  dbl4 *vel0, *vel1, *vel2, *acc0, *acc1, *acc2;
+  dbl4 *theta, *rv0, *rv1, *rv2, *ra0, *ra1, *ra2;
+  dbl4 *F, *T;
+  unsigned long long* near_mask;
+  // binning
+  int *cell_of, *cell_cnt, *cell_start, *tmp_rank, *tmp_sorted, *sorted, *sortpos;
+  // rows and in-lists
+  int *row_cnt, *row_partner, *row_off;
+  double* row_ovl;
+  int* in_cnt;
+  unsigned* in_list;
+  // contact records
+  int *c_ogid, *c_pgid;
+  const int* c_pgid_prev;
+  dbl4* c_hist;
+  const dbl4* c_hist_prev;
+  dbl4 *c_S, *c_M, *c_Mr;
+  int *sbg, *cbg;
+  const int *sbg_prev, *cbg_prev;
+  int *wh_cnt, *wh_wall;
+  dbl4* wh_hist;
+  const int *wh_cnt_prev, *wh_wall_prev;
+  const dbl4* wh_hist_prev;
+  // status and scalars
+  int* status;                    // [0] error code, [1] detail
+  unsigned long long* counters;   // [0] candidates, [1] PW contacts
+  unsigned long long* red;        // [0] max |v| bits, [1] max |a| bits
+  int* iter;
+  int* next_update;
+  int* out_cnt;
+  int* out_list;
+  int* moves;      // [0] count, then (dst, src) pairs
+  int* map_pos;    // deletion scratch
+  int* map_id;
+};
+
+__device__ __forceinline__ void raise(const Dev& d, int code, int detail) {
+  if (atomicCAS(d.status, 0, code) == 0) d.status[1] = detail;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of int32 (n elements) into out[0..n], out[n] = total.
+__global__ void k_scan_reduce(const int* __restrict__ in, long long n, int* __restrict__ bsum) {
+  __shared__ int warp_sums[32];
+  long long base = (long long)blockIdx.x * kScanTile;
+  int s = 0;
+  for (int k = 0; k < 4; k++) {
+    long long i = base + (long long)k * 1024 + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int v = warp_sums[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = v;
+  }
+}
+
+__device__ __forceinline__ int block_exclusive_scan_1024(int v, int* sh, int* total) {
+  // inclusive warp scan
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0;
+    int z = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += y;
+    }
+    sh[lane] = z - w;  // exclusive warp offsets
+    if (lane == 31) sh[32] = z;
+  }
+  __syncthreads();
+  int r = sh[wid] + x - v;
+  *total = sh[32];
+  __syncthreads();
+  return r;
+}
+
+__global__ void k_scan_blocks(int* bsum, int nb) {
+  __shared__ int sh[33];
+  int carry = 0;
+  for (int base = 0; base < nb; base += 1024) {
+    int i = base + threadIdx.x;
+    int v = (i < nb) ? bsum[i] : 0;
+    int tot;
+    int e = block_exclusive_scan_1024(v, sh, &tot);
+    if (i < nb) bsum[i] = e + carry;
+    carry += tot;
+  }
+}
+
+__global__ void k_scan_apply(const int* __restrict__ in, long long n, const int* __restrict__ bsum,
+                             int* __restrict__ out) {
+  __shared__ int sh[33];
+  long long base = (long long)blockIdx.x * kScanTile;
+  int carry = bsum[blockIdx.x];
+  for (int k = 0; k < 4; k++) {
+    long long i = base + (long long)k * 1024 + threadIdx.x;
+    int v = (i < n) ? in[i] : 0;
+    int tot;
+    int e = block_exclusive_scan_1024(v, sh, &tot);
+    if (i < n) out[i] = carry + e;
+    carry += tot;
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = carry;
+}
+
+// ---------------------------------------------------------------------------
+// UpdateNearPrtclsPW (Prtcl_ContactSearchPW.f90:159-235): near-wall bit mask per
+// particle (walls whose AABB +- DeltaXmax2 holds the particle), max |v|, max |a|.
+__global__ void k_wall_refresh(Dev d) {
+  if (*d.iter < *d.next_update) return;
+  int n = *d.n;
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  double vmax = 0.0, amax = 0.0;
+  if (p < n) {
+    dbl4 P = d.posr[p];
+    unsigned long long mask = 0ull;
+    for (int k = 0; k < d.nw; k++) {
+      const double* r = d.walls + k * SDEM_W_SIZE;
+      double pminx = r[SDEM_W_MIN] - d.dx2, pminy = r[SDEM_W_MIN + 1] - d.dx2, pminz = r[SDEM_W_MIN + 2] - d.dx2;
+      double pmaxx = r[SDEM_W_MAX] + d.dx2, pmaxy = r[SDEM_W_MAX + 1] + d.dx2, pmaxz = r[SDEM_W_MAX + 2] + d.dx2;
+      if (P.x >= pminx && P.x <= pmaxx && P.y >= pminy && P.y <= pmaxy && P.z >= pminz && P.z <= pmaxz)
+        mask |= (1ull << k);
+    }
+    d.near_mask[p] = mask;
+    vmax = sdem::norm3(sdem::xyz(d.vel0[p]));
+    amax = sdem::norm3(sdem::xyz(d.acc0[p]));
+  }
+  // non-negative doubles order like their bit patterns
+  for (int o = 16; o > 0; o >>= 1) {
+    vmax = fmax(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+    amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&d.red[0], (unsigned long long)__double_as_longlong(vmax));
+    atomicMax(&d.red[1], (unsigned long long)__double_as_longlong(amax));
+  }
+}
+
+__global__ void k_wall_refresh_end(Dev d) {
+  int it = *d.iter;
+  if (it < *d.next_update) return;
+  double max_v = __longlong_as_double((long long)d.red[0]);
+  double max_a = __longlong_as_double((long long)d.red[1]);
+  d.red[0] = 0ull;
+  d.red[1] = 0ull;
+  max_v = max_v + d.max_wall_vel;
+  max_v = (max_v > 0.3) ? max_v : 0.3;
+  max_v = max_v * 1.5;
+  double gn = sdem::norm3(sdem::mk3(d.g.x, d.g.y, d.g.z));
+  max_a = (max_a > gn) ? max_a : gn;
+  max_a = max_a * 1.5;
+  double t = (sqrt(max_v * max_v + 2.0 * max_a * d.dx1) - max_v) / max_a;
+  int numIter = (int)(t / d.law.dt);
+  numIter = numIter > 1 ? numIter : 1;
+  numIter = numIter < d.wall_max_update_iter ? numIter : d.wall_max_update_iter;
+  *d.next_update = it + numIter;
+}
+
+// ---------------------------------------------------------------------------
+// Binning: NBSM_clcBoxIndex (Prtcl_NBS_Munjiza.f90:193-198) + counting sort.
+// Linear cell key orders cells as the reference's sweep visits them:
+// row iy (outer), column ix, cell iz (inner).
+__global__ void k_bin(Dev d) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *d.n) return;
+  dbl4 P = d.posr[p];
+  double rpdx = P.x - d.x0, rpdy = P.y - d.y0, rpdz = P.z - d.z0;
+  double fx = floor(rpdx / d.cell), fy = floor(rpdy / d.cell), fz = floor(rpdz / d.cell);
+  // grid index is floor()+1 in [1, n]; 0-based here
+  if (!(fx >= 0.0 && fx < (double)d.nx && fy >= 0.0 && fy < (double)d.ny && fz >= 0.0 && fz < (double)d.nz)) {
+    raise(d, SDEM_E_GRID, p);
+    d.cell_of[p] = -1;
+    return;
+  }
+  long long key = ((long long)fy * d.nx + (long long)fx) * d.nz + (long long)fz;
+  d.cell_of[p] = (int)key;
+  d.tmp_rank[p] = atomicAdd(&d.cell_cnt[key], 1);
+}
+
+__global__ void k_scatter(Dev d) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *d.n) return;
+  int key = d.cell_of[p];
+  if (key < 0) return;
+  d.tmp_sorted[d.cell_start[key] + d.tmp_rank[p]] = p;
+}
+
+// Deterministic order inside a cell: decreasing particle index (the reference
+// pushes Y, X and Z lists front-first, Prtcl_NBS_Munjiza.f90:224-271).
+__global__ void k_cellorder(Dev d) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *d.n) return;
+  int key = d.cell_of[p];
+  if (key < 0) return;
+  int a = d.cell_start[key], b = d.cell_start[key + 1];
+  int rank = 0;
+  for (int t = a; t < b; t++) rank += (d.tmp_sorted[t] > p);
+  d.sorted[a + rank] = p;
+  d.sortpos[p] = a + rank;
+}
+
+// ---------------------------------------------------------------------------
+// NBSM_LoopNBSMask + NBSM_FineSearch2 for one target (one thread per sort
+// position s).  Visit order per target: the tail of its own cell, then
+// (ix,iy,iz-1), (ix-1,iy,iz-1..iz+1), then row iy-1: columns ix-1..ix+1,
+// cells iz-1..iz+1 -- the order of Prtcl_NBS_Munjiza.f90:409-468.
+__global__ void k_search(Dev d) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = *d.n;
+  unsigned long long cand = 0;
+  if (s < d.n_launch) {
+    if (s >= n) {
+      d.row_cnt[s] = 0;
+    } else {
+      int m = d.sorted[s];
+      int key = d.cell_of[m];
+      int iz = key % d.nz;
+      int rest = key / d.nz;
+      int ix = rest % d.nx;
+      int iy = rest / d.nx;
+      dbl4 Pm = d.posr[m];
+      int cnt = 0;
+      const int K = d.K, Kin = d.Kin, ncap = d.ncap;
+      auto test = [&](int t) {
+        int q = d.sorted[t];
+        dbl4 Pq = d.posr[q];
+        double dr = Pm.w + Pq.w;
+        double dr2 = dr * dr;
+        double dx = Pm.x - Pq.x;
+        double d2sum = dx * dx;
+        if (d2sum > dr2) return;
+        double dy = Pm.y - Pq.y;
+        d2sum = dy * dy + d2sum;
+        if (d2sum > dr2) return;
+        double dz = Pm.z - Pq.z;
+        d2sum = dz * dz + d2sum;
+        if (d2sum > dr2) return;
+        double ovrlp = dr - sqrt(d2sum);
+        if (cnt < K) {
+          d.row_partner[(size_t)cnt * ncap + s] = q;
+          d.row_ovl[(size_t)cnt * ncap + s] = ovrlp;
+          int slot = atomicAdd(&d.in_cnt[q], 1);
+          if (slot < Kin) d.in_list[(size_t)slot * ncap + q] = ((unsigned)s << 6) | (unsigned)cnt;
+          else raise(d, SDEM_E_CL_FULL, q);
+        } else {
+          raise(d, SDEM_E_CL_FULL, m);
+        }
+        cnt++;
+      };
+      // same cell, particles after the target in list order
+      {
+        int b = d.cell_start[key + 1];
+        for (int t = s + 1; t < b; t++) test(t);
+        cand += (unsigned long long)(b - s - 1);
+      }
+      auto visit = [&](int cx, int cy, int cz) {
+        if (cx < 0 || cx >= d.nx || cy < 0 || cz < 0 || cz >= d.nz) return;
+        long long k2 = ((long long)cy * d.nx + cx) * d.nz + cz;
+        int a = d.cell_start[k2], b = d.cell_start[k2 + 1];
+        for (int t = a; t < b; t++) test(t);
+        cand += (unsigned long long)(b - a);
+      };
+      visit(ix, iy, iz - 1);
+      visit(ix - 1, iy, iz - 1);
+      visit(ix - 1, iy, iz);
+      visit(ix - 1, iy, iz + 1);
+      for (int lx = -1; lx <= 1; lx++)
+        for (int i = -1; i <= 1; i++) visit(ix + lx, iy - 1, iz + i);
+      d.row_cnt[s] = cnt < K ? cnt : K;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) cand += __shfl_down_sync(0xffffffffu, cand, o);
+  if ((threadIdx.x & 31) == 0 && cand) atomicAdd(&d.counters[0], cand);
+}
+
+// Per-id index of this step's rows, used by the next step's history lookup.
+__global__ void k_gid_index(Dev d) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= *d.n) return;
+  int g = d.gid[d.sorted[s]];
+  d.sbg[g] = d.row_off[s];
+  d.cbg[g] = d.row_cnt[s];
+}
+
+// ---------------------------------------------------------------------------
+// One thread per contact: Find_insert's history lookup + ContactForce_PP.
+__device__ __forceinline__ int find_row(const int* __restrict__ off, int n, int c) {
+  int lo = 0, hi = n;  // off[lo] <= c < off[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (off[mid] <= c) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kThreads) k_force(Dev d) {
+  const int n = *d.n;
+  const int C = d.row_off[d.n_launch];
+  if (C > d.ccap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) raise(d, SDEM_E_CL_FULL, C);
+    return;
+  }
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+    int s = find_row(d.row_off, n, c);
+    int slot = c - d.row_off[s];
+    int m = d.sorted[s];
+    int q = d.row_partner[(size_t)slot * d.ncap + s];
+    double ovrlp = d.row_ovl[(size_t)slot * d.ncap + s];
+    int gm = d.gid[m], gq = d.gid[q];
+    // Find_insert: history of the pair from the previous step (either particle
+    // may have been its target then), else a new contact (TanDelta 0, VelRel -2).
+    dbl4 hist = make_dbl4(0.0, 0.0, 0.0, -2.0);
+    {
+      int a = d.sbg_prev[gm], k = d.cbg_prev[gm];
+      bool found = false;
+      for (int j = 0; j < k; j++)
+        if (d.c_pgid_prev[a + j] == gq) { hist = d.c_hist_prev[a + j]; found = true; break; }
+      if (!found) {
+        a = d.sbg_prev[gq];
+        k = d.cbg_prev[gq];
+        for (int j = 0; j < k; j++)
+          if (d.c_pgid_prev[a + j] == gm) { hist = d.c_hist_prev[a + j]; break; }
+      }
+    }
+    // the lower id is particle i of the pair (FineSearch2, Prtcl_NBS_Munjiza.f90:525-529)
+    bool m_lo = gm < gq;
+    int pid = m_lo ? m : q, pjd = m_lo ? q : m;
+    const double* P = d.bpp + ((size_t)(d.ptype[pjd] - 1) * d.nT + (d.ptype[pid] - 1)) * SDEM_BP_SIZE;
+    dbl4 Pi = d.posr[pid], Pj = d.posr[pjd];
+    r3 Norm_v = sdem::nv3(sdem::sub3(sdem::xyz(Pj), sdem::xyz(Pi)));
+    r3 S, M, Mr;
+    sdem::force_law(d.law, P, sdem::xyz(d.vel0[pid]), sdem::xyz(d.vel0[pjd]), sdem::xyz(d.rv0[pid]),
+                    sdem::xyz(d.rv0[pjd]), Pi.w, Pj.w, Norm_v, ovrlp, hist, S, M, Mr);
+    d.c_ogid[c] = gm;
+    d.c_pgid[c] = gq;
+    d.c_hist[c] = hist;
+    d.c_S[c] = sdem::d4(S, m_lo ? 1.0 : 0.0);  // .w: is the row's target particle i
+    d.c_M[c] = sdem::d4(M, 0.0);
+    d.c_Mr[c] = sdem::d4(Mr, 0.0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per particle: contact sums in the reference's scatter order, walls,
+// acceleration and Adams-Bashforth update.
+//
+// Order: the reference adds each pair's force to both particles when the pair
+// is visited.  Pairs that hold particle p are visited (a) as the partner of an
+// earlier target of p's own cell, (b) as p's own target row, (c) as the partner
+// of targets in later cells; (a) and (c) are ordered by (target sort position,
+// slot), which is exactly the packed in-list key, and (b) is the row order.
+__global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *d.n) return;
+  const int ncap = d.ncap;
+  const int s = d.sortpos[p];
+  const dbl4 Pp = d.posr[p];
+  const double ri = Pp.w;
+  r3 F = sdem::mk3(0.0, 0.0, 0.0), T = sdem::mk3(0.0, 0.0, 0.0);
+
+  auto apply = [&](int c, bool p_lo) {
+    dbl4 S = d.c_S[c], M = d.c_M[c], Mr = d.c_Mr[c];
+    r3 Ms = sdem::scale3(sdem::xyz(M), ri);
+    if (p_lo) {
+      F = sdem::add3(F, sdem::xyz(S));
+      T = sdem::add3(sdem::add3(T, Ms), sdem::xyz(Mr));
+    } else {
+      F = sdem::sub3(F, sdem::xyz(S));
+      T = sdem::sub3(sdem::add3(T, Ms), sdem::xyz(Mr));
+    }
+  };
+
+  unsigned e[kMaxK];
+  int nin = d.in_cnt[p];
+  if (nin > d.Kin) nin = d.Kin;
+  for (int k = 0; k < nin; k++) {
+    unsigned v = d.in_list[(size_t)k * ncap + p];
+    int j = k - 1;
+    while (j >= 0 && e[j] > v) { e[j + 1] = e[j]; j--; }
+    e[j + 1] = v;
+  }
+  int k = 0;
+  for (; k < nin && (int)(e[k] >> 6) < s; k++) {
+    int c = d.row_off[e[k] >> 6] + (int)(e[k] & 63u);
+    apply(c, d.c_S[c].w == 0.0);
+  }
+  {
+    int a = d.row_off[s], cnt = d.row_cnt[s];
+    for (int j = 0; j < cnt; j++) apply(a + j, d.c_S[a + j].w != 0.0);
+  }
+  for (; k < nin; k++) {
+    int c = d.row_off[e[k] >> 6] + (int)(e[k] & 63u);
+    apply(c, d.c_S[c].w == 0.0);
+  }
+
+  // walls: FindContactsPW walks the near list front-first, i.e. highest wall first
+  const dbl4 v1 = d.vel0[p];
+  const dbl4 w1 = d.rv0[p];
+  const int g = d.gid[p];
+  const int ti = d.ptype[p];
+  int nwc = 0;
+  unsigned long long mask = d.near_mask[p];
+  if (mask) {
+    int pc = d.wh_cnt_prev[g];
+    for (int wi = d.nw - 1; wi >= 0; wi--) {
+      if (!((mask >> wi) & 1ull)) continue;
+      sdem::Wall W = sdem::load_wall(d.walls, d.wflags, wi);
+      double ovrlp;
+      r3 nv;
+      if (!sdem::wall_contact(W, Pp, ovrlp, nv)) continue;
+      dbl4 hist = make_dbl4(0.0, 0.0, 0.0, -2.0);
+      for (int j = 0; j < pc; j++)
+        if (d.wh_wall_prev[(size_t)g * kKw + j] == wi) { hist = d.wh_hist_prev[(size_t)g * kKw + j]; break; }
+      const double* P = d.bpw + ((size_t)(W.wall_type - 1) * d.nT + (ti - 1)) * SDEM_BP_SIZE;
+      r3 S, M, Mr;
+      r3 Norm_v = sdem::scale3(nv, -1.0);
+      sdem::force_law(d.law, P, sdem::xyz(v1), W.vel, sdem::xyz(w1), sdem::mk3(0.0, 0.0, 0.0), ri,
+                      1.00E20 * ri, Norm_v, ovrlp, hist, S, M, Mr);
+      F = sdem::add3(F, S);
+      T = sdem::add3(sdem::add3(T, sdem::scale3(M, ri)), Mr);
+      if (nwc < kKw) {
+        d.wh_wall[(size_t)g * kKw + nwc] = wi;
+        d.wh_hist[(size_t)g * kKw + nwc] = hist;
+      } else {
+        raise(d, SDEM_E_CL_FULL, p);
+      }
+      nwc++;
+    }
+  }
+  d.wh_cnt[g] = nwc < kKw ? nwc : kKw;
+  if (nwc) atomicAdd(&d.counters[1], (unsigned long long)nwc);
+  d.F[p] = sdem::d4(F, 0.0);
+  d.T[p] = sdem::d4(T, 0.0);
+
+  // clc_Acceleration, Prtcl_DEMSystem.f90:174-180
+  const double Mass = d.mass[ti - 1], Inertia = d.inertia[ti - 1];
+  r3 a1 = sdem::add3(sdem::div3(F, Mass), sdem::mk3(d.g.x, d.g.y, d.g.z));
+  r3 al1 = sdem::div3(T, Inertia);
+  const double dt = d.law.dt;
+  const double AB2C1 = 3.0 / 2.0, AB2C2 = -1.0 / 2.0;
+  const double AB3C1 = 23.0 / 12.0, AB3C2 = -16.0 / 12.0, AB3C3 = 5.0 / 12.0;
+
+  // Prtcl_Integrate, linear part (Prtcl_Integration.f90:25-53)
+  r3 x = sdem::xyz(Pp);
+  r3 lv1 = sdem::xyz(v1);
+  r3 lv1_new;
+  if (d.pi == SDEM_PIM_FE) {
+    x = sdem::add3(x, sdem::scale3(lv1, dt));
+    lv1_new = sdem::add3(lv1, sdem::scale3(a1, dt));
+    d.acc0[p] = sdem::d4(a1, 0.0);
+  } else if (d.pi == SDEM_PIM_AB2) {
+    r3 lv2 = sdem::xyz(d.vel1[p]);
+    r3 la2 = sdem::xyz(d.acc1[p]);
+    x = sdem::add3(x, sdem::scale3(sdem::add3(sdem::scale3(lv1, AB2C1), sdem::scale3(lv2, AB2C2)), dt));
+    lv1_new = sdem::add3(lv1, sdem::scale3(sdem::add3(sdem::scale3(a1, AB2C1), sdem::scale3(la2, AB2C2)), dt));
+    d.vel1[p] = sdem::d4(lv1, 0.0);
+    d.acc1[p] = sdem::d4(a1, 0.0);
+    d.acc0[p] = sdem::d4(a1, 0.0);
+  } else {
+    r3 lv2 = sdem::xyz(d.vel1[p]), lv3 = sdem::xyz(d.vel2[p]);
+    r3 la2 = sdem::xyz(d.acc1[p]), la3 = sdem::xyz(d.acc2[p]);
+    x = sdem::add3(x, sdem::scale3(sdem::add3(sdem::add3(sdem::scale3(lv1, AB3C1), sdem::scale3(lv2, AB3C2)),
+                                              sdem::scale3(lv3, AB3C3)), dt));
+    lv1_new = sdem::add3(lv1, sdem::scale3(sdem::add3(sdem::add3(sdem::scale3(a1, AB3C1), sdem::scale3(la2, AB3C2)),
+                                                      sdem::scale3(la3, AB3C3)), dt));
+    d.vel2[p] = sdem::d4(lv2, 0.0);
+    d.vel1[p] = sdem::d4(lv1, 0.0);
+    d.acc2[p] = sdem::d4(la2, 0.0);
+    d.acc1[p] = sdem::d4(a1, 0.0);
+    d.acc0[p] = sdem::d4(a1, 0.0);
+  }
+  d.vel0[p] = sdem::d4(lv1_new, 0.0);
+  d.posr[p] = sdem::d4(x, Pp.w);
+
+  // rotational part (Prtcl_Integration.f90:55-86)
+  r3 th = sdem::xyz(d.theta[p]);
+  r3 rw1 = sdem::xyz(w1);
+  if (d.pri == SDEM_PIM_FE) {
+    th = sdem::add3(th, sdem::scale3(rw1, dt));
+    d.rv0[p] = sdem::d4(sdem::add3(rw1, sdem::scale3(al1, dt)), 0.0);
+    d.ra0[p] = sdem::d4(al1, 0.0);
+  } else if (d.pri == SDEM_PIM_AB2) {
+    // Prtcl_Integration.f90:64 starts from GPrtcl_linVel(1,i), already updated
+    r3 wa = d.quirk ? lv1_new : rw1;
+    r3 rw2 = sdem::xyz(d.rv1[p]);
+    r3 ra2 = sdem::xyz(d.ra1[p]);
+    th = sdem::add3(th, sdem::scale3(sdem::add3(sdem::scale3(wa, AB2C1), sdem::scale3(rw2, AB2C2)), dt));
+    d.rv0[p] = sdem::d4(sdem::add3(wa, sdem::scale3(sdem::add3(sdem::scale3(al1, AB2C1), sdem::scale3(ra2, AB2C2)), dt)), 0.0);
+    d.rv1[p] = sdem::d4(wa, 0.0);
+    d.ra1[p] = sdem::d4(al1, 0.0);
+    d.ra0[p] = sdem::d4(al1, 0.0);
+  } else {
+    r3 rw2 = sdem::xyz(d.rv1[p]), rw3 = sdem::xyz(d.rv2[p]);
+    r3 ra2 = sdem::xyz(d.ra1[p]), ra3 = sdem::xyz(d.ra2[p]);
+    th = sdem::add3(th, sdem::scale3(sdem::add3(sdem::add3(sdem::scale3(rw1, AB3C1), sdem::scale3(rw2, AB3C2)),
+                                                sdem::scale3(rw3, AB3C3)), dt));
+    d.rv0[p] = sdem::d4(sdem::add3(rw1, sdem::scale3(sdem::add3(sdem::add3(sdem::scale3(al1, AB3C1), sdem::scale3(ra2, AB3C2)),
+                                                                sdem::scale3(ra3, AB3C3)), dt)), 0.0);
+    d.rv2[p] = sdem::d4(rw2, 0.0);
+    d.rv1[p] = sdem::d4(rw1, 0.0);
+    d.ra2[p] = sdem::d4(ra2, 0.0);
+    d.ra1[p] = sdem::d4(al1, 0.0);
+    d.ra0[p] = sdem::d4(al1, 0.0);
+  }
+  d.theta[p] = sdem::d4(th, 0.0);
+
+  // out-of-domain candidates for the delete passes (Prtcl_Comm.f90:1569-1840)
+  if (x.y >= d.dmax.y || x.y < d.dmin.y || x.x >= d.dmax.x || x.x < d.dmin.x || x.z >= d.dmax.z ||
+      x.z < d.dmin.z) {
+    int k2 = atomicAdd(d.out_cnt, 1);
+    if (k2 < kOutCap) d.out_list[k2] = p;
+    else raise(d, SDEM_E_CAPACITY, p);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One-rank delete of particles outside [min,max), y pencil, five passes of
+// swap-with-last (Prtcl_Comm.f90:1569-1840).  Single thread; runs on the few
+// candidates only (positions of untouched particles equal their index).
+__device__ __forceinline__ bool out_pass(const Dev& d, int id, int pass) {
+  dbl4 P = d.posr[id];
+  switch (pass) {
+    case 0: return P.y >= d.dmax.y || P.y < d.dmin.y;
+    case 1: return P.x >= d.dmax.x;
+    case 2: return P.x < d.dmin.x;
+    case 3: return P.z >= d.dmax.z;
+    default: return P.z < d.dmin.z;
+  }
+}
+
+__global__ void k_delete(Dev d) {
+  int U = *d.out_cnt;
+  d.moves[0] = 0;
+  if (U == 0) return;
+  if (U > kOutCap) return;  // already raised
+  int* L = d.out_list;
+  for (int i = 1; i < U; i++) {  // ascending original index
+    int v = L[i], j = i - 1;
+    while (j >= 0 && L[j] > v) { L[j + 1] = L[j]; j--; }
+    L[j + 1] = v;
+  }
+  int n = *d.n;
+  int nm = 0;  // map: position -> particle (original index) for touched positions
+  auto content = [&](int pos) -> int {
+    for (int j = nm - 1; j >= 0; j--)
+      if (d.map_pos[j] == pos) return d.map_id[j];
+    return pos;
+  };
+  auto set = [&](int pos, int id) {
+    for (int j = nm - 1; j >= 0; j--)
+      if (d.map_pos[j] == pos) { d.map_id[j] = id; return; }
+    d.map_pos[nm] = pos;
+    d.map_id[nm] = id;
+    nm++;
+  };
+  auto where = [&](int id) -> int {  // current position of a candidate, -1 if gone
+    for (int j = nm - 1; j >= 0; j--)
+      if (d.map_id[j] == id && d.map_pos[j] < n) return d.map_pos[j];
+    if (id < n && content(id) == id) return id;
+    return -1;
+  };
+  int* B = d.moves + 1 + 2 * (5 * kOutCap);  // scratch after the move list
+  for (int pass = 0; pass < 5; pass++) {
+    int nb = 0;
+    for (int i = 0; i < U; i++) {
+      int id = L[i];
+      if (!out_pass(d, id, pass)) continue;
+      int pos = where(id);
+      if (pos < 0) continue;
+      int j = nb - 1;
+      while (j >= 0 && B[j] > pos) { B[j + 1] = B[j]; j--; }
+      B[j + 1] = pos;
+      nb++;
+    }
+    for (int i = 0; i < nb; i++) {
+      int b = B[i];
+      if (b >= n) break;
+      while (true) {
+        int v = content(n - 1);
+        if (b != n - 1) set(b, v);
+        n--;
+        if (b >= n) break;
+        if (!out_pass(d, v, pass)) break;
+      }
+    }
+  }
+  int mv = 0;
+  for (int j = 0; j < nm; j++)
+    if (d.map_pos[j] < n && d.map_id[j] != d.map_pos[j]) {
+      d.moves[1 + 2 * mv] = d.map_pos[j];
+      d.moves[2 + 2 * mv] = d.map_id[j];
+      mv++;
+    }
+  d.moves[0] = mv;
+  *d.n = n;
+}
+
+// GL_copy + CL_copy + CSPW_copy for each move (force and torque are not part of
+// GL_copy and stay where they are).  Sources lie beyond the new count and
+// destinations below it, so the copies are independent.
+__global__ void k_apply_moves(Dev d) {
+  int mv = d.moves[0];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < mv; i += gridDim.x * blockDim.x) {
+    int dst = d.moves[1 + 2 * i], src = d.moves[2 + 2 * i];
+    d.gid[dst] = d.gid[src];
+    d.ptype[dst] = d.ptype[src];
+    d.usrmark[dst] = d.usrmark[src];
+    d.posr[dst] = d.posr[src];
+    d.vel0[dst] = d.vel0[src];
+    d.acc0[dst] = d.acc0[src];
+    if (d.tsize > 1) { d.vel1[dst] = d.vel1[src]; d.acc1[dst] = d.acc1[src]; }
+    if (d.tsize > 2) { d.vel2[dst] = d.vel2[src]; d.acc2[dst] = d.acc2[src]; }
+    d.theta[dst] = d.theta[src];
+    d.rv0[dst] = d.rv0[src];
+    d.ra0[dst] = d.ra0[src];
+    if (d.rsize > 1) { d.rv1[dst] = d.rv1[src]; d.ra1[dst] = d.ra1[src]; }
+    if (d.rsize > 2) { d.rv2[dst] = d.rv2[src]; d.ra2[dst] = d.ra2[src]; }
+    d.near_mask[dst] = d.near_mask[src];
+  }
+}
+
+__global__ void k_step_end(Dev d, int* counters_out) {
+  counters_out[SDEM_CNT_PP] = d.row_off[d.n_launch];
+  counters_out[SDEM_CNT_PPG] = 0;
+  counters_out[SDEM_CNT_PPFIX] = 0;
+  counters_out[SDEM_CNT_PW] = (int)d.counters[1];
+  counters_out[SDEM_CNT_CNSV] = (int)d.counters[0];
+  counters_out[SDEM_CNT_NLOCAL] = *d.n;
+  *d.iter += 1;
+  counters_out[SDEM_CNT_ITER] = *d.iter;
+  counters_out[SDEM_CNT_NEXTWALL] = *d.next_update;
+  d.counters[0] = 0;
+  d.counters[1] = 0;
+  *d.out_cnt = 0;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct sdem_h {
+  sdem_cfg cfg{};
+  int dev = 0;
+  int num_sms = 152;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<void*> allocs;
+  // tables
+  int nT = 0, nWT = 0;
+  double maxR = 0.0;
+  std::vector<double> h_radius;
+  double *radius = nullptr, *mass = nullptr, *inertia = nullptr, *bpp = nullptr, *bpw = nullptr;
+  int nw = 0;
+  double* walls = nullptr;
+  int* wflags = nullptr;
+  std::vector<int> h_wall_id;
+  double max_wall_vel = 0.0;
+  bool have_types = false;
+  // grid
+  double cell = 0, x0 = 0, y0 = 0, z0 = 0;
+  int nx = 0, ny = 0, nz = 0;
+  long long ncell = 0;
+  int *cell_cnt = nullptr, *cell_start = nullptr, *scan_tmp = nullptr;
+  size_t scan_tmp_n = 0;
+  // particles
+  int n_host = 0;  // count at upload (upper bound of the device count)
+  std::vector<int> h_gid;
+  int *gid = nullptr, *ptype = nullptr, *usrmark = nullptr;
+  dbl4 *posr = nullptr, *vel[3] = {}, *acc[3] = {}, *theta = nullptr, *rv[3] = {}, *ra[3] = {};
+  dbl4 *F = nullptr, *T = nullptr;
+  unsigned long long* near_mask = nullptr;
+  int *cell_of = nullptr, *tmp_rank = nullptr, *tmp_sorted = nullptr, *sorted = nullptr, *sortpos = nullptr;
+  int K = 24;
+  int *row_cnt = nullptr, *row_partner = nullptr, *row_off = nullptr, *in_cnt = nullptr;
+  double* row_ovl = nullptr;
+  unsigned* in_list = nullptr;
+  int ccap = 0;
+  int *c_ogid = nullptr, *c_pgid[2] = {}, *sbg[2] = {}, *cbg[2] = {};
+  dbl4 *c_hist[2] = {}, *c_S = nullptr, *c_M = nullptr, *c_Mr = nullptr;
+  int *wh_cnt[2] = {}, *wh_wall[2] = {};
+  dbl4* wh_hist[2] = {};
+  int cur = 0;  // buffer written by the next step
+  // device scalars
+  int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
+  unsigned long long* ull = nullptr;  // counters[2], red[2]
+  int *out_list = nullptr, *moves = nullptr, *map_pos = nullptr, *map_id = nullptr;
+  int* h_counters = nullptr;  // pinned
+  bool stepped = false;
+  // diagnostics: kernel launches issued, optional per-phase CUDA events
+  long long launches = 0;
+  bool prof = false;
+  int prof_steps = 0, prof_cap = 0;
+  std::vector<cudaEvent_t> prof_ev;   // prof_cap * (kPhases + 1)
+};
+
+namespace {
+
+int set_err(sdem_h* h, int code, const std::string& msg) {
+  h->err = msg;
+  return code;
+}
+
+int cuda_fail(sdem_h* h, cudaError_t e, const char* where) {
+  return set_err(h, SDEM_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+template <class T>
+int dalloc(sdem_h* h, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(h, SDEM_E_NOMEM, std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes failed");
+  }
+  cudaMemsetAsync(q, 0, bytes, h->stream);
+  h->allocs.push_back(q);
+  *p = (T*)q;
+  return 0;
+}
+
+enum { S_N = 0, S_STATUS = 1, S_ITER = 3, S_NEXT = 4, S_OUTCNT = 5, S_COUNTERS = 8, S_SIZE = 16 };
+
+Dev make_dev(sdem_h* h) {
+  Dev d{};
+  const sdem_cfg& c = h->cfg;
+  d.ncap = c.n_capacity;
+  d.n_launch = h->n_host;
+  d.n = h->scal + S_N;
+  d.max_gid = c.max_gid;
+  d.K = h->K;
+  d.Kin = h->K;
+  d.ccap = h->ccap;
+  d.tsize = c.tsize;
+  d.rsize = c.rsize;
+  d.pi = c.pi_method;
+  d.pri = c.pri_method;
+  d.quirk = c.quirk_ab2_rot;
+  d.law.cf_type = c.cf_type;
+  d.law.ct_model = c.ct_model;
+  d.law.dt = c.dt;
+  d.g = make_double3(c.gravity[0], c.gravity[1], c.gravity[2]);
+  d.cell = h->cell;
+  d.x0 = h->x0;
+  d.y0 = h->y0;
+  d.z0 = h->z0;
+  d.nx = h->nx;
+  d.ny = h->ny;
+  d.nz = h->nz;
+  d.ncell = h->ncell;
+  d.dmin = make_double3(c.dom_min[0], c.dom_min[1], c.dom_min[2]);
+  d.dmax = make_double3(c.dom_max[0], c.dom_max[1], c.dom_max[2]);
+  d.nT = h->nT;
+  d.nWT = h->nWT;
+  d.radius = h->radius;
+  d.mass = h->mass;
+  d.inertia = h->inertia;
+  d.bpp = h->bpp;
+  d.bpw = h->bpw;
+  d.nw = h->nw;
+  d.walls = h->walls;
+  d.wflags = h->wflags;
+  d.dx1 = h->maxR * c.wall_neighbor_ratio;
+  d.dx2 = h->maxR * (c.wall_neighbor_ratio + 1.0);
+  d.max_wall_vel = h->max_wall_vel;
+  d.wall_max_update_iter = c.wall_max_update_iter;
+  d.gid = h->gid;
+  d.ptype = h->ptype;
+  d.usrmark = h->usrmark;
+  d.posr = h->posr;
+  d.vel0 = h->vel[0];
+  d.vel1 = h->vel[1];
+  d.vel2 = h->vel[2];
+  d.acc0 = h->acc[0];
+  d.acc1 = h->acc[1];
+  d.acc2 = h->acc[2];
+  d.theta = h->theta;
+  d.rv0 = h->rv[0];
+  d.rv1 = h->rv[1];
+  d.rv2 = h->rv[2];
+  d.ra0 = h->ra[0];
+  d.ra1 = h->ra[1];
+  d.ra2 = h->ra[2];
+  d.F = h->F;
+  d.T = h->T;
+  d.near_mask = h->near_mask;
+  d.cell_of = h->cell_of;
+  d.cell_cnt = h->cell_cnt;
+  d.cell_start = h->cell_start;
+  d.tmp_rank = h->tmp_rank;
+  d.tmp_sorted = h->tmp_sorted;
+  d.sorted = h->sorted;
+  d.sortpos = h->sortpos;
+  d.row_cnt = h->row_cnt;
+  d.row_partner = h->row_partner;
+  d.row_off = h->row_off;
+  d.row_ovl = h->row_ovl;
+  d.in_cnt = h->in_cnt;
+  d.in_list = h->in_list;
+  int cu = h->cur, pv = 1 - h->cur;
+  d.c_ogid = h->c_ogid;
+  d.c_pgid = h->c_pgid[cu];
+  d.c_pgid_prev = h->c_pgid[pv];
+  d.c_hist = h->c_hist[cu];
+  d.c_hist_prev = h->c_hist[pv];
+  d.c_S = h->c_S;
+  d.c_M = h->c_M;
+  d.c_Mr = h->c_Mr;
+  d.sbg = h->sbg[cu];
+  d.cbg = h->cbg[cu];
+  d.sbg_prev = h->sbg[pv];
+  d.cbg_prev = h->cbg[pv];
+  d.wh_cnt = h->wh_cnt[cu];
+  d.wh_wall = h->wh_wall[cu];
+  d.wh_hist = h->wh_hist[cu];
+  d.wh_cnt_prev = h->wh_cnt[pv];
+  d.wh_wall_prev = h->wh_wall[pv];
+  d.wh_hist_prev = h->wh_hist[pv];
+  d.status = h->scal + S_STATUS;
+  d.counters = h->ull;
+  d.red = h->ull + 2;
+  d.iter = h->scal + S_ITER;
+  d.next_update = h->scal + S_NEXT;
+  d.out_cnt = h->scal + S_OUTCNT;
+  d.out_list = h->out_list;
+  d.moves = h->moves;
+  d.map_pos = h->map_pos;
+  d.map_id = h->map_id;
+  return d;
+}
+
+int grid_for(long long n) { return (int)std::max<long long>(1, (n + kThreads - 1) / kThreads); }
+
+void scan(sdem_h* h, const int* in, long long n, int* out) {
+  int nb = (int)std::max<long long>(1, (n + kScanTile - 1) / kScanTile);
+  k_scan_reduce<<<nb, 1024, 0, h->stream>>>(in, n, h->scan_tmp);
+  k_scan_blocks<<<1, 1024, 0, h->stream>>>(h->scan_tmp, nb);
+  k_scan_apply<<<nb, 1024, 0, h->stream>>>(in, n, h->scan_tmp, out);
+}
+
+int enqueue_step(sdem_h* h) {
+  Dev d = make_dev(h);
+  int n = h->n_host;
+  cudaStream_t st = h->stream;
+  cudaEvent_t* ev = nullptr;
+  if (h->prof && h->prof_steps < h->prof_cap) ev = &h->prof_ev[(size_t)h->prof_steps * (kPhases + 1)];
+  auto mark = [&](int ph) {
+    if (ev) cudaEventRecord(ev[ph], st);
+  };
+  long long L = 0;
+  mark(PH_WALL);
+  if (h->nw > 0) {
+    k_wall_refresh<<<grid_for(n), kThreads, 0, st>>>(d);
+    k_wall_refresh_end<<<1, 1, 0, st>>>(d);
+    L += 2;
+  }
+  mark(PH_BIN);
+  cudaMemsetAsync(h->cell_cnt, 0, sizeof(int) * (size_t)h->ncell, st);
+  cudaMemsetAsync(h->in_cnt, 0, sizeof(int) * (size_t)std::max(n, 1), st);
+  k_bin<<<grid_for(n), kThreads, 0, st>>>(d);
+  mark(PH_SCAN_CELLS);
+  scan(h, h->cell_cnt, h->ncell, h->cell_start);
+  mark(PH_SCATTER);
+  k_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
+  mark(PH_CELLORDER);
+  k_cellorder<<<grid_for(n), kThreads, 0, st>>>(d);
+  mark(PH_SEARCH);
+  k_search<<<grid_for(n), kThreads, 0, st>>>(d);
+  mark(PH_SCAN_ROWS);
+  scan(h, h->row_cnt, n, h->row_off);
+  mark(PH_GID_INDEX);
+  k_gid_index<<<grid_for(n), kThreads, 0, st>>>(d);
+  mark(PH_FORCE);
+  k_force<<<h->num_sms * 8, kThreads, 0, st>>>(d);
+  mark(PH_GATHER);
+  k_gather_integrate<<<grid_for(n), kThreads, 0, st>>>(d);
+  mark(PH_DELETE);
+  k_delete<<<1, 1, 0, st>>>(d);
+  k_apply_moves<<<16, kThreads, 0, st>>>(d);
+  mark(PH_END);
+  k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS);
+  mark(kPhases);
+  L += 1 + 3 + 1 + 1 + 1 + 3 + 1 + 1 + 1 + 2 + 1;
+  h->launches += L;
+  if (ev) h->prof_steps++;
+  h->cur = 1 - h->cur;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
+  return 0;
+}
+
+int sync_and_check(sdem_h* h) {
+  CK(cudaStreamSynchronize(h->stream));
+  int s[S_SIZE];
+  CK(cudaMemcpy(s, h->scal, sizeof s, cudaMemcpyDeviceToHost));
+  std::memcpy(h->h_counters, s + S_COUNTERS, sizeof(int) * SDEM_CNT_SIZE);
+  if (s[S_STATUS] != 0) {
+    int code = s[S_STATUS], detail = s[S_STATUS + 1];
+    std::string msg;
+    switch (code) {
+      case SDEM_E_GRID: msg = "particle index " + std::to_string(detail) + " is outside the padded search grid"; break;
+      case SDEM_E_CL_FULL: msg = "contact capacity exceeded (detail " + std::to_string(detail) +
+                                 "): raise cntct_list_size or max_contacts_per_particle"; break;
+      case SDEM_E_CAPACITY: msg = "too many out-of-domain particles in one step"; break;
+      default: msg = "device error " + std::to_string(code) + " detail " + std::to_string(detail);
+    }
+    // clear so the handle stays usable for downloads
+    int z[2] = {0, 0};
+    cudaMemcpy(h->scal + S_STATUS, z, sizeof z, cudaMemcpyHostToDevice);
+    return set_err(h, code, msg);
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+void sdem_default_cfg(sdem_cfg* c) {
+  std::memset(c, 0, sizeof *c);
+  c->n_capacity = 8000;
+  c->max_gid = 8000;
+  c->tsize = 1;
+  c->rsize = 1;
+  c->cf_type = SDEM_CFT_LSD;
+  c->ct_model = SDEM_CTM_CONSTANT;
+  c->pi_method = SDEM_PIM_FE;
+  c->pri_method = SDEM_PIM_FE;
+  c->cs_method = SDEM_CSM_NBS_MUNJIZA;
+  c->cntct_list_size = 6;
+  c->base_wall_id = 10000000;
+  c->wall_max_update_iter = 100;
+  c->quirk_ab2_rot = 1;
+  c->max_contacts_per_particle = 0;
+  c->dt = 1.0E-5;
+  c->gravity[1] = -9.81;
+  c->cs_ratio = 1.0;
+  c->wall_neighbor_ratio = 2.0;
+}
+
+int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
+  if (!cfg || !out) return SDEM_E_ARG;
+  *out = nullptr;
+  sdem_h* h = new sdem_h();
+  h->cfg = *cfg;
+  const sdem_cfg& c = h->cfg;
+  auto bad = [&](const char* m) {
+    h->err = m;
+    *out = h;
+    return SDEM_E_ARG;
+  };
+  if (c.n_capacity < 1) return bad("n_capacity must be >= 1");
+  if (c.max_gid < 1) return bad("max_gid must be >= 1");
+  if (c.tsize < 1 || c.tsize > 3 || c.rsize < 1 || c.rsize > 3) return bad("tsize/rsize must be 1..3");
+  if (c.tsize < c.pi_method || c.rsize < c.pri_method) return bad("tsize >= PI_Method and rsize >= PRI_Method required");
+  if (c.cf_type != SDEM_CFT_LSD && c.cf_type != SDEM_CFT_NLIN) return bad("cf_type must be 1 (LSD) or 2 (Hertz)");
+  if (c.ct_model != SDEM_CTM_CONSTANT && c.ct_model != SDEM_CTM_VARIABLE) return bad("ct_model must be 1 or 2");
+  if (c.cs_method != SDEM_CSM_NBS_MUNJIZA) {
+    h->err = "only CS_Method=1 (NBS Munjiza) is implemented on the GPU";
+    *out = h;
+    return SDEM_E_UNSUPPORTED;
+  }
+  if (c.periodic[0] || c.periodic[1] || c.periodic[2]) {
+    h->err = "periodic directions are not implemented on the GPU";
+    *out = h;
+    return SDEM_E_UNSUPPORTED;
+  }
+  if (!(c.cs_ratio >= 1.0)) return bad("Prtcl_cs_ratio must be >= 1 for the one-level NBS search");
+  if (c.n_capacity >= (1 << 26)) return bad("n_capacity must be < 2^26");
+  h->K = c.max_contacts_per_particle > 0 ? c.max_contacts_per_particle : 24;
+  if (h->K > kMaxK) return bad("max_contacts_per_particle must be <= 64");
+  *out = h;
+  if (cudaGetDevice(&h->dev) != cudaSuccess) return set_err(h, SDEM_E_CUDA, "no CUDA device");
+  CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->dev));
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  int N = c.n_capacity;
+  int rc = 0;
+  rc |= dalloc(h, &h->gid, N);
+  rc |= dalloc(h, &h->ptype, N);
+  rc |= dalloc(h, &h->usrmark, N);
+  rc |= dalloc(h, &h->posr, N);
+  for (int k = 0; k < 3; k++) {
+    if (k < c.tsize) { rc |= dalloc(h, &h->vel[k], N); rc |= dalloc(h, &h->acc[k], N); }
+    if (k < c.rsize) { rc |= dalloc(h, &h->rv[k], N); rc |= dalloc(h, &h->ra[k], N); }
+  }
+  rc |= dalloc(h, &h->theta, N);
+  rc |= dalloc(h, &h->F, N);
+  rc |= dalloc(h, &h->T, N);
+  rc |= dalloc(h, &h->near_mask, N);
+  rc |= dalloc(h, &h->cell_of, N);
+  rc |= dalloc(h, &h->tmp_rank, N);
+  rc |= dalloc(h, &h->tmp_sorted, N);
+  rc |= dalloc(h, &h->sorted, N);
+  rc |= dalloc(h, &h->sortpos, N);
+  rc |= dalloc(h, &h->row_cnt, N);
+  rc |= dalloc(h, &h->row_off, (size_t)N + 1);
+  rc |= dalloc(h, &h->row_partner, (size_t)N * h->K);
+  rc |= dalloc(h, &h->row_ovl, (size_t)N * h->K);
+  rc |= dalloc(h, &h->in_cnt, N);
+  rc |= dalloc(h, &h->in_list, (size_t)N * h->K);
+  h->ccap = std::max(1, c.cntct_list_size) * N;
+  rc |= dalloc(h, &h->c_ogid, h->ccap);
+  rc |= dalloc(h, &h->c_S, h->ccap);
+  rc |= dalloc(h, &h->c_M, h->ccap);
+  rc |= dalloc(h, &h->c_Mr, h->ccap);
+  size_t G = (size_t)c.max_gid + 1;
+  for (int b = 0; b < 2; b++) {
+    rc |= dalloc(h, &h->c_pgid[b], h->ccap);
+    rc |= dalloc(h, &h->c_hist[b], h->ccap);
+    rc |= dalloc(h, &h->sbg[b], G);
+    rc |= dalloc(h, &h->cbg[b], G);
+    rc |= dalloc(h, &h->wh_cnt[b], G);
+    rc |= dalloc(h, &h->wh_wall[b], G * kKw);
+    rc |= dalloc(h, &h->wh_hist[b], G * kKw);
+  }
+  rc |= dalloc(h, &h->scal, S_SIZE);
+  rc |= dalloc(h, &h->ull, 4);
+  rc |= dalloc(h, &h->out_list, kOutCap);
+  rc |= dalloc(h, &h->moves, 1 + 2 * 5 * kOutCap + 5 * kOutCap);
+  rc |= dalloc(h, &h->map_pos, 5 * kOutCap);
+  rc |= dalloc(h, &h->map_id, 5 * kOutCap);
+  rc |= dalloc(h, &h->scan_tmp, 65536);
+  if (rc) return SDEM_E_NOMEM;
+  CK(cudaMallocHost(&h->h_counters, sizeof(int) * SDEM_CNT_SIZE));
+  std::memset(h->h_counters, 0, sizeof(int) * SDEM_CNT_SIZE);
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int sdem_set_types(sdem_h* h, int nT, const double* radius, const double* mass, const double* inertia,
+                   const double* bnry_pp, int nWT, const double* bnry_pw) {
+  if (!h) return SDEM_E_ARG;
+  if (nT < 1 || nWT < 1 || !radius || !mass || !inertia || !bnry_pp || !bnry_pw)
+    return set_err(h, SDEM_E_ARG, "sdem_set_types: bad arguments");
+  if (h->have_types) return set_err(h, SDEM_E_ARG, "sdem_set_types: tables are set once per handle");
+  h->nT = nT;
+  h->nWT = nWT;
+  h->h_radius.assign(radius, radius + nT);
+  int rc = 0;
+  rc |= dalloc(h, &h->radius, nT);
+  rc |= dalloc(h, &h->mass, nT);
+  rc |= dalloc(h, &h->inertia, nT);
+  rc |= dalloc(h, &h->bpp, (size_t)nT * nT * SDEM_BP_SIZE);
+  rc |= dalloc(h, &h->bpw, (size_t)nT * nWT * SDEM_BP_SIZE);
+  if (rc) return SDEM_E_NOMEM;
+  CK(cudaMemcpy(h->radius, radius, sizeof(double) * nT, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->mass, mass, sizeof(double) * nT, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->inertia, inertia, sizeof(double) * nT, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->bpp, bnry_pp, sizeof(double) * nT * nT * SDEM_BP_SIZE, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->bpw, bnry_pw, sizeof(double) * nT * nWT * SDEM_BP_SIZE, cudaMemcpyHostToDevice));
+  // Init_NBSM, Prtcl_NBS_Munjiza.f90:66-77 (one rank: subdomain = domain)
+  double maxR = radius[0];
+  for (int t = 1; t < nT; t++) maxR = std::max(maxR, radius[t]);
+  h->maxR = maxR;
+  const sdem_cfg& c = h->cfg;
+  double maxDiam = 2.0 * maxR;
+  h->cell = c.cs_ratio * maxDiam;
+  h->x0 = c.dom_min[0] - h->cell * 1.05;
+  h->y0 = c.dom_min[1] - h->cell * 1.05;
+  h->z0 = c.dom_min[2] - h->cell * 1.05;
+  double xed = c.dom_max[0] + h->cell * 1.05, yed = c.dom_max[1] + h->cell * 1.05, zed = c.dom_max[2] + h->cell * 1.05;
+  h->nx = (int)((xed - h->x0) / h->cell) + 1;
+  h->ny = (int)((yed - h->y0) / h->cell) + 1;
+  h->nz = (int)((zed - h->z0) / h->cell) + 1;
+  h->ncell = (long long)h->nx * h->ny * h->nz;
+  if (h->ncell >= (1ll << 31) - 1) return set_err(h, SDEM_E_ARG, "search grid has more than 2^31 cells");
+  rc |= dalloc(h, &h->cell_cnt, (size_t)h->ncell);
+  rc |= dalloc(h, &h->cell_start, (size_t)h->ncell + 1);
+  if (rc) return SDEM_E_NOMEM;
+  long long nb = std::max<long long>((h->ncell + kScanTile - 1) / kScanTile, (h->cfg.n_capacity + kScanTile - 1) / kScanTile);
+  if (nb > 65536) {
+    rc |= dalloc(h, &h->scan_tmp, (size_t)nb);
+    if (rc) return SDEM_E_NOMEM;
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  h->have_types = true;
+  return 0;
+}
+
+int sdem_set_walls(sdem_h* h, int nw, const double* wall, const int* flags) {
+  if (!h) return SDEM_E_ARG;
+  if (nw < 0 || nw > kMaxWalls) return set_err(h, SDEM_E_ARG, "sdem_set_walls: 0 <= nw <= 64");
+  if (nw > 0 && (!wall || !flags)) return set_err(h, SDEM_E_ARG, "sdem_set_walls: null arrays");
+  h->nw = nw;
+  h->h_wall_id.assign(nw, 0);
+  double mv = 0.0;
+  for (int k = 0; k < nw; k++) {
+    const double* v = wall + (size_t)k * SDEM_W_SIZE + SDEM_W_VEL;
+    double s = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    mv = (mv > s) ? mv : s;
+    h->h_wall_id[k] = flags[(size_t)k * SDEM_WF_SIZE + SDEM_WF_WALL_ID];
+    int wt = flags[(size_t)k * SDEM_WF_SIZE + SDEM_WF_WALL_TYPE];
+    if (h->have_types && (wt < 1 || wt > h->nWT)) return set_err(h, SDEM_E_ARG, "sdem_set_walls: wall_Type out of range");
+  }
+  h->max_wall_vel = mv;
+  int rc = 0;
+  if (!h->walls) {
+    rc |= dalloc(h, &h->walls, (size_t)kMaxWalls * SDEM_W_SIZE);
+    rc |= dalloc(h, &h->wflags, (size_t)kMaxWalls * SDEM_WF_SIZE);
+    if (rc) return SDEM_E_NOMEM;
+  }
+  if (nw > 0) {
+    CK(cudaMemcpy(h->walls, wall, sizeof(double) * nw * SDEM_W_SIZE, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->wflags, flags, sizeof(int) * nw * SDEM_WF_SIZE, cudaMemcpyHostToDevice));
+  }
+  // the near-wall list is rebuilt at the next step
+  int zero = 0;
+  CK(cudaMemcpy(h->scal + S_NEXT, &zero, sizeof zero, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, const int* usrmark, const double* posR,
+                          const double* linVel, const double* linAcc, const double* theta, const double* rotVel,
+                          const double* rotAcc) {
+  if (!h) return SDEM_E_ARG;
+  const sdem_cfg& c = h->cfg;
+  if (!h->have_types) return set_err(h, SDEM_E_ARG, "sdem_upload_particles: call sdem_set_types first");
+  if (n < 0 || n > c.n_capacity) return set_err(h, SDEM_E_CAPACITY, "sdem_upload_particles: n exceeds n_capacity");
+  if (n > 0 && (!id || !ptype || !posR || !linVel)) return set_err(h, SDEM_E_ARG, "sdem_upload_particles: null arrays");
+  std::vector<char> seen((size_t)c.max_gid + 1, 0);
+  for (int i = 0; i < n; i++) {
+    if (id[i] < 1 || id[i] > c.max_gid) return set_err(h, SDEM_E_BAD_ID, "particle id outside 1..max_gid");
+    if (seen[id[i]]) return set_err(h, SDEM_E_BAD_ID, "duplicate particle id");
+    seen[id[i]] = 1;
+    if (ptype[i] < 1 || ptype[i] > h->nT) return set_err(h, SDEM_E_ARG, "particle type outside 1..nT");
+  }
+  h->h_gid.assign(id, id + n);
+  std::vector<int> um(n, 0);
+  if (usrmark) std::copy(usrmark, usrmark + n, um.begin());
+  CK(cudaMemcpy(h->gid, id, sizeof(int) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->ptype, ptype, sizeof(int) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->usrmark, um.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  std::vector<dbl4> buf(std::max(n, 1));
+  for (int i = 0; i < n; i++) buf[i] = make_dbl4(posR[4 * i], posR[4 * i + 1], posR[4 * i + 2], posR[4 * i + 3]);
+  CK(cudaMemcpy(h->posr, buf.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice));
+  auto put3 = [&](dbl4* dst, const double* src, int levels, int k) -> int {
+    for (int i = 0; i < n; i++) {
+      if (src) {
+        const double* v = src + ((size_t)i * levels + k) * 3;
+        buf[i] = make_dbl4(v[0], v[1], v[2], 0.0);
+      } else {
+        buf[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+      }
+    }
+    CK(cudaMemcpy(dst, buf.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice));
+    return 0;
+  };
+  int rc = 0;
+  for (int k = 0; k < c.tsize; k++) {
+    rc |= put3(h->vel[k], linVel, c.tsize, k);
+    rc |= put3(h->acc[k], linAcc, c.tsize, k);
+  }
+  for (int k = 0; k < c.rsize; k++) {
+    rc |= put3(h->rv[k], rotVel, c.rsize, k);
+    rc |= put3(h->ra[k], rotAcc, c.rsize, k);
+  }
+  rc |= put3(h->theta, theta, 1, 0);
+  if (rc) return rc;
+  // history reset: both buffers empty; near-wall list refreshed at the next step
+  size_t G = (size_t)c.max_gid + 1;
+  for (int b = 0; b < 2; b++) {
+    CK(cudaMemset(h->cbg[b], 0, sizeof(int) * G));
+    CK(cudaMemset(h->sbg[b], 0, sizeof(int) * G));
+    CK(cudaMemset(h->wh_cnt[b], 0, sizeof(int) * G));
+  }
+  CK(cudaMemset(h->F, 0, sizeof(dbl4) * c.n_capacity));
+  CK(cudaMemset(h->T, 0, sizeof(dbl4) * c.n_capacity));
+  CK(cudaMemset(h->near_mask, 0, sizeof(unsigned long long) * c.n_capacity));
+  int sc[S_SIZE] = {0};
+  sc[S_N] = n;
+  CK(cudaMemcpy(h->scal, sc, sizeof sc, cudaMemcpyHostToDevice));
+  CK(cudaMemset(h->ull, 0, sizeof(unsigned long long) * 4));
+  h->n_host = n;
+  h->cur = 0;
+  h->stepped = false;
+  std::memset(h->h_counters, 0, sizeof(int) * SDEM_CNT_SIZE);
+  h->h_counters[SDEM_CNT_NLOCAL] = n;
+  return 0;
+}
+
+int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* partner_id, const double* tandelta,
+                         const double* velrel) {
+  if (!h) return SDEM_E_ARG;
+  if (nc < 0 || (nc > 0 && (!owner_idx || !partner_id || !tandelta || !velrel)))
+    return set_err(h, SDEM_E_ARG, "sdem_upload_contacts: bad arguments");
+  const sdem_cfg& c = h->cfg;
+  int n = h->n_host;
+  // The history the next step reads is the "previous" buffer.
+  int pv = 1 - h->cur;
+  struct PP { int lo, hi; dbl4 hist; };
+  std::vector<PP> pp;
+  std::vector<std::vector<std::pair<int, dbl4>>> wl(n);
+  for (int i = 0; i < nc; i++) {
+    int o = owner_idx[i];
+    if (o < 0 || o >= n) return set_err(h, SDEM_E_ARG, "sdem_upload_contacts: owner index out of range");
+    int go = h->h_gid[o], pid = partner_id[i];
+    dbl4 hist = make_dbl4(tandelta[3 * i], tandelta[3 * i + 1], tandelta[3 * i + 2], velrel[i]);
+    if (pid > c.base_wall_id) {
+      int wi = -1;
+      for (int k = 0; k < h->nw; k++)
+        if (h->h_wall_id[k] == pid) { wi = k; break; }
+      if (wi < 0) continue;  // a wall this handle does not have: the record is never looked up
+      bool dup = false;
+      for (auto& e : wl[o]) dup |= (e.first == wi);
+      if (!dup) wl[o].push_back({wi, hist});
+    } else {
+      // Only the lower id's record is ever found by Find_insert (its bucket).
+      if (go < pid) pp.push_back({go, pid, hist});
+    }
+  }
+  // rows keyed by the lower id
+  std::stable_sort(pp.begin(), pp.end(), [](const PP& a, const PP& b) { return a.lo < b.lo || (a.lo == b.lo && a.hi < b.hi); });
+  pp.erase(std::unique(pp.begin(), pp.end(), [](const PP& a, const PP& b) { return a.lo == b.lo && a.hi == b.hi; }), pp.end());
+  if ((long long)pp.size() > h->ccap) return set_err(h, SDEM_E_CL_FULL, "sdem_upload_contacts: more records than contact capacity");
+  size_t G = (size_t)c.max_gid + 1;
+  std::vector<int> sbg(G, 0), cbg(G, 0), pg(pp.size());
+  std::vector<dbl4> hs(pp.size());
+  for (size_t i = 0; i < pp.size(); i++) {
+    if (i == 0 || pp[i].lo != pp[i - 1].lo) sbg[pp[i].lo] = (int)i;
+    cbg[pp[i].lo]++;
+    pg[i] = pp[i].hi;
+    hs[i] = pp[i].hist;
+  }
+  CK(cudaMemcpy(h->sbg[pv], sbg.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->cbg[pv], cbg.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
+  if (!pp.empty()) {
+    CK(cudaMemcpy(h->c_pgid[pv], pg.data(), sizeof(int) * pp.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->c_hist[pv], hs.data(), sizeof(dbl4) * pp.size(), cudaMemcpyHostToDevice));
+  }
+  std::vector<int> whc(G, 0), whw(G * kKw, 0);
+  std::vector<dbl4> whh(G * kKw);
+  for (int o = 0; o < n; o++) {
+    int g = h->h_gid[o];
+    int k = 0;
+    for (auto& e : wl[o]) {
+      if (k >= kKw) return set_err(h, SDEM_E_CL_FULL, "sdem_upload_contacts: more than 4 wall contacts on one particle");
+      whw[(size_t)g * kKw + k] = e.first;
+      whh[(size_t)g * kKw + k] = e.second;
+      k++;
+    }
+    whc[g] = k;
+  }
+  CK(cudaMemcpy(h->wh_cnt[pv], whc.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->wh_wall[pv], whw.data(), sizeof(int) * G * kKw, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->wh_hist[pv], whh.data(), sizeof(dbl4) * G * kKw, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int sdem_step_async(sdem_h* h, int nsteps) {
+  if (!h) return SDEM_E_ARG;
+  if (!h->have_types) return set_err(h, SDEM_E_ARG, "sdem_step: call sdem_set_types first");
+  if (nsteps < 0) return set_err(h, SDEM_E_ARG, "sdem_step: nsteps < 0");
+  if (h->n_host == 0) return 0;
+  for (int i = 0; i < nsteps; i++) {
+    int rc = enqueue_step(h);
+    if (rc) return rc;
+  }
+  h->stepped = h->stepped || nsteps > 0;
+  return 0;
+}
+
+int sdem_step(sdem_h* h, int nsteps) {
+  int rc = sdem_step_async(h, nsteps);
+  if (rc) return rc;
+  return sync_and_check(h);
+}
+
+int sdem_get_stream(sdem_h* h, void** stream) {
+  if (!h || !stream) return SDEM_E_ARG;
+  *stream = (void*)h->stream;
+  return 0;
+}
+
+int sdem_download_particles(sdem_h* h, int* n_out, int* id, int* ptype, int* usrmark, double* posR, double* linVel,
+                            double* linAcc, double* theta, double* rotVel, double* rotAcc) {
+  if (!h) return SDEM_E_ARG;
+  int rc = sync_and_check(h);
+  if (rc && rc != SDEM_E_CL_FULL && rc != SDEM_E_GRID && rc != SDEM_E_CAPACITY) return rc;
+  int n = 0;
+  CK(cudaMemcpy(&n, h->scal + S_N, sizeof n, cudaMemcpyDeviceToHost));
+  if (n_out) *n_out = n;
+  const sdem_cfg& c = h->cfg;
+  if (id) CK(cudaMemcpy(id, h->gid, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if (ptype) CK(cudaMemcpy(ptype, h->ptype, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if (usrmark) CK(cudaMemcpy(usrmark, h->usrmark, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  std::vector<dbl4> buf(std::max(n, 1));
+  if (posR) {
+    CK(cudaMemcpy(buf.data(), h->posr, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) { posR[4 * i] = buf[i].x; posR[4 * i + 1] = buf[i].y; posR[4 * i + 2] = buf[i].z; posR[4 * i + 3] = buf[i].w; }
+  }
+  auto get3 = [&](double* dst, dbl4* src, int levels, int k) -> int {
+    CK(cudaMemcpy(buf.data(), src, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) {
+      double* v = dst + ((size_t)i * levels + k) * 3;
+      v[0] = buf[i].x; v[1] = buf[i].y; v[2] = buf[i].z;
+    }
+    return 0;
+  };
+  rc = 0;
+  for (int k = 0; k < c.tsize; k++) {
+    if (linVel) rc |= get3(linVel, h->vel[k], c.tsize, k);
+    if (linAcc) rc |= get3(linAcc, h->acc[k], c.tsize, k);
+  }
+  for (int k = 0; k < c.rsize; k++) {
+    if (rotVel) rc |= get3(rotVel, h->rv[k], c.rsize, k);
+    if (rotAcc) rc |= get3(rotAcc, h->ra[k], c.rsize, k);
+  }
+  if (theta) rc |= get3(theta, h->theta, 1, 0);
+  return rc;
+}
+
+int sdem_download_forces(sdem_h* h, double* F, double* T) {
+  if (!h) return SDEM_E_ARG;
+  int rc = sync_and_check(h);
+  if (rc) return rc;
+  int n = 0;
+  CK(cudaMemcpy(&n, h->scal + S_N, sizeof n, cudaMemcpyDeviceToHost));
+  std::vector<dbl4> buf(std::max(n, 1));
+  if (F) {
+    CK(cudaMemcpy(buf.data(), h->F, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) { F[3 * i] = buf[i].x; F[3 * i + 1] = buf[i].y; F[3 * i + 2] = buf[i].z; }
+  }
+  if (T) {
+    CK(cudaMemcpy(buf.data(), h->T, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) { T[3 * i] = buf[i].x; T[3 * i + 1] = buf[i].y; T[3 * i + 2] = buf[i].z; }
+  }
+  return 0;
+}
+
+namespace {
+struct CRec { int owner, partner; double t[3]; double vr; };
+
+int gather_contacts(sdem_h* h, std::vector<CRec>& out) {
+  int rc = sync_and_check(h);
+  if (rc) return rc;
+  out.clear();
+  int n = 0;
+  CK(cudaMemcpy(&n, h->scal + S_N, sizeof n, cudaMemcpyDeviceToHost));
+  std::vector<int> gid(std::max(n, 1));
+  CK(cudaMemcpy(gid.data(), h->gid, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  const sdem_cfg& c = h->cfg;
+  std::vector<int> idx_of((size_t)c.max_gid + 1, -1);
+  for (int i = 0; i < n; i++) idx_of[gid[i]] = i;
+  // the buffers last written are "prev" now (cur flipped after each step)
+  int lw = 1 - h->cur;
+  size_t G = (size_t)c.max_gid + 1;
+  if (h->stepped) {
+    int C = 0;
+    CK(cudaMemcpy(&C, h->row_off + h->n_host, sizeof C, cudaMemcpyDeviceToHost));
+    std::vector<int> og(std::max(C, 1)), pg(std::max(C, 1));
+    std::vector<dbl4> hs(std::max(C, 1));
+    if (C > 0) {
+      CK(cudaMemcpy(og.data(), h->c_ogid, sizeof(int) * C, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(pg.data(), h->c_pgid[lw], sizeof(int) * C, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(hs.data(), h->c_hist[lw], sizeof(dbl4) * C, cudaMemcpyDeviceToHost));
+    }
+    for (int i = 0; i < C; i++) {
+      int a = idx_of[og[i]], b = idx_of[pg[i]];
+      CRec r;
+      r.t[0] = hs[i].x; r.t[1] = hs[i].y; r.t[2] = hs[i].z; r.vr = hs[i].w;
+      if (a >= 0) { r.owner = a; r.partner = pg[i]; out.push_back(r); }
+      if (b >= 0) { r.owner = b; r.partner = og[i]; out.push_back(r); }
+    }
+  } else {
+    // not stepped since upload: report the uploaded history
+    std::vector<int> sbg(G), cbg(G);
+    CK(cudaMemcpy(sbg.data(), h->sbg[lw], sizeof(int) * G, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(cbg.data(), h->cbg[lw], sizeof(int) * G, cudaMemcpyDeviceToHost));
+    long long tot = 0;
+    for (size_t g = 0; g < G; g++) tot += cbg[g];
+    std::vector<int> pg(std::max<long long>(tot, 1));
+    std::vector<dbl4> hs(std::max<long long>(tot, 1));
+    if (tot > 0) {
+      CK(cudaMemcpy(pg.data(), h->c_pgid[lw], sizeof(int) * tot, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(hs.data(), h->c_hist[lw], sizeof(dbl4) * tot, cudaMemcpyDeviceToHost));
+    }
+    for (size_t g = 0; g < G; g++)
+      for (int j = 0; j < cbg[g]; j++) {
+        int e = sbg[g] + j;
+        int a = idx_of[g], b = idx_of[pg[e]];
+        CRec r;
+        r.t[0] = hs[e].x; r.t[1] = hs[e].y; r.t[2] = hs[e].z; r.vr = hs[e].w;
+        if (a >= 0) { r.owner = a; r.partner = pg[e]; out.push_back(r); }
+        if (b >= 0) { r.owner = b; r.partner = (int)g; out.push_back(r); }
+      }
+  }
+  std::vector<int> whc(G), whw(G * kKw);
+  std::vector<dbl4> whh(G * kKw);
+  CK(cudaMemcpy(whc.data(), h->wh_cnt[lw], sizeof(int) * G, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(whw.data(), h->wh_wall[lw], sizeof(int) * G * kKw, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(whh.data(), h->wh_hist[lw], sizeof(dbl4) * G * kKw, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; i++) {
+    int g = gid[i];
+    for (int j = 0; j < whc[g] && j < kKw; j++) {
+      int wi = whw[(size_t)g * kKw + j];
+      if (wi < 0 || wi >= h->nw) continue;
+      CRec r;
+      r.owner = i;
+      r.partner = h->h_wall_id[wi];
+      dbl4 v = whh[(size_t)g * kKw + j];
+      r.t[0] = v.x; r.t[1] = v.y; r.t[2] = v.z; r.vr = v.w;
+      out.push_back(r);
+    }
+  }
+  std::sort(out.begin(), out.end(), [](const CRec& a, const CRec& b) {
+    return a.owner < b.owner || (a.owner == b.owner && a.partner < b.partner);
+  });
+  return 0;
+}
+}  // namespace
+
+int sdem_download_contacts(sdem_h* h, int cap, int* nc, int* owner_idx, int* partner_id, double* tandelta,
+                           double* velrel) {
+  if (!h || !nc) return SDEM_E_ARG;
+  std::vector<CRec> recs;
+  int rc = gather_contacts(h, recs);
+  if (rc) return rc;
+  *nc = (int)recs.size();
+  if ((int)recs.size() > cap || !owner_idx || !partner_id || !tandelta || !velrel) return 0;
+  for (size_t i = 0; i < recs.size(); i++) {
+    owner_idx[i] = recs[i].owner;
+    partner_id[i] = recs[i].partner;
+    tandelta[3 * i] = recs[i].t[0];
+    tandelta[3 * i + 1] = recs[i].t[1];
+    tandelta[3 * i + 2] = recs[i].t[2];
+    velrel[i] = recs[i].vr;
+  }
+  return 0;
+}
+
+int sdem_check_restart_limit(sdem_h* h) {
+  if (!h) return SDEM_E_ARG;
+  std::vector<CRec> recs;
+  int rc = gather_contacts(h, recs);
+  if (rc) return rc;
+  size_t i = 0;
+  while (i < recs.size()) {
+    size_t j = i;
+    while (j < recs.size() && recs[j].owner == recs[i].owner) j++;
+    if (j - i > 20) return set_err(h, SDEM_E_NCV20, "CL_Count_Cntctlink: so big ncv (more than 20 contacts on particle " +
+                                                        std::to_string(recs[i].owner) + ")");
+    i = j;
+  }
+  return 0;
+}
+
+int sdem_counters(sdem_h* h, int* out) {
+  if (!h || !out) return SDEM_E_ARG;
+  int rc = sync_and_check(h);
+  if (rc) return rc;
+  std::memcpy(out, h->h_counters, sizeof(int) * SDEM_CNT_SIZE);
+  return 0;
+}
+
+int sdem_launch_count(sdem_h* h, long long* n) {
+  if (!h || !n) return SDEM_E_ARG;
+  *n = h->launches;
+  return 0;
+}
+
+int sdem_profile_begin(sdem_h* h, int max_steps) {
+  if (!h || max_steps < 1) return SDEM_E_ARG;
+  for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
+  h->prof_ev.assign((size_t)max_steps * (kPhases + 1), nullptr);
+  for (auto& e : h->prof_ev) CK(cudaEventCreate(&e));
+  h->prof_cap = max_steps;
+  h->prof_steps = 0;
+  h->prof = true;
+  return 0;
+}
+
+int sdem_profile_end(sdem_h* h, int cap, double* ms, int* nsteps) {
+  if (!h || !ms || !nsteps) return SDEM_E_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  for (int p = 0; p < cap && p < kPhases; p++) ms[p] = 0.0;
+  for (int s = 0; s < h->prof_steps; s++) {
+    cudaEvent_t* ev = &h->prof_ev[(size_t)s * (kPhases + 1)];
+    for (int p = 0; p < kPhases && p < cap; p++) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, ev[p], ev[p + 1]));
+      ms[p] += t;
+    }
+  }
+  *nsteps = h->prof_steps;
+  for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
+  h->prof_ev.clear();
+  h->prof = false;
+  h->prof_steps = h->prof_cap = 0;
+  return kPhases;
+}
+
+const char* sdem_profile_phase_name(int i) { return (i >= 0 && i < kPhases) ? kPhaseNames[i] : ""; }
+
+const char* sdem_last_error(sdem_h* h) { return h ? h->err.c_str() : "null handle"; }
+
+void sdem_destroy(sdem_h* h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->h_counters) cudaFreeHost(h->h_counters);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+}  // extern "C"

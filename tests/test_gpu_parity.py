@@ -1,0 +1,184 @@
+"""Parity of the GB300 path (through the C ABI) with the CPU oracle.
+
+Bars: contact sets (particle-particle and particle-wall) equal; contact
+history, forces and torques within 1e-12 relative; counters equal.  The GPU
+sums every particle's contacts in the reference's scatter order, so the only
+floating-point difference left is ovrlp**1.5 / ovrlp**0.25 (sqrt forms vs
+libm pow, ~1 ulp) and pow(V, 0.4/0.2) (CUDA vs libm).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleSystem
+from sdem_gb300 import beds, props
+from sdem_gb300.capi import DEMSystem, SdemError
+from tests.helpers import assert_same_contact_sets, compare_history, force_scale, keyed_contacts
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12   # forces, torques and contact history (spec bar)
+
+
+def cloud(**kw):
+    base = dict(n=700, seed=11, box=(0.011, 0.011, 0.011), ntypes=7)
+    base.update(kw)
+    return beds.random_cloud_case(**base)
+
+
+CASES = {
+    "hertz_ab2": lambda: cloud(),
+    "lsd_ab2": lambda: cloud(seed=12, cf_type=props.CFT_LSD, ntypes=3),
+    "hertz_finite_walls": lambda: cloud(seed=13, finite_walls=True),
+    "hertz_ab3": lambda: cloud(seed=14, pi=3, pri=3),
+    "lsd_fe": lambda: cloud(seed=15, cf_type=props.CFT_LSD, pi=1, pri=1),
+    "hertz_ct2_noquirk": lambda: beds.scaled(cloud(seed=16), ct_model=2, quirk_ab2_rot=0),
+    "mono_one_type": lambda: cloud(seed=17, ntypes=1),
+}
+
+
+def compare_step(g, o, case, what):
+    cg, co = g.counters(), o.counters()
+    for k in ("pp", "pw", "cnsv", "nlocal"):
+        assert cg[k] == co[k], f"{what}: counter {k}: gpu {cg[k]} oracle {co[k]}"
+    kg = keyed_contacts(g, case.opts.base_wall_id)
+    ko = keyed_contacts(o, case.opts.base_wall_id)
+    assert_same_contact_sets(kg, ko, what)
+    compare_history(kg, ko, RTOL)
+    sg, so = g.state(), o.state()
+    np.testing.assert_array_equal(sg.id, so.id)
+    Fg, Tg = g.forces()
+    Fo, To = o.forces()
+    fs = force_scale(Fo, 1e-6 * max(np.abs(Fo).max(), 1e-30))
+    ts = force_scale(To, 1e-6 * max(np.abs(To).max(), 1e-30))
+    assert np.all(np.abs(Fg - Fo).max(axis=1) <= RTOL * fs), f"{what}: force mismatch"
+    assert np.all(np.abs(Tg - To).max(axis=1) <= RTOL * ts), f"{what}: torque mismatch"
+    # the state after the step: positions differ only through those forces
+    np.testing.assert_allclose(sg.posR, so.posR, rtol=1e-13, atol=1e-18)
+    vs = np.abs(so.linVel).max() + 1e-30
+    assert np.abs(sg.linVel - so.linVel).max() <= 1e-12 * vs
+    ws = np.abs(so.rotVel).max() + 1e-30
+    assert np.abs(sg.rotVel - so.rotVel).max() <= 1e-12 * ws
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_one_step_from_identical_inputs(gpu_lib, name):
+    case = CASES[name]()
+    g, o = DEMSystem(case), OracleSystem(case)
+    g.step(1)
+    o.step(1)
+    assert g.counters()["pp"] > 50, "case should have many contacts"
+    compare_step(g, o, case, name)
+
+
+@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "hertz_finite_walls"])
+def test_twenty_steps_resynchronised(gpu_lib, name):
+    """A chain of single steps, each from the oracle's state and contact list
+    (restart-file style), so chaos cannot hide or create a mismatch."""
+    case = CASES[name]()
+    o = OracleSystem(case)
+    for k in range(20):
+        st = o.state()
+        c = beds.Case(case.name, case.opts, case.tables, case.walls, st, contacts=o.contacts())
+        g = DEMSystem(c)
+        g.step(1)
+        o.step(1)
+        compare_step(g, o, case, f"{name} step {k}")
+        g.close()
+
+
+@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2"])
+def test_free_run_trajectory(gpu_lib, name):
+    """50 free-running steps: contact sets stay identical and the state within
+    a loose bound (differences start at ~1 ulp per step)."""
+    case = CASES[name]()
+    g, o = DEMSystem(case), OracleSystem(case)
+    for k in range(50):
+        g.step(1)
+        o.step(1)
+        kg = keyed_contacts(g, case.opts.base_wall_id)
+        ko = keyed_contacts(o, case.opts.base_wall_id)
+        assert_same_contact_sets(kg, ko, f"{name} free step {k}")
+    np.testing.assert_allclose(g.state().posR, o.state().posR, rtol=1e-11, atol=1e-15)
+
+
+def test_contact_history_upload(gpu_lib):
+    """Contacts handed over as a restart file lists them (both sides of every
+    pair) carry their spring history into the next step."""
+    case = CASES["hertz_ab2"]()
+    o = OracleSystem(case)
+    o.step(3)
+    st = o.state()
+    cont = o.contacts()
+    c = beds.Case(case.name, case.opts, case.tables, case.walls, st, contacts=cont)
+    g = DEMSystem(c)
+    kg0 = keyed_contacts(g, case.opts.base_wall_id)
+    ko0 = keyed_contacts(o, case.opts.base_wall_id)
+    assert_same_contact_sets(kg0, ko0, "after upload")
+    compare_history(kg0, ko0, 0.0)
+    o2 = OracleSystem(c)
+    g.step(1)
+    o2.step(1)
+    compare_step(g, o2, case, "restart chain")
+
+
+def test_upload_download_roundtrip(gpu_lib):
+    case = CASES["hertz_ab3"]()
+    g = DEMSystem(case)
+    s = g.state()
+    p = case.particles
+    for a, b in ((s.id, p.id), (s.ptype, p.ptype), (s.posR, p.posR), (s.linVel, p.linVel), (s.linAcc, p.linAcc),
+                 (s.theta, p.theta), (s.rotVel, p.rotVel), (s.rotAcc, p.rotAcc)):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_out_of_domain_delete_order(gpu_lib):
+    """Particles that leave the domain are deleted by swap-with-last in the
+    reference's five passes; the surviving order must match."""
+    case = cloud(seed=21, n=400)
+    case.walls.walls = case.walls.walls[1:]   # no floor
+    case.walls.flags = case.walls.flags[1:]
+    p = case.particles
+    rng = np.random.default_rng(5)
+    low = np.argsort(p.posR[:, 1])[:60]
+    p.linVel[low, :, 1] = -rng.uniform(20.0, 40.0, len(low))   # these fall out within a few steps
+    g, o = DEMSystem(case), OracleSystem(case)
+    for k in range(8):
+        g.step(1)
+        o.step(1)
+        np.testing.assert_array_equal(g.state().id, o.state().id)
+        assert g.counters()["nlocal"] == o.counters()["nlocal"]
+    assert g.counters()["nlocal"] < case.particles.n
+    compare_step(g, o, case, "after deletes")
+
+
+def test_deterministic(gpu_lib):
+    case = CASES["hertz_ab2"]()
+    a, b = DEMSystem(case), DEMSystem(case)
+    a.step(10)
+    b.step(10)
+    np.testing.assert_array_equal(a.state().posR, b.state().posR)
+    np.testing.assert_array_equal(a.forces()[0], b.forces()[0])
+
+
+def test_grid_error(gpu_lib):
+    case = cloud(seed=22, n=50)
+    case.particles.posR[3, 0] = 5.0   # far outside the padded grid
+    g = DEMSystem(case)
+    with pytest.raises(SdemError) as e:
+        g.step(1)
+    assert e.value.code == 6
+
+
+def test_row_capacity_error(gpu_lib):
+    case = beds.scaled(cloud(seed=23), max_contacts_per_particle=1)
+    g = DEMSystem(case)
+    with pytest.raises(SdemError) as e:
+        g.step(1)
+    assert e.value.code == 3
+
+
+def test_unsupported_options_are_refused(gpu_lib):
+    case = beds.scaled(cloud(seed=24, n=20), periodic=(1, 0, 0))
+    with pytest.raises(SdemError) as e:
+        DEMSystem(case)
+    assert e.value.code == 10

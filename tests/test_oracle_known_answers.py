@@ -1,0 +1,147 @@
+"""Known-answer tests that pin the CPU oracle (the reference ships no tests or
+golden vectors; these analytic cases pin the restated physics instead)."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleSystem
+from sdem_gb300 import beds, props
+from sdem_gb300.geometry import WallSet, box_walls
+
+
+def two_sphere_case(cf_type, v, e_n=0.9, mu=0.3, d=1e-3, dt=2e-8, pi=2, pri=1, E=None, walls=None, box=0.01):
+    if cf_type == props.CFT_LSD:
+        E = E or props.lsd_youngs_for_stiffness(1e4, 0.05, d, 2500.0, 0.3)
+    else:
+        E = E or 5e7
+    c = (mu, mu, 0.0, e_n, e_n)
+    t = props.build_tables(cf_type, [d], [2500.0], [E], [0.3], c, [E], [0.3], c)
+    o = beds.Options(dt=dt, minpoint=(0, 0, 0), maxpoint=(box, box, box), gravity=(0.0, 0.0, 0.0),
+                     cf_type=cf_type, pi_method=pi, pri_method=pri)
+    mid = box / 2
+    pos = np.array([[mid - 0.5005 * d, mid, mid], [mid + 0.5005 * d, mid, mid]])
+    vel = np.array([[v, 0, 0], [-v, 0, 0]])
+    p = beds.new_particles(pos, np.array([1, 1]), t.radius, vel, o.tsize, o.rsize)
+    return beds.Case("two", o, t, walls or WallSet(), p)
+
+
+def run_until_separated(sysm, max_steps=200000, chunk=200):
+    touched = False
+    for _ in range(max_steps // chunk):
+        sysm.step(chunk)
+        c = sysm.counters()["pp"]
+        touched = touched or c > 0
+        st = sysm.state()
+        gap = st.posR[1, 0] - st.posR[0, 0] - 2 * st.posR[0, 3]
+        if touched and c == 0 and gap > 0:
+            return st
+    raise AssertionError("spheres did not separate")
+
+
+@pytest.mark.parametrize("v", [0.05, 0.2])
+def test_lsd_head_on_restitution(v):
+    # Linear spring-dashpot with stiffness and damping frozen at first touch:
+    # the damping coefficient of Prtcl_Property.f90:237 gives restitution e_n.
+    case = two_sphere_case(props.CFT_LSD, v, e_n=0.9)
+    s = OracleSystem(case)
+    st = run_until_separated(s, chunk=50)
+    vout = st.linVel[1, 0, 0] - st.linVel[0, 0, 0]
+    ratio = vout / (2 * v)
+    assert abs(ratio - 0.9) < 0.01, ratio
+
+
+def test_hertz_head_on_restitution():
+    # Hertz damping of Prtcl_Property.f90:244 (an empirical fit): restitution
+    # close to e_n for a head-on impact.
+    case = two_sphere_case(props.CFT_NLIN, 0.2, e_n=0.8, dt=2e-8)
+    s = OracleSystem(case)
+    st = run_until_separated(s, chunk=200)
+    ratio = (st.linVel[1, 0, 0] - st.linVel[0, 0, 0]) / 0.4
+    assert abs(ratio - 0.8) < 0.05, ratio
+
+
+def test_momentum_conserved_in_head_on():
+    case = two_sphere_case(props.CFT_NLIN, 0.2, e_n=0.8, dt=2e-8)
+    s = OracleSystem(case)
+    s.step(400)
+    F, T = s.forces()
+    assert s.counters()["pp"] == 1
+    np.testing.assert_array_equal(F[0], -F[1])
+
+
+def test_ab2_free_fall_closed_form():
+    # AB2 with constant acceleration: v_n = v0 + n a dt, x_n = x0 + n v0 dt + a dt^2 (n^2-1)/2
+    t = props.build_tables(1, [1e-3], [2500.0], [1e7], [0.3], (0.3, 0.3, 0.1, 0.9, 0.9), [1e7], [0.3],
+                           (0.3, 0.3, 0.1, 0.9, 0.9))
+    o = beds.Options(dt=1e-4, minpoint=(0, 0, 0), maxpoint=(1, 1, 1), pi_method=2, pri_method=2)
+    p = beds.new_particles(np.array([[0.5, 0.9, 0.5]]), np.array([1]), t.radius, np.array([[0.0, 0.1, 0.0]]), 2, 2)
+    p.linAcc[:] = (0.0, -9.81, 0.0)  # AB history already holds the constant acceleration
+    s = OracleSystem(beds.Case("fall", o, t, WallSet(), p))
+    n = 100
+    s.step(n)
+    st = s.state()
+    a, dt = -9.81, 1e-4
+    assert st.linVel[0, 0, 1] == pytest.approx(0.1 + n * a * dt, rel=1e-12)
+    assert st.posR[0, 1] == pytest.approx(0.9 + n * 0.1 * dt + a * dt * dt * (n * n - 1) / 2, rel=1e-12)
+
+
+def test_ab2_rotation_quirk_reads_linear_velocity():
+    # Prtcl_Integration.f90:64: with PRI_Method=2 the rotation starts from linVel(1).
+    t = props.build_tables(1, [1e-3], [2500.0], [1e7], [0.3], (0.3, 0.3, 0.1, 0.9, 0.9), [1e7], [0.3],
+                           (0.3, 0.3, 0.1, 0.9, 0.9))
+    o = beds.Options(dt=1e-5, minpoint=(0, 0, 0), maxpoint=(1, 1, 1), pi_method=2, pri_method=2,
+                     gravity=(0.0, 0.0, 0.0))
+    p = beds.new_particles(np.array([[0.5, 0.5, 0.5]]), np.array([1]), t.radius, np.array([[0.3, 0.2, 0.1]]), 2, 2)
+    s = OracleSystem(beds.Case("q", o, t, WallSet(), p))
+    s.step(1)
+    np.testing.assert_array_equal(s.state().rotVel[0, 0], [0.3, 0.2, 0.1])
+    o2 = beds.Options(**{**o.__dict__, "quirk_ab2_rot": 0})
+    s2 = OracleSystem(beds.Case("q", o2, t, WallSet(), p))
+    s2.step(1)
+    np.testing.assert_array_equal(s2.state().rotVel[0, 0], [0.0, 0.0, 0.0])
+
+
+def test_wall_rebound():
+    # sphere dropped onto an infinite floor (no gravity): rebound ratio ~ e_n
+    e = 0.8
+    t = props.build_tables(2, [1e-3], [2500.0], [5e7], [0.3], (0.3, 0.3, 0.0, e, e), [5e7], [0.3],
+                           (0.3, 0.3, 0.0, e, e))
+    o = beds.Options(dt=2e-8, minpoint=(0, 0, 0), maxpoint=(0.01, 0.01, 0.01), gravity=(0.0, 0.0, 0.0), cf_type=2,
+                     pi_method=2, pri_method=1)
+    p = beds.new_particles(np.array([[0.005, 0.000501, 0.005]]), np.array([1]), t.radius,
+                           np.array([[0.0, -0.2, 0.0]]), 2, 1)
+    w = box_walls((0, 0, 0), (0.01, 0.01, 0.01))
+    s = OracleSystem(beds.Case("w", o, t, w, p))
+    touched = False
+    for _ in range(2000):
+        s.step(100)
+        c = s.counters()["pw"]
+        touched = touched or c > 0
+        if touched and c == 0:
+            break
+    v = s.state().linVel[0, 0, 1]
+    assert abs(v / 0.2 - e) < 0.05, v
+
+
+def test_coulomb_sliding_on_floor():
+    # a sphere pressed on the floor (gravity) and sliding: |F_t| = mu_k |F_n| once slipping
+    mu = 0.3
+    t = props.build_tables(2, [1e-3], [2500.0], [5e7], [0.3], (mu, mu, 0.0, 0.8, 0.8), [5e7], [0.3],
+                           (mu, mu, 0.0, 0.8, 0.8))
+    o = beds.Options(dt=1e-7, minpoint=(0, 0, 0), maxpoint=(0.01, 0.01, 0.01), gravity=(0.0, -9.81, 0.0), cf_type=2,
+                     pi_method=1, pri_method=1)
+    r = t.radius[0]
+    m = t.mass[0]
+    K = t.bpw[2]
+    delta = (m * 9.81 / K) ** (2.0 / 3.0)
+    p = beds.new_particles(np.array([[0.005, r - delta, 0.005]]), np.array([1]), t.radius,
+                           np.array([[0.1, 0.0, 0.0]]), 1, 1)
+    w = box_walls((0, 0, 0), (0.01, 0.01, 0.01))
+    s = OracleSystem(beds.Case("slide", o, t, w, p))
+    s.step(3000)
+    F, T = s.forces()
+    ft = math.hypot(F[0, 0], F[0, 2])
+    fn = abs(F[0, 1])
+    assert s.counters()["pw"] == 1
+    assert ft == pytest.approx(mu * fn, rel=1e-9)
