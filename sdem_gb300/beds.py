@@ -287,5 +287,41 @@ def random_cloud_case(n: int, seed: int, box=(0.01, 0.01, 0.01), ntypes: int = 5
     return Case(f"cloud_{n}_{seed}", opts, tables, walls, parts)
 
 
+def lattice_cloud_case(n: int, seed: int, nn: float = 1.05e-3, ntypes: int = 7, cf_type: int = props.CFT_NLIN,
+                       d_lo: float = 0.8e-3, d_hi: float = 1.2e-3, vmax: float = 0.3, pi: int = 2, pri: int = 2,
+                       dt: float = 1.0e-6, jitter: float = 0.02e-3, finite_walls: bool = False,
+                       margin: float = 0.8e-3) -> Case:
+    """Dense cloud for parity tests: an FCC lattice with nearest-neighbour
+    distance `nn`, random types (diameters spread over [d_lo, d_hi]), jitter
+    U(-jitter, jitter), velocities U(-vmax, vmax) and angular velocities
+    U(-50, 50) rad/s.  Neighbours whose radii sum exceeds their distance start
+    in contact, so the first step has several contacts per sphere."""
+    rng = np.random.default_rng(seed)
+    if cf_type == props.CFT_NLIN:
+        diam, tables = hertz_poly_tables(ntypes, d_lo, d_hi)
+    else:
+        diam = np.linspace(d_lo, d_hi, ntypes) if ntypes > 1 else np.array([0.5 * (d_lo + d_hi)])
+        E = props.lsd_youngs_for_stiffness(1.0e4, 0.05, float(diam.mean()), 2500.0, 0.3)
+        c = (0.3, 0.2, 0.1, 0.9, 0.9)
+        tables = props.build_tables(props.CFT_LSD, list(diam), [2500.0] * ntypes, [E] * ntypes, [0.3] * ntypes,
+                                    c, [E], [0.3], c)
+    cube = nn * math.sqrt(2.0)
+    m = int(math.ceil((n / 4.0) ** (1.0 / 3.0)))
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 3)
+    pos = ((g[:, None, :] + basis[None, :, :]).reshape(-1, 3) * cube)[:n] + margin
+    pos = pos + rng.uniform(-jitter, jitter, size=pos.shape)
+    box = tuple(float(v) for v in (pos.max(axis=0) + margin))
+    ptype = rng.integers(1, ntypes + 1, size=n).astype(np.int32)
+    vel = rng.uniform(-vmax, vmax, size=(n, 3))
+    opts = Options(dt=dt, minpoint=(0.0, 0.0, 0.0), maxpoint=box, cf_type=cf_type, pi_method=pi, pri_method=pri)
+    parts = new_particles(pos, ptype, tables.radius, vel, opts.tsize, opts.rsize)
+    parts.rotVel[:] = rng.uniform(-50.0, 50.0, size=(n, 1, 3))
+    # spheres near the walls already touch them
+    walls = box_walls((margin * 0.4, margin * 0.4, margin * 0.4), tuple(b - margin * 0.4 for b in box),
+                      infinite=not finite_walls, base_wall_id=opts.base_wall_id)
+    return Case(f"lattice_{n}_{seed}", opts, tables, walls, parts)
+
+
 def scaled(case: Case, **opt_changes) -> Case:
     return replace(case, opts=replace(case.opts, **opt_changes))

@@ -20,9 +20,9 @@ RTOL = 1e-12   # forces, torques and contact history (spec bar)
 
 
 def cloud(**kw):
-    base = dict(n=700, seed=11, box=(0.011, 0.011, 0.011), ntypes=7)
+    base = dict(n=800, seed=11, ntypes=7)
     base.update(kw)
-    return beds.random_cloud_case(**base)
+    return beds.lattice_cloud_case(**base)
 
 
 CASES = {
@@ -32,7 +32,7 @@ CASES = {
     "hertz_ab3": lambda: cloud(seed=14, pi=3, pri=3),
     "lsd_fe": lambda: cloud(seed=15, cf_type=props.CFT_LSD, pi=1, pri=1),
     "hertz_ct2_noquirk": lambda: beds.scaled(cloud(seed=16), ct_model=2, quirk_ab2_rot=0),
-    "mono_one_type": lambda: cloud(seed=17, ntypes=1),
+    "mono_one_type": lambda: cloud(seed=17, ntypes=1, nn=0.995e-3),
 }
 
 
@@ -140,7 +140,7 @@ def test_out_of_domain_delete_order(gpu_lib):
     p = case.particles
     rng = np.random.default_rng(5)
     low = np.argsort(p.posR[:, 1])[:60]
-    p.linVel[low, :, 1] = -rng.uniform(20.0, 40.0, len(low))   # these fall out within a few steps
+    p.linVel[low, :, 1] = -rng.uniform(200.0, 400.0, len(low))[:, None]   # these fall out within a few steps
     g, o = DEMSystem(case), OracleSystem(case)
     for k in range(8):
         g.step(1)
@@ -162,7 +162,7 @@ def test_deterministic(gpu_lib):
 
 def test_grid_error(gpu_lib):
     case = cloud(seed=22, n=50)
-    case.particles.posR[3, 0] = 5.0   # far outside the padded grid
+    case.particles.posR[3, 0] = 5.0   # far outside the padded grid (and the domain)
     g = DEMSystem(case)
     with pytest.raises(SdemError) as e:
         g.step(1)
