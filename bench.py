@@ -198,17 +198,12 @@ def our_arm(args):
         if dist:
             dist.barrier()
 
-    def allreduce(x, op):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
-        return float(t.item())
+    from sdem_gb300 import replicas
 
     from sdem_gb300 import build
     build.build()
     from sdem_gb300.capi import DEMSystem
-    seed = 2 + rank
+    seed = replicas.rank_seed(2, rank)
     case = make_case(args.n, seed)
     n = case.particles.n
     sysm = DEMSystem(case)
@@ -232,9 +227,8 @@ def our_arm(args):
     phases, nprof = sysm.profile_end()
     launches = sysm.launch_count() - l0
     cnt = sysm.counters()
-    ms_max = allreduce(ms, "max")
-    n_all = allreduce(float(n), "sum")
-    value = n_all * K / (ms_max * 1e-3)
+    value, t_max, n_all = replicas.aggregate(ms * 1e-3, n, K, device="cuda")
+    ms_max = t_max * 1e3
 
     # dominant kernel: the contact-force kernel (one thread per contact)
     C = cnt["pp"]
@@ -277,7 +271,7 @@ def our_arm(args):
         out = sys2.state()
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
-        el = allreduce(el, "max")
+        _, el, _ = replicas.aggregate(el, n, Ke, device="cuda")
         h2d = sum(getattr(st, f).nbytes for f in ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta",
                                                   "rotVel", "rotAcc"))
         d2h = sum(getattr(out, f).nbytes for f in ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta",
