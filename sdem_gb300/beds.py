@@ -151,7 +151,7 @@ def hertz_poly_tables(ntypes: int = 41, d_lo: float = 0.8e-3, d_hi: float = 1.2e
     return diam, tables
 
 
-def deposited_positions(rng, diam_of_particle: np.ndarray, box, floor_y: float, overlap: float,
+def deposited_positions(rng, diam_of_particle: np.ndarray, box, floor_y: float, overlap,
                         spacing: float, jitter: float):
     """Layer-by-layer deposition onto a body-centred column grid.
 
@@ -159,12 +159,16 @@ def deposited_positions(rng, diam_of_particle: np.ndarray, box, floor_y: float, 
     shifted by half a spacing in x and z.  Each sphere (lateral jitter
     U(-jitter, jitter)) is lowered until it rests on the highest of the floor,
     the spheres of the layer below and the sphere two layers below in its own
-    column, then sunk by `overlap`.  With spacing >= max diameter + 2*jitter no
-    two spheres of one layer touch.  Returns positions in placement order
-    (bottom layer first)."""
+    column, then sunk by `overlap` (a number, or a function of (layer, number
+    of layers) giving the sink of that layer).  With spacing >= max diameter +
+    2*jitter no two spheres of one layer touch.  Returns positions in
+    placement order (bottom layer first)."""
     n = len(diam_of_particle)
     r = 0.5 * diam_of_particle
     pos = np.zeros((n, 3))
+    per_even = (int((box[0] - spacing) / spacing) + 1) * (int((box[2] - spacing) / spacing) + 1)
+    n_layers = int(math.ceil(n / max(per_even - per_even ** 0.5, 1)))
+    sink = overlap if callable(overlap) else (lambda k, nl: overlap)
     done = 0
     layers = []   # per layer: (origin, x, z, y, r) grids with NaN where empty
     k = 0
@@ -199,7 +203,7 @@ def deposited_positions(rng, diam_of_particle: np.ndarray, box, floor_y: float, 
                     reach = (rr + sr) ** 2 - ((x - px[qx2, qz2]) ** 2 + (z - pz[qx2, qz2]) ** 2)
                     valid = ok & np.isfinite(sy) & (reach > 0)
                     y = np.where(valid, np.maximum(y, sy + np.sqrt(np.where(valid, reach, 0.0))), y)
-        y = y - overlap
+        y = y - sink(k, n_layers)
         pos[done:done + cnt] = np.stack([x, y, z], axis=1)
         grids = [np.full((nxl, nzl), np.nan) for _ in range(4)]
         for g, v in zip(grids, (x, z, y, rr)):
@@ -212,19 +216,37 @@ def deposited_positions(rng, diam_of_particle: np.ndarray, box, floor_y: float, 
     return pos
 
 
+def hydrostatic_sink(tables, ntypes: int, g: float = 9.81):
+    """Sink of each layer of a deposited column so that every resting contact
+    carries the weight above it: delta = (W / K)^(2/3) with W the weight of the
+    layers above (one sphere per layer in a column) and K the Hertz stiffness
+    coefficient of a mid-size pair (Prtcl_Property.f90:241-242)."""
+    mid = ntypes // 2
+    K = float(tables.bpp.reshape(ntypes, ntypes, 11)[mid, mid, 2])
+    m = float(tables.mass[mid])
+
+    def sink(k: int, n_layers: int) -> float:
+        above = max(n_layers - k, 1)
+        return (above * m * g / K) ** (2.0 / 3.0)
+    return sink
+
+
 def hertz_poly_case(n: int = 1_000_000, seed: int = 2, box=(0.1, 0.6, 0.1), ntypes: int = 41,
-                    dt: float = 1.0e-6, overlap: float = 1.0e-6, pi: int = 2, pri: int = 2) -> Case:
+                    dt: float = 1.0e-6, overlap=None, pi: int = 2, pri: int = 2) -> Case:
     """Polydisperse Hertz-Mindlin bed: d uniform in [0.8, 1.2] mm realised as
     `ntypes` discrete types (10 um steps for 41), density 2500 kg/m^3,
     E = 5e7 Pa, nu = 0.3, restitution 0.8, friction 0.4 (rolling 0.1), in a
     0.1 x 0.6 x 0.1 m box with a floor and four side walls, dt = 1e-6 s.
     Positions: seeded deposition onto a body-centred column grid (spacing
     1.3 mm, lateral jitter 0.05 mm), each sphere resting on its highest support
-    with `overlap` of sink, i.e. a packed bed just after deposition."""
+    with a sink that makes each resting contact carry the weight above it
+    (hydrostatic_sink), i.e. a packed bed close to static equilibrium along
+    its columns."""
     rng = np.random.default_rng(seed)
     diam, tables = hertz_poly_tables(ntypes)
     ptype = rng.integers(1, ntypes + 1, size=n).astype(np.int32)
-    pos = deposited_positions(rng, diam[ptype - 1], box, 0.0, overlap, spacing=1.3e-3, jitter=0.05e-3)
+    sink = overlap if overlap is not None else hydrostatic_sink(tables, ntypes)
+    pos = deposited_positions(rng, diam[ptype - 1], box, 0.0, sink, spacing=1.3e-3, jitter=0.05e-3)
     opts = Options(dt=dt, minpoint=(0.0, 0.0, 0.0), maxpoint=tuple(box), cf_type=props.CFT_NLIN,
                    pi_method=pi, pri_method=pri)
     vel = np.zeros((n, 3))

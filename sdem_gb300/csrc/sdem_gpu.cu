@@ -69,7 +69,7 @@ struct Dev {
   int tsize, rsize, pi, pri, quirk;
   sdem::LawCfg law;
   double3 g;
-  double cell, x0, y0, z0;
+  double cell, rcell, x0, y0, z0;
   int nx, ny, nz;
   long long ncell;
   double3 dmin, dmax;
@@ -272,7 +272,9 @@ __global__ void k_bin(Dev d) {
   if (p >= *d.n) return;
   dbl4 P = d.posr[p];
   double rpdx = P.x - d.x0, rpdy = P.y - d.y0, rpdz = P.z - d.z0;
-  double fx = floor(rpdx / d.cell), fy = floor(rpdy / d.cell), fz = floor(rpdz / d.cell);
+  // rpd/cell_len, IEEE-exact through the reciprocal of the cell size
+  double fx = floor(sdem::div_by(rpdx, d.cell, d.rcell)), fy = floor(sdem::div_by(rpdy, d.cell, d.rcell)),
+         fz = floor(sdem::div_by(rpdz, d.cell, d.rcell));
   // grid index is floor()+1 in [1, n]; 0-based here
   if (!(fx >= 0.0 && fx < (double)d.nx && fy >= 0.0 && fy < (double)d.ny && fz >= 0.0 && fz < (double)d.nz)) {
     raise(d, SDEM_E_GRID, p);
@@ -317,7 +319,6 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   int n = *d.n;
   unsigned long long cand = 0;
-  int nwc = 0;
   if (s < d.n_launch) {
     if (s >= n) {
       d.row_cnt[s] = 0;
@@ -392,9 +393,23 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
         for (int i = -1; i <= 1; i++) visit(ix + lx, iy - 1, iz + i);
       d.row_cnt[s] = cnt < K ? cnt : K;
 
-      // Wall contacts of this particle: FindContactsPW (Prtcl_ContactSearchPW.f90:308-317)
-      // walks the near-wall list front-first, i.e. the highest wall index first.
-      unsigned long long mask = d.near_mask[m];
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) cand += __shfl_down_sync(0xffffffffu, cand, o);
+  if ((threadIdx.x & 31) == 0 && cand) atomicAdd(&d.counters[0], cand);
+}
+
+// Wall contacts of each particle: FindContactsPW (Prtcl_ContactSearchPW.f90:308-317)
+// walks the near-wall list front-first, i.e. the highest wall index first.
+// Slots j < kKw per particle keep that order; the compact list feeds k_wall_force.
+__global__ void __launch_bounds__(kThreads) k_wall_detect(Dev d) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  int nwc = 0;
+  if (m < *d.n) {
+    unsigned long long mask = d.near_mask[m];
+    if (mask) {
+      const dbl4 Pm = d.posr[m];
+      const int ncap = d.ncap;
       while (mask) {
         int wi = 63 - __clzll((long long)mask);
         mask &= ~(1ull << wi);
@@ -412,18 +427,12 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
         }
         nwc++;
       }
-      d.w_cnt[m] = nwc < kKw ? nwc : kKw;
-      d.wh_cnt[d.gid[m]] = nwc < kKw ? nwc : kKw;
     }
+    d.w_cnt[m] = nwc < kKw ? nwc : kKw;
+    d.wh_cnt[d.gid[m]] = nwc < kKw ? nwc : kKw;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    cand += __shfl_down_sync(0xffffffffu, cand, o);
-    nwc += __shfl_down_sync(0xffffffffu, nwc, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (cand) atomicAdd(&d.counters[0], cand);
-    if (nwc) atomicAdd(&d.counters[1], (unsigned long long)nwc);
-  }
+  for (int o = 16; o > 0; o >>= 1) nwc += __shfl_down_sync(0xffffffffu, nwc, o);
+  if ((threadIdx.x & 31) == 0 && nwc) atomicAdd(&d.counters[1], (unsigned long long)nwc);
 }
 
 // One thread per wall contact: Find_insert on the particle's bucket (key = wall)
@@ -511,21 +520,15 @@ __global__ void __launch_bounds__(kThreads) k_force(Dev d) {
     int pid = m_lo ? m : q, pjd = m_lo ? q : m;
     const double* P = d.bpp + ((size_t)(d.ptype[pjd] - 1) * d.nT + (d.ptype[pid] - 1)) * SDEM_BP_SIZE;
     dbl4 Pi = d.posr[pid], Pj = d.posr[pjd];
-    // ovrlp = dr - sqrt(d2sum) of NBSM_FineSearch2 (Prtcl_NBS_Munjiza.f90:514-522),
-    // with the target as pid1 as there
-    double ovrlp;
-    {
-      const dbl4 A = m_lo ? Pi : Pj, B = m_lo ? Pj : Pi;
-      double dr = A.w + B.w;
-      double dx = A.x - B.x;
-      double d2sum = dx * dx;
-      double dy = A.y - B.y;
-      d2sum = dy * dy + d2sum;
-      double dz = A.z - B.z;
-      d2sum = dz * dz + d2sum;
-      ovrlp = dr - sqrt(d2sum);
-    }
-    r3 Norm_v = sdem::nv3(sdem::sub3(sdem::xyz(Pj), sdem::xyz(Pi)));
+    // Norm_v = Posj .nv. Posi (real4_nv, Prtcl_TypeDef.f90:268-281) and
+    // ovrlp = dr - sqrt(d2sum) (NBSM_FineSearch2, Prtcl_NBS_Munjiza.f90:514-522)
+    // share one length: d2sum = dz*dz + (dy*dy + dx*dx) is bitwise
+    // (sx*sx + sy*sy) + sz*sz for s = Posj - Posi (squares ignore the sign and
+    // a two-term IEEE sum is commutative).
+    const r3 sv = sdem::sub3(sdem::xyz(Pj), sdem::xyz(Pi));
+    const double normv = sdem::norm3(sv);
+    const double ovrlp = (Pi.w + Pj.w) - normv;
+    r3 Norm_v = (normv > 1.0000E-10) ? sdem::div3_rcp(sv, normv) : sdem::mk3(0.0, 0.0, 0.0);
     r3 S, M, Mr;
     sdem::force_law(d.law, P, sdem::xyz(d.vel0[pid]), sdem::xyz(d.vel0[pjd]), sdem::xyz(d.rv0[pid]),
                     sdem::xyz(d.rv0[pjd]), Pi.w, Pj.w, Norm_v, ovrlp, hist, S, M, Mr);
@@ -573,34 +576,28 @@ __global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
   const int ncap = d.ncap;
   const int s = d.sortpos[p];
   const dbl4 Pp = d.posr[p];
-  const double ri = Pp.w;
   r3 F = sdem::mk3(0.0, 0.0, 0.0), T = sdem::mk3(0.0, 0.0, 0.0);
 
-  // contact records hold ri*Moment (c_M, particle i = lower id) and rj*Moment
-  // (c_Mj) already: only the additions of the scatter run here
-  auto apply = [&](int c, bool p_lo) {
-    const dbl4 S = d.c_S[c], Mr = d.c_Mr[c];
-    if (p_lo) {
-      const dbl4 Ms = d.c_M[c];
-      F = sdem::add3(F, sdem::xyz(S));
-      T = sdem::add3(sdem::add3(T, sdem::xyz(Ms)), sdem::xyz(Mr));
-    } else {
-      const dbl4 Ms = d.c_Mj[c];
-      F = sdem::sub3(F, sdem::xyz(S));
-      T = sdem::sub3(sdem::add3(T, sdem::xyz(Ms)), sdem::xyz(Mr));
-    }
-  };
-  auto apply_in = [&](unsigned key) {
-    int c = d.row_off[key >> 6] + (int)(key & 63u);
-    apply(c, d.c_S[c].w == 0.0);   // p is the row's partner: particle i iff the target is not
-  };
-  auto apply_own = [&]() {
-    int a = d.row_off[s], cnt = d.row_cnt[s];
-    for (int j = 0; j < cnt; j++) apply(a + j, d.c_S[a + j].w != 0.0);
-  };
-
+  // The contact records of p in the reference's scatter order: in-list
+  // entries of earlier targets, p's own row, in-list entries of later
+  // targets, then wall contacts.  Their indices go to a small per-thread list
+  // first (integer work), so the FP64 additions run in one loop whose trip
+  // count is the warp's maximum, not once per branch.
   int nin = d.in_cnt[p];
   if (nin > d.Kin) nin = d.Kin;
+  const int own_a = d.row_off[s], own_n = d.row_cnt[s];
+  const int nwc = d.w_cnt[p];
+  // entry: (contact index << 1) | (p is particle i), or -(wall slot + 1)
+  int list[2 * kMaxK + kKw];
+  int nl = 0;
+  auto push = [&](int c, bool p_lo) { list[nl++] = (c << 1) | (p_lo ? 1 : 0); };
+  auto push_in = [&](unsigned key) {
+    const int c = d.row_off[key >> 6] + (int)(key & 63u);
+    push(c, d.c_S[c].w == 0.0);   // p is the row's partner: particle i iff the target is not
+  };
+  auto push_own = [&]() {
+    for (int j = 0; j < own_n; j++) push(own_a + j, d.c_S[own_a + j].w != 0.0);
+  };
   if (nin <= 8) {
     unsigned u[8];
 #pragma unroll
@@ -608,11 +605,11 @@ __global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
     sort_net<8>(u);
 #pragma unroll
     for (int k = 0; k < 8; k++)
-      if (k < nin && (int)(u[k] >> 6) < s) apply_in(u[k]);
-    apply_own();
+      if (k < nin && (int)(u[k] >> 6) < s) push_in(u[k]);
+    push_own();
 #pragma unroll
     for (int k = 0; k < 8; k++)
-      if (k < nin && (int)(u[k] >> 6) > s) apply_in(u[k]);
+      if (k < nin && (int)(u[k] >> 6) > s) push_in(u[k]);
   } else if (nin <= 16) {
     unsigned u[16];
 #pragma unroll
@@ -620,11 +617,11 @@ __global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
     sort_net<16>(u);
 #pragma unroll
     for (int k = 0; k < 16; k++)
-      if (k < nin && (int)(u[k] >> 6) < s) apply_in(u[k]);
-    apply_own();
+      if (k < nin && (int)(u[k] >> 6) < s) push_in(u[k]);
+    push_own();
 #pragma unroll
     for (int k = 0; k < 16; k++)
-      if (k < nin && (int)(u[k] >> 6) > s) apply_in(u[k]);
+      if (k < nin && (int)(u[k] >> 6) > s) push_in(u[k]);
   } else {
     unsigned e[kMaxK];
     for (int k = 0; k < nin; k++) {
@@ -634,18 +631,36 @@ __global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
       e[j + 1] = v;
     }
     int k = 0;
-    for (; k < nin && (int)(e[k] >> 6) < s; k++) apply_in(e[k]);
-    apply_own();
-    for (; k < nin; k++) apply_in(e[k]);
+    for (; k < nin && (int)(e[k] >> 6) < s; k++) push_in(e[k]);
+    push_own();
+    for (; k < nin; k++) push_in(e[k]);
   }
+  for (int j = 0; j < nwc; j++) list[nl++] = -(j + 1);
 
-  // wall contacts after all particle-particle ones, highest wall first
-  const int nwc = d.w_cnt[p];
-  for (int j = 0; j < nwc; j++) {
-    const size_t at = (size_t)j * ncap + p;
-    const dbl4 S = d.w_S[at], Ms = d.w_M[at], Mr = d.w_Mr[at];
-    F = sdem::add3(F, sdem::xyz(S));
-    T = sdem::add3(sdem::add3(T, sdem::xyz(Ms)), sdem::xyz(Mr));
+  for (int k = 0; k < nl; k++) {
+    const int e = list[k];
+    const int c = e >= 0 ? (e >> 1) : e;
+    const bool p_lo = e < 0 || (e & 1);
+    dbl4 S, Ms, Mr;
+    if (c >= 0) {
+      S = d.c_S[c];
+      Ms = p_lo ? d.c_M[c] : d.c_Mj[c];   // ri*Moment or rj*Moment
+      Mr = d.c_Mr[c];
+    } else {
+      const size_t at = (size_t)(-c - 1) * ncap + p;
+      S = d.w_S[at];
+      Ms = d.w_M[at];
+      Mr = d.w_Mr[at];
+    }
+    // F(pid) + (Fnij+Ftij) / F(pjd) - (Fnij+Ftij);
+    // T + r*Moment + Mrij / T + r*Moment - Mrij  (Prtcl_ContactForce_inc.f90:69-86)
+    if (p_lo) {
+      F = sdem::add3(F, sdem::xyz(S));
+      T = sdem::add3(sdem::add3(T, sdem::xyz(Ms)), sdem::xyz(Mr));
+    } else {
+      F = sdem::sub3(F, sdem::xyz(S));
+      T = sdem::sub3(sdem::add3(T, sdem::xyz(Ms)), sdem::xyz(Mr));
+    }
   }
   d.F[p] = sdem::d4(F, 0.0);
   d.T[p] = sdem::d4(T, 0.0);
@@ -987,6 +1002,7 @@ Dev make_dev(sdem_h* h) {
   d.law.dt = c.dt;
   d.g = make_double3(c.gravity[0], c.gravity[1], c.gravity[2]);
   d.cell = h->cell;
+  d.rcell = 1.0 / h->cell;
   d.x0 = h->x0;
   d.y0 = h->y0;
   d.z0 = h->z0;
@@ -1124,6 +1140,7 @@ int enqueue_step(sdem_h* h) {
   k_cellorder<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_SEARCH);
   k_search<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_wall_detect<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_SCAN_ROWS);
   scan(h, h->row_cnt, n, h->row_off);
   mark(PH_GID_INDEX);
@@ -1140,7 +1157,7 @@ int enqueue_step(sdem_h* h) {
   mark(PH_END);
   k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS);
   mark(kPhases);
-  L += 1 + 3 + 1 + 1 + 1 + 3 + 1 + 1 + 1 + 1 + 2 + 1;
+  L += 1 + 3 + 1 + 1 + 2 + 3 + 1 + 1 + 1 + 1 + 2 + 1;
   h->launches += L;
   if (ev) h->prof_steps++;
   h->cur = 1 - h->cur;
@@ -1234,6 +1251,8 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   }
   if (!(c.cs_ratio >= 1.0)) return bad("Prtcl_cs_ratio must be >= 1 for the one-level NBS search");
   if (c.n_capacity >= (1 << 26)) return bad("n_capacity must be < 2^26");
+  if ((long long)std::max(1, c.cntct_list_size) * c.n_capacity >= (1ll << 30))
+    return bad("cntct_list_size * n_capacity must be < 2^30");
   h->K = c.max_contacts_per_particle > 0 ? c.max_contacts_per_particle : 24;
   if (h->K > kMaxK) return bad("max_contacts_per_particle must be <= 64");
   *out = h;
