@@ -213,6 +213,7 @@ def our_arm(args):
     barrier()
     torch.cuda.synchronize()
     l0 = sysm.launch_count()
+    sums0 = sysm.counter_sums()
     sysm.profile_begin(K)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -227,11 +228,14 @@ def our_arm(args):
     phases, nprof = sysm.profile_end()
     launches = sysm.launch_count() - l0
     cnt = sysm.counters()
+    sums1 = sysm.counter_sums()
+    C_avg = (sums1["pp"] - sums0["pp"]) / max(sums1["steps"] - sums0["steps"], 1)
+    PW_avg = (sums1["pw"] - sums0["pw"]) / max(sums1["steps"] - sums0["steps"], 1)
     value, t_max, n_all = replicas.aggregate(ms * 1e-3, n, K, device="cuda")
     ms_max = t_max * 1e3
 
     # dominant kernel: the contact-force kernel (one thread per contact)
-    C = cnt["pp"]
+    C = C_avg
     dom = max(phases, key=phases.get)
     t_force = phases["force"] / nprof * 1e-3
     force_bytes = 80.0 * C          # per persistent contact: key, spring and VelRel_Init read + written
@@ -294,7 +298,8 @@ def our_arm(args):
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "n_particles": n, "contact_model": "Hertz-Mindlin",
                        "types": int(case.tables.n_types), "dt": case.opts.dt, "integrator": "AB2",
-                       "pp_contacts": C, "pw_contacts": cnt["pw"], "contacts_per_particle": C / n,
+                       "pp_contacts_avg": C, "pw_contacts_avg": PW_avg, "contacts_per_particle": C / n,
+                       "pp_contacts_last": cnt["pp"],
                        "bed": "seeded deposited packing (seed 2+rank), see sdem_gb300.beds.hertz_poly_case",
                        "l2": "state > L2 (no flush)", "parallelism": f"replicas x{ws}"},
             "e2e": e2e,

@@ -206,6 +206,9 @@ int sdem_download_forces(sdem_h* h, double* F, double* T);
 int sdem_counters(sdem_h* h, int* out);
 
 /* ---- diagnostics (no counterpart in the reference) ---------------------- */
+/* Sums since the last upload: out[0] particle-particle contacts over all
+ * steps, out[1] wall contacts, out[2] steps (averages over a timed window). */
+int sdem_counter_sums(sdem_h* h, long long* out);
 /* Number of kernel launches this handle has issued. */
 int sdem_launch_count(sdem_h* h, long long* n);
 /* Starts per-phase CUDA-event timing of the next max_steps steps. */

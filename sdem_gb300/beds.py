@@ -216,45 +216,137 @@ def deposited_positions(rng, diam_of_particle: np.ndarray, box, floor_y: float, 
     return pos
 
 
-def hydrostatic_sink(tables, ntypes: int, g: float = 9.81):
-    """Sink of each layer of a deposited column so that every resting contact
-    carries the weight above it: delta = (W / K)^(2/3) with W the weight of the
-    layers above (one sphere per layer in a column) and K the Hertz stiffness
-    coefficient of a mid-size pair (Prtcl_Property.f90:241-242)."""
-    mid = ntypes // 2
-    K = float(tables.bpp.reshape(ntypes, ntypes, 11)[mid, mid, 2])
-    m = float(tables.mass[mid])
+def settled_deposition(rng, ptype: np.ndarray, ids: np.ndarray, tables, box, spacing: float, jitter: float,
+                       gravity: float = 9.81, wall_type: int = 1):
+    """Deposition onto a body-centred column grid in static equilibrium along
+    its resting contacts.
 
-    def sink(k: int, n_layers: int) -> float:
-        above = max(n_layers - k, 1)
-        return (above * m * g / K) ** (2.0 / 3.0)
-    return sink
+    Geometry: layer by layer (even layers on the grid spacing/2 + i*spacing,
+    odd layers shifted by half a spacing in x and z, lateral jitter
+    U(-jitter, jitter)), every sphere rests on the highest of the floor and the
+    spheres of the four layers below -- its support.  Loads: the weight of a
+    sphere plus everything resting on it, summed from the top down.  Sinks:
+    from the bottom up, each sphere is lowered with its support and then by
+    delta/cos(theta) more, where delta = (N/K)^(2/3) is the Hertz overlap that
+    carries the normal load N = load/cos(theta) of the inclined contact, with
+    the pair's own K (the reference's table record of the lower-id sphere,
+    Prtcl_Property.f90:137-142, 241-242) or the wall's.  Positions in placement
+    order (bottom layer first)."""
+    n = len(ptype)
+    nT = len(tables.radius)
+    r = tables.radius[ptype - 1]
+    m = tables.mass[ptype - 1]
+    pos = np.zeros((n, 3))
+    sup = np.full(n, -1, dtype=np.int64)
+    layer_of = np.zeros(n, dtype=np.int64)
+    done = 0
+    layers = []   # per layer: (origin, x, z, y, r, global index) grids
+    k = 0
+    while done < n:
+        org = 0.5 * spacing + (0.5 * spacing if k % 2 else 0.0)
+        nxl = int((box[0] - org - 0.5 * spacing) / spacing) + 1
+        nzl = int((box[2] - org - 0.5 * spacing) / spacing) + 1
+        cnt = min(nxl * nzl, n - done)
+        gx, gz = np.divmod(np.arange(cnt), nzl)
+        xg = org + gx * spacing
+        zg = org + gz * spacing
+        x = xg + rng.uniform(-jitter, jitter, cnt)
+        z = zg + rng.uniform(-jitter, jitter, cnt)
+        rr = r[done:done + cnt]
+        y = rr.copy()
+        s_of = np.full(cnt, -1, dtype=np.int64)
+        for back in (1, 2, 3, 4):
+            if len(layers) < back:
+                continue
+            porg, px, pz, py, pr, pid = layers[-back]
+            pnx, pnz = px.shape
+            bx = np.floor((xg - porg) / spacing + 1e-9).astype(np.int64)
+            bz = np.floor((zg - porg) / spacing + 1e-9).astype(np.int64)
+            for dxs in (-1, 0, 1, 2):
+                for dzs in (-1, 0, 1, 2):
+                    qx = bx + dxs
+                    qz = bz + dzs
+                    ok = (qx >= 0) & (qx < pnx) & (qz >= 0) & (qz < pnz)
+                    qx2 = np.clip(qx, 0, pnx - 1)
+                    qz2 = np.clip(qz, 0, pnz - 1)
+                    sy = py[qx2, qz2]
+                    reach = (rr + pr[qx2, qz2]) ** 2 - ((x - px[qx2, qz2]) ** 2 + (z - pz[qx2, qz2]) ** 2)
+                    valid = ok & np.isfinite(sy) & (reach > 0)
+                    cand = np.where(valid, sy + np.sqrt(np.where(valid, reach, 0.0)), -np.inf)
+                    better = cand > y
+                    y = np.where(better, cand, y)
+                    s_of = np.where(better, pid[qx2, qz2], s_of)
+        sl = slice(done, done + cnt)
+        pos[sl] = np.stack([x, y, z], axis=1)
+        sup[sl] = s_of
+        layer_of[sl] = k
+        grids = [np.full((nxl, nzl), np.nan) for _ in range(4)]
+        for g_, v in zip(grids, (x, z, y, rr)):
+            g_[gx, gz] = v
+        gid_grid = np.full((nxl, nzl), -1, dtype=np.int64)
+        gid_grid[gx, gz] = np.arange(done, done + cnt)
+        layers.append((org, *grids, gid_grid))
+        done += cnt
+        k += 1
+    # loads, top down
+    load = m * gravity
+    for L in range(k - 1, -1, -1):
+        idx = np.nonzero(layer_of == L)[0]
+        s_ = sup[idx]
+        on = s_ >= 0
+        np.add.at(load, s_[on], load[idx[on]])
+    # sinks, bottom up
+    bpp = tables.bpp.reshape(nT, nT, 11)
+    bpw = tables.bpw.reshape(-1, nT, 11)
+    geo_y = pos[:, 1].copy()
+    for L in range(k):
+        idx = np.nonzero(layer_of == L)[0]
+        s_ = sup[idx]
+        on = s_ >= 0
+        cos_t = np.ones(len(idx))
+        K = bpw[wall_type - 1, ptype[idx] - 1, 2].copy()
+        base = np.zeros(len(idx))
+        if on.any():
+            a, b = idx[on], s_[on]
+            # a support far to the side would let the sphere roll off: the sink
+            # is computed with cos(theta) >= 0.3 there
+            cos_t[on] = np.maximum((geo_y[a] - geo_y[b]) / (r[a] + r[b]), 0.3)
+            lo = np.where(ids[a] < ids[b], a, b)
+            hi = np.where(ids[a] < ids[b], b, a)
+            K[on] = bpp[ptype[hi] - 1, ptype[lo] - 1, 2]
+            base[on] = geo_y[b] - pos[b, 1]   # the support's own sink
+        delta = (load[idx] / cos_t / K) ** (2.0 / 3.0)
+        pos[idx, 1] = geo_y[idx] - base - delta / cos_t
+    if pos[:, 1].max() + r.max() > box[1]:
+        raise ValueError("deposited bed is taller than the box")
+    return pos
 
 
 def hertz_poly_case(n: int = 1_000_000, seed: int = 2, box=(0.1, 0.6, 0.1), ntypes: int = 41,
-                    dt: float = 1.0e-6, overlap=None, pi: int = 2, pri: int = 2) -> Case:
+                    dt: float = 1.0e-6, pi: int = 2, pri: int = 2) -> Case:
     """Polydisperse Hertz-Mindlin bed: d uniform in [0.8, 1.2] mm realised as
     `ntypes` discrete types (10 um steps for 41), density 2500 kg/m^3,
     E = 5e7 Pa, nu = 0.3, restitution 0.8, friction 0.4 (rolling 0.1), in a
-    0.1 x 0.6 x 0.1 m box with a floor and four side walls, dt = 1e-6 s.
-    Positions: seeded deposition onto a body-centred column grid (spacing
-    1.3 mm, lateral jitter 0.05 mm), each sphere resting on its highest support
-    with a sink that makes each resting contact carry the weight above it
-    (hydrostatic_sink), i.e. a packed bed close to static equilibrium along
-    its columns."""
+    0.1 x 0.6 x 0.1 m box with a floor and four side walls, gravity -y,
+    dt = 1e-6 s.  Positions: settled_deposition (column grid spacing 1.3 mm,
+    lateral jitter 0.05 mm), a packed bed in static equilibrium along its
+    resting contacts, at rest.  Particle order and ids are a seeded shuffle
+    (the reference's maker also shuffles its particles, Prtcl_Variables.f90:279-288)."""
     rng = np.random.default_rng(seed)
     diam, tables = hertz_poly_tables(ntypes)
     ptype = rng.integers(1, ntypes + 1, size=n).astype(np.int32)
-    sink = overlap if overlap is not None else hydrostatic_sink(tables, ntypes)
-    pos = deposited_positions(rng, diam[ptype - 1], box, 0.0, sink, spacing=1.3e-3, jitter=0.05e-3)
+    perm = rng.permutation(n)            # storage position of the k-th placed sphere
+    ids = np.empty(n, dtype=np.int64)
+    ids[perm] = np.arange(1, n + 1)      # id = storage position + 1
+    ids = ids.astype(np.int64)
+    placed_ids = np.empty(n, dtype=np.int64)
+    placed_ids[:] = perm + 1
+    pos = settled_deposition(rng, ptype, placed_ids, tables, box, spacing=1.3e-3, jitter=0.05e-3)
     opts = Options(dt=dt, minpoint=(0.0, 0.0, 0.0), maxpoint=tuple(box), cf_type=props.CFT_NLIN,
                    pi_method=pi, pri_method=pri)
     vel = np.zeros((n, 3))
-    parts = new_particles(pos, ptype, tables.radius, vel, opts.tsize, opts.rsize)
-    # the reference's index order is unrelated to space (its maker shuffles,
-    # Prtcl_Variables.f90:279-288): shuffle the same way with the seed
-    perm = rng.permutation(n)
-    parts = parts.take(perm)
+    placed = new_particles(pos, ptype, tables.radius, vel, opts.tsize, opts.rsize)
+    parts = placed.take(np.argsort(perm))
     parts.id = np.arange(1, n + 1, dtype=np.int32)
     walls = box_walls(opts.minpoint, opts.maxpoint, infinite=True, base_wall_id=opts.base_wall_id)
     return Case(f"hertz_poly_{n}", opts, tables, walls, parts,

@@ -26,7 +26,7 @@ CNT_NAMES = ("pp", "ppg", "ppfix", "pw", "cnsv", "nlocal", "iter", "next_wall_up
 EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls", "sdem_upload_particles",
             "sdem_upload_contacts", "sdem_step", "sdem_step_async", "sdem_get_stream",
             "sdem_download_particles", "sdem_download_contacts", "sdem_check_restart_limit",
-            "sdem_download_forces", "sdem_counters", "sdem_launch_count", "sdem_profile_begin",
+            "sdem_download_forces", "sdem_counters", "sdem_counter_sums", "sdem_launch_count", "sdem_profile_begin",
             "sdem_profile_end", "sdem_profile_phase_name", "sdem_last_error", "sdem_destroy")
 
 
@@ -105,6 +105,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_download_forces.argtypes = [P, dp, dp]
     lib.sdem_counters.argtypes = [P, ip]
     lib.sdem_launch_count.argtypes = [P, C.POINTER(C.c_longlong)]
+    lib.sdem_counter_sums.argtypes = [P, C.POINTER(C.c_longlong)]
     lib.sdem_profile_begin.argtypes = [P, C.c_int]
     lib.sdem_profile_end.argtypes = [P, C.c_int, dp, ip]
     lib.sdem_profile_phase_name.argtypes = [C.c_int]
@@ -220,6 +221,11 @@ class DEMSystem:
         self._check(self.lib.sdem_download_contacts(self.h, max(m, 1), C.byref(nc), iptr(o), iptr(q), dptr(t),
                                                     dptr(v)))
         return o[:m], q[:m], t[:m], v[:m]
+
+    def counter_sums(self) -> dict:
+        out = (C.c_longlong * 3)()
+        self._check(self.lib.sdem_counter_sums(self.h, out))
+        return {"pp": out[0], "pw": out[1], "steps": out[2]}
 
     def launch_count(self) -> int:
         n = C.c_longlong()

@@ -119,7 +119,7 @@ struct Dev {
   const dbl4* wh_hist_prev;
   // status and scalars
   int* status;                    // [0] error code, [1] detail
-  unsigned long long* counters;   // [0] candidates, [1] PW contacts
+  unsigned long long* counters;   // [0] candidates, [1] PW contacts, [2..4] sums since upload: PP, PW, steps
   unsigned long long* red;        // [0] max |v| bits, [1] max |a| bits
   int* iter;
   int* next_update;
@@ -868,6 +868,9 @@ __global__ void k_step_end(Dev d, int* counters_out) {
   *d.iter += 1;
   counters_out[SDEM_CNT_ITER] = *d.iter;
   counters_out[SDEM_CNT_NEXTWALL] = *d.next_update;
+  d.counters[2] += (unsigned long long)d.row_off[d.n_launch];
+  d.counters[3] += d.counters[1];
+  d.counters[4] += 1ull;
   d.counters[0] = 0;
   d.counters[1] = 0;
   *d.out_cnt = 0;
@@ -931,7 +934,7 @@ struct sdem_h {
   int cur = 0;  // buffer written by the next step
   // device scalars
   int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
-  unsigned long long* ull = nullptr;  // counters[2], red[2]
+  unsigned long long* ull = nullptr;  // counters[5] (see Dev::counters), unused, red[2]
   int *out_list = nullptr, *moves = nullptr, *map_pos = nullptr, *map_id = nullptr;
   int* h_counters = nullptr;  // pinned
   bool stepped = false;
@@ -1092,7 +1095,7 @@ Dev make_dev(sdem_h* h) {
   d.wh_hist_prev = h->wh_hist[pv];
   d.status = h->scal + S_STATUS;
   d.counters = h->ull;
-  d.red = h->ull + 2;
+  d.red = h->ull + 6;
   d.iter = h->scal + S_ITER;
   d.next_update = h->scal + S_NEXT;
   d.out_cnt = h->scal + S_OUTCNT;
@@ -1308,7 +1311,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
     rc |= dalloc(h, &h->wh_hist[b], G * kKw);
   }
   rc |= dalloc(h, &h->scal, S_SIZE);
-  rc |= dalloc(h, &h->ull, 4);
+  rc |= dalloc(h, &h->ull, 8);
   rc |= dalloc(h, &h->out_list, kOutCap);
   rc |= dalloc(h, &h->moves, 1 + 2 * 5 * kOutCap + 5 * kOutCap);
   rc |= dalloc(h, &h->map_pos, 5 * kOutCap);
@@ -1483,7 +1486,7 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   int sc[S_SIZE] = {0};
   sc[S_N] = n;
   CK(cudaMemcpy(h->scal, sc, sizeof sc, cudaMemcpyHostToDevice));
-  CK(cudaMemset(h->ull, 0, sizeof(unsigned long long) * 4));
+  CK(cudaMemset(h->ull, 0, sizeof(unsigned long long) * 8));
   h->n_host = n;
   h->cur = 0;
   h->stepped = false;
@@ -1815,6 +1818,16 @@ int sdem_counters(sdem_h* h, int* out) {
   int rc = sync_and_check(h);
   if (rc) return rc;
   std::memcpy(out, h->h_counters, sizeof(int) * SDEM_CNT_SIZE);
+  return 0;
+}
+
+int sdem_counter_sums(sdem_h* h, long long* out) {
+  if (!h || !out) return SDEM_E_ARG;
+  int rc = sync_and_check(h);
+  if (rc) return rc;
+  unsigned long long v[3];
+  CK(cudaMemcpy(v, h->ull + 2, sizeof v, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 3; i++) out[i] = (long long)v[i];
   return 0;
 }
 
