@@ -220,7 +220,32 @@ int sdem_profile_end(sdem_h* h, int cap, double* ms, int* nsteps);
 /* Name of phase i ("" outside the range). */
 const char* sdem_profile_phase_name(int i);
 
-/* Message of the last failure on this handle ("" when none). */
+/* ---- allocation-free contact count (no counterpart in the reference) ------
+ * For callers that cannot allocate device memory -- a host running inside
+ * another framework's memory pool, or code between a pool reset and its next
+ * allocation -- yet hold a particle set on the device and need its contact
+ * count, e.g. to size buffers before creating a handle (sdem_create
+ * allocates).  It counts, for the n particles of d_posR (device memory,
+ * 4 doubles x, y, z, radius per particle, 32-byte aligned), the exact
+ * particle-particle contacts (numCntcts(1)) and the candidate pairs of the
+ * search (num_Cnsv_cntct) on the grid that sdem_create + sdem_set_types would
+ * build from cfg and the largest radius max_radius, and writes them to
+ * d_counts[0..1] (device memory).  It allocates nothing: its scratch is one
+ * fixed-size device array in the library (about 6.3 MB, held by every GPU
+ * that loads the library until the process exits), which limits n to
+ * SDEM_NOALLOC_MAX_PARTICLES and the grid to SDEM_NOALLOC_MAX_CELLS; larger
+ * inputs are refused with SDEM_E_CAPACITY.  The first call on a device looks
+ * up the array's device address, so make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (other streams or host
+ * threads) race.  The call returns after the work on `stream` finished; on
+ * failure sdem_last_error(NULL) gives the message. */
+#define SDEM_NOALLOC_MAX_PARTICLES 65536
+#define SDEM_NOALLOC_MAX_CELLS     524288
+int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, const double* d_posR,
+                                unsigned long long* d_counts, void* stream);
+
+/* Message of the last failure on this handle ("" when none); with h == NULL,
+ * the last failure of sdem_count_contacts_noalloc on the calling thread. */
 const char* sdem_last_error(sdem_h* h);
 
 void sdem_destroy(sdem_h* h);

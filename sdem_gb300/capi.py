@@ -27,7 +27,8 @@ EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls
             "sdem_upload_contacts", "sdem_step", "sdem_step_async", "sdem_get_stream",
             "sdem_download_particles", "sdem_download_contacts", "sdem_check_restart_limit",
             "sdem_download_forces", "sdem_counters", "sdem_counter_sums", "sdem_launch_count", "sdem_profile_begin",
-            "sdem_profile_end", "sdem_profile_phase_name", "sdem_last_error", "sdem_destroy")
+            "sdem_profile_end", "sdem_profile_phase_name", "sdem_count_contacts_noalloc", "sdem_last_error",
+            "sdem_destroy")
 
 
 class SdemCfg(C.Structure):
@@ -110,6 +111,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_profile_end.argtypes = [P, C.c_int, dp, ip]
     lib.sdem_profile_phase_name.argtypes = [C.c_int]
     lib.sdem_profile_phase_name.restype = C.c_char_p
+    lib.sdem_count_contacts_noalloc.argtypes = [C.POINTER(SdemCfg), C.c_double, C.c_int, P, P, P]
     lib.sdem_last_error.argtypes = [P]
     lib.sdem_last_error.restype = C.c_char_p
     lib.sdem_destroy.argtypes = [P]
@@ -133,6 +135,21 @@ def iptr(a: Optional[np.ndarray]):
         return None
     assert a.dtype == np.int32 and a.flags.c_contiguous
     return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+NOALLOC_MAX_PARTICLES = 65536
+NOALLOC_MAX_CELLS = 524288
+
+
+def count_contacts_noalloc(cfg: SdemCfg, max_radius: float, n: int, d_posR: int, d_counts: int,
+                           stream: int = 0) -> None:
+    """sdem_count_contacts_noalloc: device pointers in, device counts out, no
+    device allocation (see include/sdem_gpu.h)."""
+    lib = load()
+    rc = lib.sdem_count_contacts_noalloc(C.byref(cfg), float(max_radius), int(n), C.c_void_p(d_posR),
+                                         C.c_void_p(d_counts), C.c_void_p(stream))
+    if rc:
+        raise SdemError(rc, lib.sdem_last_error(None).decode())
 
 
 class DEMSystem:

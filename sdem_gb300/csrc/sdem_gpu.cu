@@ -878,6 +878,117 @@ __global__ void k_step_end(Dev d, int* counters_out) {
 }
 
 // ---------------------------------------------------------------------------
+// Allocation-free contact count (sdem_count_contacts_noalloc).
+//
+// Callers that cannot allocate device memory -- a host that runs inside
+// another framework's memory pool, or code between a pool reset and its next
+// allocation -- can still count the contacts of a particle set they already
+// hold on the device, e.g. to size their contact buffers before creating a
+// handle.  The scratch this needs (search grid, counting sort, prefilter copy)
+// is a file-scope device array of fixed size: every GPU that loads the library
+// holds it, ~6.3 MB, until the process exits.
+constexpr int kNaMaxN = 1 << 16;       // SDEM_NOALLOC_MAX_PARTICLES
+constexpr int kNaMaxCells = 1 << 19;   // SDEM_NOALLOC_MAX_CELLS
+constexpr int kNaBlocks = (kNaMaxCells + kScanTile - 1) / kScanTile;
+struct NoAllocScratch {
+  int cell_cnt[kNaMaxCells];
+  int cell_start[kNaMaxCells + 1];
+  int cell_of[kNaMaxN];
+  int tmp_rank[kNaMaxN];
+  int tmp_sorted[kNaMaxN];
+  int sorted[kNaMaxN];
+  int sortpos[kNaMaxN];
+  float4 spos[kNaMaxN];
+  int bsum[kNaBlocks];
+  int n;
+  int status[2];
+  unsigned long long counts[2];   // exact contacts, candidate pairs
+};
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+__global__ void k_na_begin(NoAllocScratch* S, int n) {
+  S->n = n;
+  S->status[0] = 0;
+  S->status[1] = 0;
+  S->counts[0] = 0ull;
+  S->counts[1] = 0ull;
+}
+
+// The search of k_search without its rows: the same half shell, the same
+// single-precision decision with the FP64 test in the ambiguous band; it only
+// counts numCntcts(1) and num_Cnsv_cntct.
+__global__ void __launch_bounds__(kThreads) k_na_count(Dev d, unsigned long long* counts) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long cand = 0, hits = 0;
+  if (s < *d.n) {
+    const int m = d.sorted[s];
+    const int key = d.cell_of[m];
+    const int iz = key % d.nz;
+    const int rest = key / d.nz;
+    const int ix = rest % d.nx;
+    const int iy = rest / d.nx;
+    const float4 Pf = d.spos[s];
+    const dbl4 Pm = d.posr[m];
+    const float margin = d.pf_margin;
+    auto test = [&](int t) {
+      const float4 Qf = d.spos[t];
+      const float fx = Pf.x - Qf.x, fy = Pf.y - Qf.y, fz = Pf.z - Qf.z;
+      const float d2f = fx * fx + fy * fy + fz * fz;
+      const float rs = Pf.w + Qf.w;
+      const float bhi = rs + margin;
+      if (d2f > bhi * bhi) return;
+      const float blo = rs - margin;
+      if (!(d2f < blo * blo)) {
+        const dbl4 Pq = d.posr[d.sorted[t]];
+        double dr = Pm.w + Pq.w;
+        double dr2 = dr * dr;
+        double dx = Pm.x - Pq.x;
+        double d2sum = dx * dx;
+        if (d2sum > dr2) return;
+        double dy = Pm.y - Pq.y;
+        d2sum = dy * dy + d2sum;
+        if (d2sum > dr2) return;
+        double dz = Pm.z - Pq.z;
+        d2sum = dz * dz + d2sum;
+        if (d2sum > dr2) return;
+      }
+      hits++;
+    };
+    {
+      const int b = d.cell_start[key + 1];
+      for (int t = s + 1; t < b; t++) test(t);
+      cand += (unsigned long long)(b - s - 1);
+    }
+    auto visit = [&](int cx, int cy, int cz) {
+      if (cx < 0 || cx >= d.nx || cy < 0 || cz < 0 || cz >= d.nz) return;
+      const long long k2 = ((long long)cy * d.nx + cx) * d.nz + cz;
+      const int a = d.cell_start[k2], b = d.cell_start[k2 + 1];
+      for (int t = a; t < b; t++) test(t);
+      cand += (unsigned long long)(b - a);
+    };
+    visit(ix, iy, iz - 1);
+    visit(ix - 1, iy, iz - 1);
+    visit(ix - 1, iy, iz);
+    visit(ix - 1, iy, iz + 1);
+    for (int lx = -1; lx <= 1; lx++)
+      for (int i = -1; i <= 1; i++) visit(ix + lx, iy - 1, iz + i);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cand += __shfl_down_sync(0xffffffffu, cand, o);
+    hits += __shfl_down_sync(0xffffffffu, hits, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (hits) atomicAdd(&counts[0], hits);
+    if (cand) atomicAdd(&counts[1], cand);
+  }
+}
+
+__global__ void k_na_end(const NoAllocScratch* S, unsigned long long* out) {
+  out[0] = S->counts[0];
+  out[1] = S->counts[1];
+}
+
+// ---------------------------------------------------------------------------
 // host side
 struct Buf {
   void* p = nullptr;
@@ -1198,6 +1309,12 @@ int sync_and_check(sdem_h* h) {
   return 0;
 }
 
+}  // namespace
+
+// Message of the last failed sdem_count_contacts_noalloc on this thread
+// (sdem_last_error(NULL) returns it).
+namespace {
+thread_local char g_noalloc_msg[160] = "";
 }  // namespace
 
 // ===========================================================================
@@ -1870,7 +1987,113 @@ int sdem_profile_end(sdem_h* h, int cap, double* ms, int* nsteps) {
 
 const char* sdem_profile_phase_name(int i) { return (i >= 0 && i < kPhases) ? kPhaseNames[i] : ""; }
 
-const char* sdem_last_error(sdem_h* h) { return h ? h->err.c_str() : "null handle"; }
+const char* sdem_last_error(sdem_h* h) { return h ? h->err.c_str() : g_noalloc_msg; }
+
+/* ---- allocation-free contact count ----------------------------------------
+ * Setup: the device address of the file-scope scratch array is looked up with
+ * cudaGetSymbolAddress once per device, by the first call on that device with
+ * it current; that first call should therefore come before any stream
+ * capture.  The array is shared by every call and keeps the last call's
+ * contents; the parts that must start at zero are cleared at the start of
+ * each call.  Calls that overlap on the GPU (different streams or host
+ * threads) race on the array. */
+namespace {
+NoAllocScratch* g_noalloc_addr[64] = {};
+
+int noalloc_fail(int code, const char* msg) {
+  std::snprintf(g_noalloc_msg, sizeof g_noalloc_msg, "%s", msg);
+  return code;
+}
+}  // namespace
+
+int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, const double* d_posR,
+                                unsigned long long* d_counts, void* stream) {
+  g_noalloc_msg[0] = 0;
+  if (!cfg || !d_counts || n < 0 || (n > 0 && !d_posR) || !(max_radius > 0.0))
+    return noalloc_fail(SDEM_E_ARG, "sdem_count_contacts_noalloc: bad arguments");
+  if (n > kNaMaxN)
+    return noalloc_fail(SDEM_E_CAPACITY, "sdem_count_contacts_noalloc: more than SDEM_NOALLOC_MAX_PARTICLES "
+                                         "(65536) particles");
+  if (((uintptr_t)d_posR & 31u) != 0 || ((uintptr_t)d_counts & 7u) != 0)
+    return noalloc_fail(SDEM_E_ARG, "sdem_count_contacts_noalloc: d_posR must be 32-byte aligned");
+  if (!(cfg->cs_ratio >= 1.0))
+    return noalloc_fail(SDEM_E_ARG, "sdem_count_contacts_noalloc: Prtcl_cs_ratio must be >= 1");
+  // Init_NBSM grid (Prtcl_NBS_Munjiza.f90:66-77), as sdem_set_types builds it
+  const double cell = cfg->cs_ratio * (2.0 * max_radius);
+  const double x0 = cfg->dom_min[0] - cell * 1.05, y0 = cfg->dom_min[1] - cell * 1.05, z0 = cfg->dom_min[2] - cell * 1.05;
+  const int nx = (int)((cfg->dom_max[0] + cell * 1.05 - x0) / cell) + 1;
+  const int ny = (int)((cfg->dom_max[1] + cell * 1.05 - y0) / cell) + 1;
+  const int nz = (int)((cfg->dom_max[2] + cell * 1.05 - z0) / cell) + 1;
+  const long long ncell = (long long)nx * ny * nz;
+  if (ncell > kNaMaxCells)
+    return noalloc_fail(SDEM_E_CAPACITY, "sdem_count_contacts_noalloc: the search grid has more than "
+                                         "SDEM_NOALLOC_MAX_CELLS (524288) cells");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return noalloc_fail(SDEM_E_CUDA, "sdem_count_contacts_noalloc: no usable CUDA device");
+  if (!g_noalloc_addr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return noalloc_fail(SDEM_E_CUDA, "sdem_count_contacts_noalloc: cudaGetSymbolAddress of the scratch failed");
+    g_noalloc_addr[dev] = (NoAllocScratch*)ptr;
+  }
+  NoAllocScratch* S = g_noalloc_addr[dev];
+  cudaStream_t st = (cudaStream_t)stream;
+  Dev d{};
+  d.ncap = kNaMaxN;
+  d.n_launch = n;
+  d.n = &S->n;
+  d.status = S->status;
+  d.cell = cell;
+  d.rcell = 1.0 / cell;
+  d.x0 = x0;
+  d.y0 = y0;
+  d.z0 = z0;
+  d.nx = nx;
+  d.ny = ny;
+  d.nz = nz;
+  d.ncell = ncell;
+  d.posr = (dbl4*)d_posR;
+  d.cell_of = S->cell_of;
+  d.cell_cnt = S->cell_cnt;
+  d.cell_start = S->cell_start;
+  d.tmp_rank = S->tmp_rank;
+  d.tmp_sorted = S->tmp_sorted;
+  d.sorted = S->sorted;
+  d.sortpos = S->sortpos;
+  d.spos = S->spos;
+  {
+    double ext = cell * (double)std::max(nx, std::max(ny, nz));
+    d.pf_margin = (float)(std::sqrt(3.0) * ext * std::ldexp(1.0, -22) + 16.0 * cell * std::ldexp(1.0, -23));
+  }
+  const int g = std::max(1, (n + kThreads - 1) / kThreads);
+  k_na_begin<<<1, 1, 0, st>>>(S, n);
+  if (cudaMemsetAsync(S->cell_cnt, 0, sizeof(int) * (size_t)ncell, st) != cudaSuccess)
+    return noalloc_fail(SDEM_E_CUDA, "sdem_count_contacts_noalloc: cudaMemsetAsync failed");
+  k_bin<<<g, kThreads, 0, st>>>(d);
+  {
+    const int nb = (int)std::max<long long>(1, (ncell + kScanTile - 1) / kScanTile);
+    k_scan_reduce<<<nb, 1024, 0, st>>>(S->cell_cnt, ncell, S->bsum);
+    k_scan_blocks<<<1, 1024, 0, st>>>(S->bsum, nb);
+    k_scan_apply<<<nb, 1024, 0, st>>>(S->cell_cnt, ncell, S->bsum, S->cell_start);
+  }
+  k_scatter<<<g, kThreads, 0, st>>>(d);
+  k_cellorder<<<g, kThreads, 0, st>>>(d);
+  k_na_count<<<g, kThreads, 0, st>>>(d, S->counts);
+  k_na_end<<<1, 1, 0, st>>>(S, d_counts);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return noalloc_fail(SDEM_E_CUDA, cudaGetErrorString(e));
+  if (cudaStreamSynchronize(st) != cudaSuccess)
+    return noalloc_fail(SDEM_E_CUDA, "sdem_count_contacts_noalloc: stream synchronisation failed");
+  int status = 0;
+  if (cudaMemcpy(&status, &S->status[0], sizeof status, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return noalloc_fail(SDEM_E_CUDA, "sdem_count_contacts_noalloc: status read failed");
+  if (status == SDEM_E_GRID)
+    return noalloc_fail(SDEM_E_GRID, "sdem_count_contacts_noalloc: a particle is outside the padded search grid");
+  if (status != 0) return noalloc_fail(status, "sdem_count_contacts_noalloc: device error");
+  return 0;
+}
 
 void sdem_destroy(sdem_h* h) {
   if (!h) return;
