@@ -52,6 +52,7 @@ constexpr int kKw = 4;            // wall contacts per particle
 constexpr int kMaxWalls = 64;     // near-wall mask is 64 bits
 constexpr int kOutCap = 4096;     // out-of-domain deletions per step
 constexpr int kScanTile = 4096;   // elements per scan block (1024 threads x 4)
+constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact records
 
 // Phases of one step, for the optional per-phase timing (sdem_profile_*).
 enum Phase { PH_WALL, PH_BIN, PH_SCAN_CELLS, PH_SCATTER, PH_CELLORDER, PH_SEARCH, PH_SCAN_ROWS, PH_GID_INDEX,
@@ -93,6 +94,7 @@ struct Dev {
   int *cell_of, *cell_cnt, *cell_start, *tmp_rank, *tmp_sorted, *sorted, *sortpos;
   float4* spos;      // cell-sorted single-precision copy (x-x0, y-y0, z-z0, r) for the prefilter
   float pf_margin;   // prefilter margin, bounds the single-precision distance error
+  float cellf;       // cell size in single precision
   // rows and in-lists
   int *row_cnt, *row_partner, *row_off;
   int* in_cnt;
@@ -115,6 +117,9 @@ struct Dev {
   dbl4 *w_S, *w_M, *w_Mr;
   int* wl;
   int* wl_cnt;
+  // gather order: particles bucketed by their number of contact records, so a
+  // warp's summation loops run the same trip count
+  int *deg_cnt, *deg_start, *deg_of, *deg_rank, *gorder;
   const int *wh_cnt_prev, *wh_wall_prev;
   const dbl4* wh_hist_prev;
   // status and scalars
@@ -307,7 +312,12 @@ __global__ void k_cellorder(Dev d) {
   d.sorted[a + rank] = p;
   d.sortpos[p] = a + rank;
   dbl4 P = d.posr[p];
-  d.spos[a + rank] = make_float4((float)(P.x - d.x0), (float)(P.y - d.y0), (float)(P.z - d.z0), (float)P.w);
+  // single-precision copy relative to the particle's own cell corner: all
+  // values are below one cell, so their rounding error is ~cell*2^-24
+  const int cz = key % d.nz, cr = key / d.nz;
+  const int cx = cr % d.nx, cy = cr / d.nx;
+  d.spos[a + rank] = make_float4((float)(P.x - (d.x0 + (double)cx * d.cell)), (float)(P.y - (d.y0 + (double)cy * d.cell)),
+                                 (float)(P.z - (d.z0 + (double)cz * d.cell)), (float)P.w);
 }
 
 // ---------------------------------------------------------------------------
@@ -339,9 +349,10 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
       // reference's FP64 test (NBSM_FineSearch2, Prtcl_NBS_Munjiza.f90:514-522);
       // only candidates inside the band run the FP64 test here.  FP64 work left
       // in this divergent loop would occupy the FP64 pipe with one or two lanes.
-      auto test = [&](int t) {
+      // (ox, oy, oz): target cell corner minus candidate cell corner (0 or one cell)
+      auto test = [&](int t, float ox, float oy, float oz) {
         const float4 Qf = d.spos[t];
-        const float fx = Pf.x - Qf.x, fy = Pf.y - Qf.y, fz = Pf.z - Qf.z;
+        const float fx = (Pf.x - Qf.x) + ox, fy = (Pf.y - Qf.y) + oy, fz = (Pf.z - Qf.z) + oz;
         const float d2f = fx * fx + fy * fy + fz * fz;
         const float rs = Pf.w + Qf.w;
         const float bhi = rs + margin;
@@ -375,14 +386,15 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
       // same cell, particles after the target in list order
       {
         int b = d.cell_start[key + 1];
-        for (int t = s + 1; t < b; t++) test(t);
+        for (int t = s + 1; t < b; t++) test(t, 0.f, 0.f, 0.f);
         cand += (unsigned long long)(b - s - 1);
       }
       auto visit = [&](int cx, int cy, int cz) {
         if (cx < 0 || cx >= d.nx || cy < 0 || cz < 0 || cz >= d.nz) return;
         long long k2 = ((long long)cy * d.nx + cx) * d.nz + cz;
         int a = d.cell_start[k2], b = d.cell_start[k2 + 1];
-        for (int t = a; t < b; t++) test(t);
+        const float ox = (float)(ix - cx) * d.cellf, oy = (float)(iy - cy) * d.cellf, oz = (float)(iz - cz) * d.cellf;
+        for (int t = a; t < b; t++) test(t, ox, oy, oz);
         cand += (unsigned long long)(b - a);
       };
       visit(ix, iy, iz - 1);
@@ -428,11 +440,34 @@ __global__ void __launch_bounds__(kThreads) k_wall_detect(Dev d) {
         nwc++;
       }
     }
-    d.w_cnt[m] = nwc < kKw ? nwc : kKw;
-    d.wh_cnt[d.gid[m]] = nwc < kKw ? nwc : kKw;
+    const int nw_c = nwc < kKw ? nwc : kKw;
+    d.w_cnt[m] = nw_c;
+    d.wh_cnt[d.gid[m]] = nw_c;
+    int deg = min(d.in_cnt[m], d.Kin) + d.row_cnt[d.sortpos[m]] + nw_c;
+    deg = deg < kDegBuckets - 1 ? deg : kDegBuckets - 1;
+    d.deg_of[m] = deg;
+    d.deg_rank[m] = atomicAdd(&d.deg_cnt[deg], 1);
   }
   for (int o = 16; o > 0; o >>= 1) nwc += __shfl_down_sync(0xffffffffu, nwc, o);
   if ((threadIdx.x & 31) == 0 && nwc) atomicAdd(&d.counters[1], (unsigned long long)nwc);
+}
+
+__global__ void k_degree_scan(Dev d) {
+  // one warp: exclusive scan of the kDegBuckets counts, highest degree first
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int b = kDegBuckets - 1; b >= 0; b--) {
+      d.deg_start[b] = acc;
+      acc += d.deg_cnt[b];
+      d.deg_cnt[b] = 0;   // ready for the next step
+    }
+  }
+}
+
+__global__ void k_degree_scatter(Dev d) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *d.n) return;
+  d.gorder[d.deg_start[d.deg_of[p]] + d.deg_rank[p]] = p;
 }
 
 // One thread per wall contact: Find_insert on the particle's bucket (key = wall)
@@ -571,8 +606,9 @@ __device__ __forceinline__ void sort_net(unsigned (&v)[N]) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= *d.n) return;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= *d.n) return;
+  const int p = d.gorder[tid];
   const int ncap = d.ncap;
   const int s = d.sortpos[p];
   const dbl4 Pp = d.posr[p];
@@ -930,9 +966,9 @@ __global__ void __launch_bounds__(kThreads) k_na_count(Dev d, unsigned long long
     const float4 Pf = d.spos[s];
     const dbl4 Pm = d.posr[m];
     const float margin = d.pf_margin;
-    auto test = [&](int t) {
+    auto test = [&](int t, float ox, float oy, float oz) {
       const float4 Qf = d.spos[t];
-      const float fx = Pf.x - Qf.x, fy = Pf.y - Qf.y, fz = Pf.z - Qf.z;
+      const float fx = (Pf.x - Qf.x) + ox, fy = (Pf.y - Qf.y) + oy, fz = (Pf.z - Qf.z) + oz;
       const float d2f = fx * fx + fy * fy + fz * fz;
       const float rs = Pf.w + Qf.w;
       const float bhi = rs + margin;
@@ -956,14 +992,15 @@ __global__ void __launch_bounds__(kThreads) k_na_count(Dev d, unsigned long long
     };
     {
       const int b = d.cell_start[key + 1];
-      for (int t = s + 1; t < b; t++) test(t);
+      for (int t = s + 1; t < b; t++) test(t, 0.f, 0.f, 0.f);
       cand += (unsigned long long)(b - s - 1);
     }
     auto visit = [&](int cx, int cy, int cz) {
       if (cx < 0 || cx >= d.nx || cy < 0 || cz < 0 || cz >= d.nz) return;
       const long long k2 = ((long long)cy * d.nx + cx) * d.nz + cz;
       const int a = d.cell_start[k2], b = d.cell_start[k2 + 1];
-      for (int t = a; t < b; t++) test(t);
+      const float ox = (float)(ix - cx) * d.cellf, oy = (float)(iy - cy) * d.cellf, oz = (float)(iz - cz) * d.cellf;
+        for (int t = a; t < b; t++) test(t, ox, oy, oz);
       cand += (unsigned long long)(b - a);
     };
     visit(ix, iy, iz - 1);
@@ -1042,6 +1079,7 @@ struct sdem_h {
   dbl4 *w_geo = nullptr, *w_S = nullptr, *w_M = nullptr, *w_Mr = nullptr;
   float4* spos = nullptr;
   float pf_margin = 0.f;
+  int *deg_cnt = nullptr, *deg_start = nullptr, *deg_of = nullptr, *deg_rank = nullptr, *gorder = nullptr;
   int cur = 0;  // buffer written by the next step
   // device scalars
   int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
@@ -1170,7 +1208,13 @@ Dev make_dev(sdem_h* h) {
   d.sorted = h->sorted;
   d.sortpos = h->sortpos;
   d.spos = h->spos;
+  d.deg_cnt = h->deg_cnt;
+  d.deg_start = h->deg_start;
+  d.deg_of = h->deg_of;
+  d.deg_rank = h->deg_rank;
+  d.gorder = h->gorder;
   d.pf_margin = h->pf_margin;
+  d.cellf = (float)h->cell;
   d.w_cnt = h->w_cnt;
   d.w_wall = h->w_wall;
   d.w_geo = h->w_geo;
@@ -1264,6 +1308,8 @@ int enqueue_step(sdem_h* h) {
   mark(PH_WALL_FORCE);
   k_wall_force<<<std::max(1, h->num_sms * 2), kThreads, 0, st>>>(d);
   mark(PH_GATHER);
+  k_degree_scan<<<1, 32, 0, st>>>(d);
+  k_degree_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
   k_gather_integrate<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_DELETE);
   k_delete<<<1, 1, 0, st>>>(d);
@@ -1271,7 +1317,7 @@ int enqueue_step(sdem_h* h) {
   mark(PH_END);
   k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS);
   mark(kPhases);
-  L += 1 + 3 + 1 + 1 + 2 + 3 + 1 + 1 + 1 + 1 + 2 + 1;
+  L += 1 + 3 + 1 + 1 + 2 + 3 + 1 + 1 + 1 + 3 + 2 + 1;
   h->launches += L;
   if (ev) h->prof_steps++;
   h->cur = 1 - h->cur;
@@ -1399,6 +1445,11 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->sorted, N);
   rc |= dalloc(h, &h->sortpos, N);
   rc |= dalloc(h, &h->spos, N);
+  rc |= dalloc(h, &h->deg_cnt, kDegBuckets);
+  rc |= dalloc(h, &h->deg_start, kDegBuckets);
+  rc |= dalloc(h, &h->deg_of, N);
+  rc |= dalloc(h, &h->deg_rank, N);
+  rc |= dalloc(h, &h->gorder, N);
   rc |= dalloc(h, &h->w_cnt, N);
   rc |= dalloc(h, &h->w_wall, (size_t)N * kKw);
   rc |= dalloc(h, &h->wl, (size_t)N * kKw);
@@ -1489,13 +1540,11 @@ int sdem_set_types(sdem_h* h, int nT, const double* radius, const double* mass, 
   h->nz = (int)((zed - h->z0) / h->cell) + 1;
   h->ncell = (long long)h->nx * h->ny * h->nz;
   // Single-precision prefilter of the search: coordinates are stored relative to
-  // the grid origin, so each is off by at most half an ulp of the grid extent;
-  // the margin is twice the resulting bound on the distance error plus the
-  // rounding of the squares and sums (relative 2^-23 of <= 2 cells).
-  {
-    double ext = h->cell * (double)std::max(h->nx, std::max(h->ny, h->nz));
-    h->pf_margin = (float)(std::sqrt(3.0) * ext * std::ldexp(1.0, -22) + 16.0 * h->cell * std::ldexp(1.0, -23));
-  }
+  // their cell corner (|value| < 1 cell), so each rounding (coordinate, radius,
+  // cell size, differences, squares and sums) is below cell*2^-23; their sum
+  // bounds the distance error by ~8*cell*2^-23, and the margin is four times
+  // that.
+  h->pf_margin = (float)(32.0 * h->cell * std::ldexp(1.0, -23));
   if (h->ncell >= (1ll << 31) - 1) return set_err(h, SDEM_E_ARG, "search grid has more than 2^31 cells");
   rc |= dalloc(h, &h->cell_cnt, (size_t)h->ncell);
   rc |= dalloc(h, &h->cell_start, (size_t)h->ncell + 1);
@@ -2063,10 +2112,8 @@ int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, c
   d.sorted = S->sorted;
   d.sortpos = S->sortpos;
   d.spos = S->spos;
-  {
-    double ext = cell * (double)std::max(nx, std::max(ny, nz));
-    d.pf_margin = (float)(std::sqrt(3.0) * ext * std::ldexp(1.0, -22) + 16.0 * cell * std::ldexp(1.0, -23));
-  }
+  d.pf_margin = (float)(32.0 * cell * std::ldexp(1.0, -23));
+  d.cellf = (float)cell;
   const int g = std::max(1, (n + kThreads - 1) / kThreads);
   k_na_begin<<<1, 1, 0, st>>>(S, n);
   if (cudaMemsetAsync(S->cell_cnt, 0, sizeof(int) * (size_t)ncell, st) != cudaSuccess)
