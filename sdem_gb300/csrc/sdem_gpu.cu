@@ -446,7 +446,15 @@ __global__ void __launch_bounds__(kThreads) k_wall_detect(Dev d) {
     int deg = min(d.in_cnt[m], d.Kin) + d.row_cnt[d.sortpos[m]] + nw_c;
     deg = deg < kDegBuckets - 1 ? deg : kDegBuckets - 1;
     d.deg_of[m] = deg;
-    d.deg_rank[m] = atomicAdd(&d.deg_cnt[deg], 1);
+    // warp-aggregated slot in the bucket: one atomic per distinct degree per warp
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, deg);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&d.deg_cnt[deg], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    d.deg_rank[m] = base + __popc(peers & ((1u << lane) - 1u));
   }
   for (int o = 16; o > 0; o >>= 1) nwc += __shfl_down_sync(0xffffffffu, nwc, o);
   if ((threadIdx.x & 31) == 0 && nwc) atomicAdd(&d.counters[1], (unsigned long long)nwc);
