@@ -16,7 +16,11 @@
  *   - plane-wall geometry          Prtcl_Geometry.f90:55-109, 185-261
  *   - acceleration, integration    Prtcl_DEMSystem.f90:166-181, 322-331;
  *                                  Prtcl_Integration.f90:15-88
- *   - one-rank out-of-domain delete (y pencil, no periodicity)
+ *   - one rank, y pencil: periodic ghost images (PC_Comm_For_Cntct,
+ *                                  Prtcl_Comm.f90:554-877), FineSearch3 + AddContactPPG +
+ *                                  ContactForce_PPG (Prtcl_NBS_Munjiza.f90:358-405, 535-557;
+ *                                  Prtcl_CL_and_CF.f90:173-195, 761-798)
+ *   - one-rank out-of-domain delete or periodic wrap (y pencil)
  *                                  Prtcl_Comm.f90:1569-1840 with GL_copy
  *                                  (Prtcl_Variables.f90:351-373), CL_copy
  *                                  (Prtcl_CL_and_CF.f90:449-458), CSPW_copy
@@ -97,6 +101,11 @@ typedef struct orc {
   double cell_len, xst_cs, yst_cs, zst_cs;
   int nx, ny, nz, mbox;
   int *bx, *by, *bz, *NextX, *NextY, *NextZ, *HeadY, *HeadX, *HeadX0;
+  /* periodic ghosts (GhostP_*, Prtcl_Variables.f90:69-73), 1-based */
+  int nGhost, mGhost;
+  int *GhostP_id, *GhostP_pType;
+  r4* GhostP_PosR;
+  r3 *GhostP_linVel, *GhostP_rotVel;
   int *HeadZ;  /* (0:1, 0:nz+1) stored [m*(nz+2) + iz] */
   int *HeadZ0; /* (0:2, 0:nz+1) */
   long long num_Cnsv;
@@ -271,7 +280,7 @@ static void init_nbsm(orc* h) {
   h->nx = (int)((xed_cs - h->xst_cs) / h->cell_len) + 1;
   h->ny = (int)((yed_cs - h->yst_cs) / h->cell_len) + 1;
   h->nz = (int)((zed_cs - h->zst_cs) / h->cell_len) + 1;
-  int mb = h->mlocal;
+  int mb = h->mlocal + (h->mGhost > 0 ? h->mGhost : 0);
   h->mbox = mb;
   free(h->bx); free(h->by); free(h->bz); free(h->NextX); free(h->NextY); free(h->NextZ);
   free(h->HeadY); free(h->HeadX); free(h->HeadX0); free(h->HeadZ); free(h->HeadZ0);
@@ -702,6 +711,157 @@ static void cl_remv_released(orc* h) {
 #define HZ(h, m, iz) ((h)->HeadZ[(m) * ((h)->nz + 2) + (iz)])
 #define HZ0(h, m, iz) ((h)->HeadZ0[(m) * ((h)->nz + 2) + (iz)])
 
+/* ---- periodic ghosts: PC_Comm_For_Cntct, y pencil, one rank --------------- */
+static void grow_nbs(orc* h);
+
+static void ghost_reserve(orc* h, int ng) {
+  if (ng <= h->mGhost) return;
+  int m = ng + ng / 2 + 16;
+  h->GhostP_id = (int*)realloc(h->GhostP_id, (size_t)(m + 1) * sizeof(int));
+  h->GhostP_pType = (int*)realloc(h->GhostP_pType, (size_t)(m + 1) * sizeof(int));
+  h->GhostP_PosR = (r4*)realloc(h->GhostP_PosR, (size_t)(m + 1) * sizeof(r4));
+  h->GhostP_linVel = (r3*)realloc(h->GhostP_linVel, (size_t)(m + 1) * sizeof(r3));
+  h->GhostP_rotVel = (r3*)realloc(h->GhostP_rotVel, (size_t)(m + 1) * sizeof(r3));
+  if (!h->GhostP_id || !h->GhostP_pType || !h->GhostP_PosR || !h->GhostP_linVel || !h->GhostP_rotVel) abort();
+  h->mGhost = m;
+}
+
+static void ghost_from_local(orc* h, int ng, int i) {
+  h->GhostP_id[ng] = h->id[i];
+  h->GhostP_pType[ng] = h->pType[i];
+  h->GhostP_PosR[ng] = h->PosR[i];
+  h->GhostP_linVel[ng] = LV(h, 1, i);
+  h->GhostP_rotVel[ng] = RV(h, 1, i);
+}
+
+static void ghost_from_ghost(orc* h, int ng, int i) {
+  h->GhostP_id[ng] = h->GhostP_id[i];
+  h->GhostP_pType[ng] = h->GhostP_pType[i];
+  h->GhostP_PosR[ng] = h->GhostP_PosR[i];
+  h->GhostP_linVel[ng] = h->GhostP_linVel[i];
+  h->GhostP_rotVel[ng] = h->GhostP_rotVel[i];
+}
+
+/* Prtcl_Comm.f90:554-877 (CASE y_axis) with every neighbour rank equal to this
+ * rank in the periodic directions: the ghost images within LenForCS (one
+ * search cell) of a periodic boundary, created in the reference's order --
+ * y first from the locals, then +x, -x, +z, -z each from the ghosts made so
+ * far and then from the locals. */
+static void comm_for_cntct(orc* h) {
+  const double L = h->cell_len;  /* LenForCS = Prtcl_cs_ratio * maxD */
+  const double* mn = h->cfg.dom_min;
+  const double* mx = h->cfg.dom_max;
+  const double Lx = mx[0] - mn[0], Ly = mx[1] - mn[1], Lz = mx[2] - mn[2];
+  int ng = 0, ngp;
+  if (h->cfg.periodic[1]) {
+    for (int i = 1; i <= h->nlocal; i++) {
+      double py = h->PosR[i].y;
+      if (py <= mn[1] + L) { ghost_reserve(h, ng + 1); ng++; ghost_from_local(h, ng, i); h->GhostP_PosR[ng].y = py + Ly; }
+      if (py >= mx[1] - L) { ghost_reserve(h, ng + 1); ng++; ghost_from_local(h, ng, i); h->GhostP_PosR[ng].y = py - Ly; }
+    }
+  }
+  if (h->cfg.periodic[0]) {
+    ngp = ng;
+    for (int i = 1; i <= ngp; i++) {
+      double px = h->GhostP_PosR[i].x;
+      if (px >= mx[0] - L) { ghost_reserve(h, ng + 1); ng++; ghost_from_ghost(h, ng, i); h->GhostP_PosR[ng].x = px - Lx; }
+    }
+    for (int i = 1; i <= h->nlocal; i++) {
+      double px = h->PosR[i].x;
+      if (px >= mx[0] - L) { ghost_reserve(h, ng + 1); ng++; ghost_from_local(h, ng, i); h->GhostP_PosR[ng].x = px - Lx; }
+    }
+    ngp = ng;
+    for (int i = 1; i <= ngp; i++) {
+      double px = h->GhostP_PosR[i].x;
+      if (px <= mn[0] + L && px >= mn[0]) { ghost_reserve(h, ng + 1); ng++; ghost_from_ghost(h, ng, i); h->GhostP_PosR[ng].x = px + Lx; }
+    }
+    for (int i = 1; i <= h->nlocal; i++) {
+      double px = h->PosR[i].x;
+      if (px <= mn[0] + L && px >= mn[0]) { ghost_reserve(h, ng + 1); ng++; ghost_from_local(h, ng, i); h->GhostP_PosR[ng].x = px + Lx; }
+    }
+  }
+  if (h->cfg.periodic[2]) {
+    ngp = ng;
+    for (int i = 1; i <= ngp; i++) {
+      double pz = h->GhostP_PosR[i].z;
+      if (pz >= mx[2] - L) { ghost_reserve(h, ng + 1); ng++; ghost_from_ghost(h, ng, i); h->GhostP_PosR[ng].z = pz - Lz; }
+    }
+    for (int i = 1; i <= h->nlocal; i++) {
+      double pz = h->PosR[i].z;
+      if (pz >= mx[2] - L) { ghost_reserve(h, ng + 1); ng++; ghost_from_local(h, ng, i); h->GhostP_PosR[ng].z = pz - Lz; }
+    }
+    ngp = ng;
+    for (int i = 1; i <= ngp; i++) {
+      double pz = h->GhostP_PosR[i].z;
+      if (pz <= mn[2] + L && pz >= mn[2]) { ghost_reserve(h, ng + 1); ng++; ghost_from_ghost(h, ng, i); h->GhostP_PosR[ng].z = pz + Lz; }
+    }
+    for (int i = 1; i <= h->nlocal; i++) {
+      double pz = h->PosR[i].z;
+      if (pz <= mn[2] + L && pz >= mn[2]) { ghost_reserve(h, ng + 1); ng++; ghost_from_local(h, ng, i); h->GhostP_PosR[ng].z = pz + Lz; }
+    }
+  }
+  h->nGhost = ng;
+  if (h->nlocal + ng > h->mbox) grow_nbs(h);
+}
+
+/* ContactForce_PPG, Prtcl_CL_and_CF.f90:761-798: force on the local particle only */
+static void contact_force_ppg(orc* h, int pid, int pjd, int ind, double ovrlp) {
+  const double* P = bp_pp(h, h->pType[pid], h->GhostP_pType[pjd]);
+  r3 S, M, Mr;
+  if (h->id[pid] < h->GhostP_id[pjd]) {
+    r4 Posi = h->PosR[pid], Posj = h->GhostP_PosR[pjd];
+    double ri = Posi.w, rj = Posj.w;
+    r3 Norm_v = nv_of(r3sub(r4xyz(Posj), r4xyz(Posi)));
+    contact_force(h, P, LV(h, 1, pid), h->GhostP_linVel[pjd], RV(h, 1, pid), h->GhostP_rotVel[pjd], ri, rj,
+                  Norm_v, ovrlp, ind, &S, &M, &Mr);
+    h->F[pid] = r3add(h->F[pid], S);
+    h->T[pid] = r3add(r3add(h->T[pid], r3scale(M, ri)), Mr);
+  } else {
+    r4 Posi = h->GhostP_PosR[pjd], Posj = h->PosR[pid];
+    double ri = Posi.w, rj = Posj.w;
+    r3 Norm_v = nv_of(r3sub(r4xyz(Posj), r4xyz(Posi)));
+    contact_force(h, P, h->GhostP_linVel[pjd], LV(h, 1, pid), h->GhostP_rotVel[pjd], RV(h, 1, pid), ri, rj,
+                  Norm_v, ovrlp, ind, &S, &M, &Mr);
+    h->F[pid] = r3sub(h->F[pid], S);
+    h->T[pid] = r3sub(r3add(h->T[pid], r3scale(M, rj)), Mr);
+  }
+}
+
+/* CL_AddContactPPG, Prtcl_CL_and_CF.f90:173-195 */
+static void add_contact_ppg(orc* h, int id1, int id2, double ovrlp) {
+  int item1, item2;
+  int gid2 = h->GhostP_id[id2];
+  find_insert(h, id1, gid2, &item1, &item2);
+  if (item1 > 0) {
+    h->CntctStatus[item2] = item1;
+    h->numCntcts[1]++;
+    contact_force_ppg(h, id1, id2, item2, ovrlp);
+  } else if (item1 == -1) {
+    fail(h, SDEM_E_BAD_ID, "CL_AddContactPPG: The inserted item's id is greater than allowed value");
+  } else {
+    fail(h, SDEM_E_CL_FULL, "CL_AddContactPPG: The container is full and there is no space for new item");
+  }
+}
+
+/* NBSM_FineSearch3, Prtcl_NBS_Munjiza.f90:535-557 (pid2 is the search index of a ghost) */
+static void fine_search3(orc* h, int pid1, int pid2) {
+  int gid = pid2 - h->nlocal;
+  double dx, dy, dz, dr, d2sum, dr2, ovrlp;
+  dr = h->PosR[pid1].w + h->GhostP_PosR[gid].w;
+  dr2 = dr * dr;
+  dx = h->PosR[pid1].x - h->GhostP_PosR[gid].x;
+  d2sum = dx * dx;
+  if (d2sum > dr2) return;
+  dy = h->PosR[pid1].y - h->GhostP_PosR[gid].y;
+  d2sum = dy * dy + d2sum;
+  if (d2sum > dr2) return;
+  dz = h->PosR[pid1].z - h->GhostP_PosR[gid].z;
+  d2sum = dz * dz + d2sum;
+  if (d2sum > dr2) return;
+  ovrlp = dr - sqrt(d2sum);
+  add_contact_ppg(h, pid1, gid, ovrlp);
+}
+
 /* NBSM_FineSearch2, :503-530 */
 static void fine_search2(orc* h, int pid1, int pid2) {
   double dx, dy, dz, dr, d2sum, dr2, ovrlp;
@@ -723,10 +883,11 @@ static void fine_search2(orc* h, int pid1, int pid2) {
 
 /* NBSM_clcBoxIndex, :163-212 (no fixed or ghost particles) */
 static int clc_box_index(orc* h) {
-  for (int i = 1; i <= h->nlocal; i++) {
-    double rpdx = h->PosR[i].x - h->xst_cs;
-    double rpdy = h->PosR[i].y - h->yst_cs;
-    double rpdz = h->PosR[i].z - h->zst_cs;
+  for (int i = 1; i <= h->nlocal + h->nGhost; i++) {
+    r4 P = (i <= h->nlocal) ? h->PosR[i] : h->GhostP_PosR[i - h->nlocal];
+    double rpdx = P.x - h->xst_cs;
+    double rpdy = P.y - h->yst_cs;
+    double rpdz = P.z - h->zst_cs;
     h->bx[i] = (int)floor(rpdx / h->cell_len) + 1;
     h->by[i] = (int)floor(rpdy / h->cell_len) + 1;
     h->bz[i] = (int)floor(rpdz / h->cell_len) + 1;
@@ -741,7 +902,7 @@ static int clc_box_index(orc* h) {
 
 static void build_y_list(orc* h) { /* :217-229 */
   for (int i = 1; i <= h->ny; i++) h->HeadY[i] = -1;
-  for (int i = 1; i <= h->nlocal; i++) {
+  for (int i = 1; i <= h->nlocal + h->nGhost; i++) {
     int iy = h->by[i];
     h->NextY[i] = h->HeadY[iy];
     h->HeadY[iy] = i;
@@ -783,25 +944,46 @@ static void build_z_list0(orc* h, int ix, int m) { /* :277-296 */
   }
 }
 
-/* NBSM_LoopNBSMask, :302-473 -- moving particles only (the ELSE branch) */
+/* NBSM_LoopNBSMask, :302-473: moving particles and their ghost images (the
+ * ghost branch :358-405 and the ELSE branch :406-469; no fixed particles) */
 static void loop_nbs_mask(orc* h, int iz) {
+  const int nl = h->nlocal;
   int m = HZ(h, 1, iz);
   while (m != -1) {
-    int n = h->NextZ[m];
-    while (n != -1) { fine_search2(h, m, n); h->num_Cnsv++; n = h->NextZ[n]; }
-    n = HZ(h, 1, iz - 1);
-    while (n != -1) { fine_search2(h, m, n); h->num_Cnsv++; n = h->NextZ[n]; }
-    for (int i = -1; i <= 1; i++) {
-      n = HZ(h, 0, iz + i);
-      while (n != -1) { fine_search2(h, m, n); h->num_Cnsv++; n = h->NextZ[n]; }
+    if (m > nl) {
+#define GHOST_VISIT(start) do { int n_ = (start); while (n_ != -1) { if (n_ <= nl) { fine_search3(h, n_, m); h->num_Cnsv++; } n_ = h->NextZ[n_]; } } while (0)
+      GHOST_VISIT(h->NextZ[m]);
+      GHOST_VISIT(HZ(h, 1, iz - 1));
+      for (int i = -1; i <= 1; i++) GHOST_VISIT(HZ(h, 0, iz + i));
+      for (int lx = 0; lx <= 2; lx++)
+        for (int i = -1; i <= 1; i++) GHOST_VISIT(HZ0(h, lx, iz + i));
+#undef GHOST_VISIT
+    } else {
+#define LOCAL_VISIT(start) do { int n_ = (start); while (n_ != -1) { if (n_ > nl) fine_search3(h, m, n_); else fine_search2(h, m, n_); h->num_Cnsv++; n_ = h->NextZ[n_]; } } while (0)
+      LOCAL_VISIT(h->NextZ[m]);
+      LOCAL_VISIT(HZ(h, 1, iz - 1));
+      for (int i = -1; i <= 1; i++) LOCAL_VISIT(HZ(h, 0, iz + i));
+      for (int lx = 0; lx <= 2; lx++)
+        for (int i = -1; i <= 1; i++) LOCAL_VISIT(HZ0(h, lx, iz + i));
+#undef LOCAL_VISIT
     }
-    for (int lx = 0; lx <= 2; lx++)
-      for (int i = -1; i <= 1; i++) {
-        n = HZ0(h, lx, iz + i);
-        while (n != -1) { fine_search2(h, m, n); h->num_Cnsv++; n = h->NextZ[n]; }
-      }
     m = h->NextZ[m];
   }
+}
+
+/* NBSM_clcBoxIndex regrow (:172-189): room for locals + ghosts */
+static void grow_nbs(orc* h) {
+  int sizen = (int)(1.2 * (double)h->mbox);
+  int need = h->nlocal + h->nGhost + 1;
+  if (sizen < need) sizen = need;
+  free(h->bx); free(h->by); free(h->bz); free(h->NextX); free(h->NextY); free(h->NextZ);
+  h->bx = (int*)xcalloc(sizen + 1, sizeof(int));
+  h->by = (int*)xcalloc(sizen + 1, sizeof(int));
+  h->bz = (int*)xcalloc(sizen + 1, sizeof(int));
+  h->NextX = (int*)xcalloc(sizen + 1, sizeof(int));
+  h->NextY = (int*)xcalloc(sizen + 1, sizeof(int));
+  h->NextZ = (int*)xcalloc(sizen + 1, sizeof(int));
+  h->mbox = sizen;
 }
 
 /* NBSM_ContactSearch, :118-158 */
@@ -1071,10 +1253,31 @@ static int out_of(orc* h, int i, int pass) {
 }
 
 /* PC_Comm_For_Exchange, y-pencil branch (Prtcl_Comm.f90:1569-1840) with one
- * rank and no periodic direction: five delete passes, each swap-with-last. */
+ * rank: five passes (y, +x, -x, +z, -z); a periodic direction wraps the
+ * positions (:1575-1582, :1612-1618, :1672-1678, ...), any other deletes the
+ * particles outside [min, max) by swap-with-last. */
 static void comm_for_exchange(orc* h) {
   int nlocal = h->nlocal;
+  const double* mn = h->cfg.dom_min;
+  const double* mx = h->cfg.dom_max;
   for (int pass = 0; pass < 5; pass++) {
+    int dir = pass == 0 ? 1 : (pass <= 2 ? 0 : 2);
+    if (h->cfg.periodic[dir]) {
+      double Lk = mx[dir] - mn[dir];
+      for (int i = 1; i <= nlocal; i++) {
+        double* c = dir == 0 ? &h->PosR[i].x : (dir == 1 ? &h->PosR[i].y : &h->PosR[i].z);
+        double v = *c;
+        if (pass == 0) {
+          if (v >= mx[1]) *c = v - Lk;
+          else if (v < mn[1]) *c = v + Lk;
+        } else if (pass == 1 || pass == 3) {
+          if (v >= mx[dir]) *c = v - Lk;
+        } else {
+          if (v < mn[dir]) *c = v + Lk;
+        }
+      }
+      continue;
+    }
     int i = 1;
     while (i <= nlocal) {
       if (out_of(h, i, pass)) {
@@ -1093,13 +1296,12 @@ static void comm_for_exchange(orc* h) {
 /* ---- one time step (DEMS_iterate, Prtcl_DEMSystem.f90:201-252) --------- */
 int orc_step(orc* h, int nsteps) {
   if (!h->have_types) return fail(h, SDEM_E_ARG, "orc_step: tables not set");
-  if (h->cfg.periodic[0] || h->cfg.periodic[1] || h->cfg.periodic[2])
-    return fail(h, SDEM_E_UNSUPPORTED, "orc_step: periodic directions are not restated");
   for (int s = 0; s < nsteps; s++) {
     /* DEMS_preIteration :322-331 */
     update_near_prtcls_pw(h, h->iterNumber);
     for (int i = 1; i <= h->nlocal; i++) { h->F[i] = zero_r3; h->T[i] = zero_r3; }
     cl_pre_iteration(h);
+    comm_for_cntct(h);
     if (nbsm_contact_search(h)) return h->err;
     find_contacts_pw(h);
     if (h->err) return h->err;
@@ -1216,5 +1418,6 @@ void orc_destroy(orc* h) {
   free(h->Bucket_PWCS); free(h->id_Wall); free(h->Next_PWCS);
   free(h->Radius); free(h->Mass); free(h->Inertia); free(h->bpp); free(h->bpw);
   free(h->walls);
+  free(h->GhostP_id); free(h->GhostP_pType); free(h->GhostP_PosR); free(h->GhostP_linVel); free(h->GhostP_rotVel);
   free(h);
 }
