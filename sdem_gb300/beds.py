@@ -437,5 +437,33 @@ def lattice_cloud_case(n: int, seed: int, nn: float = 1.05e-3, ntypes: int = 7, 
     return Case(f"lattice_{n}_{seed}", opts, tables, walls, parts)
 
 
+def periodic_lattice_case(n: int, seed: int, periodic=(1, 1, 1), nn: float = 1.05e-3, vmax: float = 0.3,
+                          offset: float = 0.3e-3, **kw) -> Case:
+    """lattice_cloud_case in a box whose periodic sides are whole FCC periods
+    (m cubes of nn*sqrt(2)), so spheres near a periodic face touch the images
+    of spheres near the opposite face exactly as they touch their lattice
+    neighbours.  Non-periodic sides get plane walls that the outermost spheres
+    touch by at most 10 um."""
+    jitter = kw.get("jitter", 0.02e-3)
+    cube = nn * math.sqrt(2.0)
+    if not (offset + jitter < 0.5 * cube):
+        raise ValueError("offset too large: the lattice would leave its periodic box")
+    m = int(math.ceil((n / 4.0) ** (1.0 / 3.0)))
+    case = lattice_cloud_case(n, seed, nn=nn, vmax=vmax, margin=offset, **kw)
+    p = case.particles
+    pos, r = p.posR[:, :3], p.posR[:, 3]
+    hi = list(case.opts.maxpoint)
+    wlo, whi = [0.0] * 3, [0.0] * 3
+    for k in range(3):
+        if periodic[k]:
+            hi[k] = m * cube
+        wlo[k] = float((pos[:, k] - r).min()) + 1.0e-5
+        whi[k] = float((pos[:, k] + r).max()) - 1.0e-5
+    opts = replace(case.opts, maxpoint=tuple(hi), periodic=tuple(int(v) for v in periodic))
+    walls = box_walls(tuple(wlo), tuple(whi), base_wall_id=opts.base_wall_id,
+                      skip_axes=[k for k in range(3) if periodic[k]])
+    return Case(f"periodic_{n}_{seed}_{''.join(str(int(v)) for v in periodic)}", opts, case.tables, walls, p)
+
+
 def scaled(case: Case, **opt_changes) -> Case:
     return replace(case, opts=replace(case.opts, **opt_changes))

@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libsdem_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-         "-Xcompiler", "-fno-strict-aliasing"]
+         "-Xcompiler", "-fno-strict-aliasing", "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:

@@ -30,11 +30,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/sdem_gpu.h"
@@ -53,6 +55,7 @@ constexpr int kMaxWalls = 64;     // near-wall mask is 64 bits
 constexpr int kOutCap = 4096;     // out-of-domain deletions per step
 constexpr int kScanTile = 4096;   // elements per scan block (1024 threads x 4)
 constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact records
+constexpr int kImgFlag = 1 << 30; // c_ogid bit: a pair with a periodic image (ids < 2^30)
 
 // Phases of one step, for the optional per-phase timing (sdem_profile_*).
 enum Phase { PH_WALL, PH_BIN, PH_SCAN_CELLS, PH_SCATTER, PH_CELLORDER, PH_SEARCH, PH_SCAN_ROWS, PH_GID_INDEX,
@@ -66,6 +69,15 @@ const char* const kPhaseNames[kPhases] = {"wall_refresh", "bin", "scan_cells", "
 struct Dev {
   int ncap, n_launch;
   int* n;  // device particle count (changes on deletion)
+  // periodic images: ghosts live at indices [n, n + ng) of the search arrays
+  // (gid, ptype, posr, vel0, rv0 and the binning/row arrays, stride nall)
+  int nall, nall_launch, gcap;
+  int* ng;
+  int* nt;   // n + ng: particles the search sees
+  int per[3];
+  double3 Lbox;
+  double lencs;   // LenForCS = Prtcl_cs_ratio * maxD (Prtcl_Comm.f90:80-81)
+  int *gflag, *goff;
   int max_gid, K, Kin, ccap;
   int tsize, rsize, pi, pri, quirk;
   sdem::LawCfg law;
@@ -105,8 +117,12 @@ struct Dev {
   dbl4* c_hist;
   const dbl4* c_hist_prev;
   dbl4 *c_S, *c_M, *c_Mj, *c_Mr;
-  int *sbg, *cbg;
-  const int *sbg_prev, *cbg_prev;
+  // contact history by the reference's bucket owner (Find_insert's bkt_id):
+  // the lower id for particle-particle pairs, the local particle for a pair
+  // with a periodic image; own_c lists this step's contacts of each owner id
+  int Ko;
+  int *own_cnt, *own_c;
+  const int *own_cnt_prev, *own_c_prev;
   int *wh_cnt, *wh_wall;
   dbl4* wh_hist;
   // wall contacts of this step: per particle up to kKw slots (decreasing wall
@@ -124,7 +140,8 @@ struct Dev {
   const dbl4* wh_hist_prev;
   // status and scalars
   int* status;                    // [0] error code, [1] detail
-  unsigned long long* counters;   // [0] candidates, [1] PW contacts, [2..4] sums since upload: PP, PW, steps
+  unsigned long long* counters;   // [0] candidates, [1] PW contacts, [2..4] sums since upload: PP, PW, steps,
+                                  // [5] contacts with periodic images (numCntcts(2))
   unsigned long long* red;        // [0] max |v| bits, [1] max |a| bits
   int* iter;
   int* next_update;
@@ -269,12 +286,98 @@ __global__ void k_wall_refresh_end(Dev d) {
 }
 
 // ---------------------------------------------------------------------------
+// Periodic images: PC_Comm_For_Cntct (Prtcl_Comm.f90:554-877, y pencil, one
+// rank).  Passes in the reference's order -- y (from the locals, up to two
+// images each), then +x, -x, +z, -z, each over the images made so far and
+// then the locals -- as ordered stream compactions: a flag per candidate
+// (images first, then locals), an exclusive scan, a scatter.  Candidate j of
+// a pass: j < gcap is image j (if j < ng), j >= gcap is local j - gcap.
+enum GhostPass { GP_Y = 0, GP_XP = 1, GP_XM = 2, GP_ZP = 3, GP_ZM = 4 };
+
+
+// number of images candidate P spawns in this pass
+__device__ __forceinline__ int ghost_count(const Dev& d, int pass, const dbl4& P) {
+  const double L = d.lencs;
+  switch (pass) {
+    case GP_Y: return (P.y <= d.dmin.y + L ? 1 : 0) + (P.y >= d.dmax.y - L ? 1 : 0);
+    case GP_XP: return P.x >= d.dmax.x - L ? 1 : 0;
+    case GP_XM: return (P.x <= d.dmin.x + L && P.x >= d.dmin.x) ? 1 : 0;
+    case GP_ZP: return P.z >= d.dmax.z - L ? 1 : 0;
+    default: return (P.z <= d.dmin.z + L && P.z >= d.dmin.z) ? 1 : 0;
+  }
+}
+
+__global__ void k_ghost_begin(Dev d) {
+  *d.ng = 0;
+  *d.nt = *d.n;
+}
+
+__global__ void k_ghost_flag(Dev d, int pass) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int len = d.gcap + d.n_launch;
+  if (j >= len) return;
+  const int n = *d.n, ng = *d.ng;
+  int src = -1;
+  if (j < d.gcap) {
+    if (pass != GP_Y && j < ng) src = n + j;
+  } else if (j - d.gcap < n) {
+    src = j - d.gcap;
+  }
+  d.gflag[j] = src >= 0 ? ghost_count(d, pass, d.posr[src]) : 0;
+}
+
+__global__ void k_ghost_scatter(Dev d, int pass) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int len = d.gcap + d.n_launch;
+  if (j >= len || d.gflag[j] == 0) return;
+  const int n = *d.n, ng = *d.ng;
+  const int src = j < d.gcap ? n + j : j - d.gcap;
+  const dbl4 P = d.posr[src];
+  int out = ng + d.goff[j];
+  auto emit = [&](int dir, double shift) {
+    if (out >= d.gcap) {
+      raise(d, SDEM_E_CAPACITY, out);
+      return;
+    }
+    const int g = n + out;
+    dbl4 Q = P;
+    if (dir == 0) Q.x = P.x + shift;
+    else if (dir == 1) Q.y = P.y + shift;
+    else Q.z = P.z + shift;
+    d.posr[g] = Q;
+    d.gid[g] = d.gid[src];
+    d.ptype[g] = d.ptype[src];
+    d.vel0[g] = d.vel0[src];
+    d.rv0[g] = d.rv0[src];
+    out++;
+  };
+  switch (pass) {
+    case GP_Y:
+      if (P.y <= d.dmin.y + d.lencs) emit(1, d.Lbox.y);
+      if (P.y >= d.dmax.y - d.lencs) emit(1, -d.Lbox.y);
+      break;
+    case GP_XP: emit(0, -d.Lbox.x); break;
+    case GP_XM: emit(0, d.Lbox.x); break;
+    case GP_ZP: emit(2, -d.Lbox.z); break;
+    default: emit(2, d.Lbox.z); break;
+  }
+}
+
+__global__ void k_ghost_count(Dev d) {
+  const int add = d.goff[d.gcap + d.n_launch];
+  int ng = *d.ng + add;
+  if (ng > d.gcap) ng = d.gcap;
+  *d.ng = ng;
+  *d.nt = *d.n + ng;
+}
+
+// ---------------------------------------------------------------------------
 // Binning: NBSM_clcBoxIndex (Prtcl_NBS_Munjiza.f90:193-198) + counting sort.
 // Linear cell key orders cells as the reference's sweep visits them:
 // row iy (outer), column ix, cell iz (inner).
 __global__ void k_bin(Dev d) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= *d.n) return;
+  if (p >= *d.nt) return;
   dbl4 P = d.posr[p];
   double rpdx = P.x - d.x0, rpdy = P.y - d.y0, rpdz = P.z - d.z0;
   // rpd/cell_len, IEEE-exact through the reciprocal of the cell size
@@ -293,7 +396,7 @@ __global__ void k_bin(Dev d) {
 
 __global__ void k_scatter(Dev d) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= *d.n) return;
+  if (p >= *d.nt) return;
   int key = d.cell_of[p];
   if (key < 0) return;
   d.tmp_sorted[d.cell_start[key] + d.tmp_rank[p]] = p;
@@ -303,7 +406,7 @@ __global__ void k_scatter(Dev d) {
 // pushes Y, X and Z lists front-first, Prtcl_NBS_Munjiza.f90:224-271).
 __global__ void k_cellorder(Dev d) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= *d.n) return;
+  if (p >= *d.nt) return;
   int key = d.cell_of[p];
   if (key < 0) return;
   int a = d.cell_start[key], b = d.cell_start[key + 1];
@@ -327,13 +430,17 @@ __global__ void k_cellorder(Dev d) {
 // cells iz-1..iz+1 -- the order of Prtcl_NBS_Munjiza.f90:409-468.
 __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int n = *d.n;
+  const int nt = *d.nt;
+  const int nloc = *d.n;
   unsigned long long cand = 0;
-  if (s < d.n_launch) {
-    if (s >= n) {
+  if (s < d.nall_launch) {
+    if (s >= nt) {
       d.row_cnt[s] = 0;
     } else {
       const int m = d.sorted[s];
+      // a periodic image as target pairs with local particles only
+      // (LoopNBSMask, Prtcl_NBS_Munjiza.f90:358-405 -> FineSearch3(n, m))
+      const bool m_img = m >= nloc;
       const int key = d.cell_of[m];
       const int iz = key % d.nz;
       const int rest = key / d.nz;
@@ -343,7 +450,7 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
       const dbl4 Pm = d.posr[m];
       const float margin = d.pf_margin;
       int cnt = 0;
-      const int K = d.K, Kin = d.Kin, ncap = d.ncap;
+      const int K = d.K, Kin = d.Kin, ncap = d.ncap, nall = d.nall;
       // The single-precision distance is within pf_margin of the exact one, so
       // outside the band |d - (ri+rj)| < pf_margin the FP32 test decides the
       // reference's FP64 test (NBSM_FineSearch2, Prtcl_NBS_Munjiza.f90:514-522);
@@ -351,6 +458,10 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
       // in this divergent loop would occupy the FP64 pipe with one or two lanes.
       // (ox, oy, oz): target cell corner minus candidate cell corner (0 or one cell)
       auto test = [&](int t, float ox, float oy, float oz) {
+        if (m_img) {
+          if (d.sorted[t] >= nloc) return;   // image-image pairs are not searched
+          cand++;
+        }
         const float4 Qf = d.spos[t];
         const float fx = (Pf.x - Qf.x) + ox, fy = (Pf.y - Qf.y) + oy, fz = (Pf.z - Qf.z) + oz;
         const float d2f = fx * fx + fy * fy + fz * fz;
@@ -374,10 +485,12 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
           if (d2sum > dr2) return;
         }
         if (cnt < K) {
-          d.row_partner[(size_t)cnt * ncap + s] = q;
-          int slot = atomicAdd(&d.in_cnt[q], 1);
-          if (slot < Kin) d.in_list[(size_t)slot * ncap + q] = ((unsigned)s << 6) | (unsigned)cnt;
-          else raise(d, SDEM_E_CL_FULL, q);
+          d.row_partner[(size_t)cnt * nall + s] = q;
+          if (q < nloc) {   // an image receives no force: it has no in-list
+            int slot = atomicAdd(&d.in_cnt[q], 1);
+            if (slot < Kin) d.in_list[(size_t)slot * ncap + q] = ((unsigned)s << 6) | (unsigned)cnt;
+            else raise(d, SDEM_E_CL_FULL, q);
+          }
         } else {
           raise(d, SDEM_E_CL_FULL, m);
         }
@@ -387,7 +500,7 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
       {
         int b = d.cell_start[key + 1];
         for (int t = s + 1; t < b; t++) test(t, 0.f, 0.f, 0.f);
-        cand += (unsigned long long)(b - s - 1);
+        if (!m_img) cand += (unsigned long long)(b - s - 1);
       }
       auto visit = [&](int cx, int cy, int cz) {
         if (cx < 0 || cx >= d.nx || cy < 0 || cz < 0 || cz >= d.nz) return;
@@ -395,7 +508,7 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
         int a = d.cell_start[k2], b = d.cell_start[k2 + 1];
         const float ox = (float)(ix - cx) * d.cellf, oy = (float)(iy - cy) * d.cellf, oz = (float)(iz - cz) * d.cellf;
         for (int t = a; t < b; t++) test(t, ox, oy, oz);
-        cand += (unsigned long long)(b - a);
+        if (!m_img) cand += (unsigned long long)(b - a);
       };
       visit(ix, iy, iz - 1);
       visit(ix - 1, iy, iz - 1);
@@ -509,13 +622,11 @@ __global__ void __launch_bounds__(kThreads) k_wall_force(Dev d) {
   }
 }
 
-// Per-id index of this step's rows, used by the next step's history lookup.
+// Empties this step's owner table for every local id (images never own).
 __global__ void k_gid_index(Dev d) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= *d.n) return;
-  int g = d.gid[d.sorted[s]];
-  d.sbg[g] = d.row_off[s];
-  d.cbg[g] = d.row_cnt[s];
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *d.n) return;
+  d.own_cnt[d.gid[p]] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -531,40 +642,47 @@ __device__ __forceinline__ int find_row(const int* __restrict__ off, int n, int 
 }
 
 __global__ void __launch_bounds__(kThreads) k_force(Dev d) {
-  const int n = *d.n;
-  const int C = d.row_off[d.n_launch];
+  const int nt = *d.nt;
+  const int nloc = *d.n;
+  const int C = d.row_off[d.nall_launch];
   if (C > d.ccap) {
     if (blockIdx.x == 0 && threadIdx.x == 0) raise(d, SDEM_E_CL_FULL, C);
     return;
   }
+  unsigned long long nimg = 0;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
-    int s = find_row(d.row_off, n, c);
+    int s = find_row(d.row_off, nt, c);
     int slot = c - d.row_off[s];
     int m = d.sorted[s];
-    int q = d.row_partner[(size_t)slot * d.ncap + s];
+    int q = d.row_partner[(size_t)slot * d.nall + s];
     int gm = d.gid[m], gq = d.gid[q];
-    // Find_insert: history of the pair from the previous step (either particle
-    // may have been its target then), else a new contact (TanDelta 0, VelRel -2).
-    dbl4 hist = make_dbl4(0.0, 0.0, 0.0, -2.0);
-    {
-      int a = d.sbg_prev[gm], k = d.cbg_prev[gm];
-      bool found = false;
-      for (int j = 0; j < k; j++)
-        if (d.c_pgid_prev[a + j] == gq) { hist = d.c_hist_prev[a + j]; found = true; break; }
-      if (!found) {
-        a = d.sbg_prev[gq];
-        k = d.cbg_prev[gq];
-        for (int j = 0; j < k; j++)
-          if (d.c_pgid_prev[a + j] == gm) { hist = d.c_hist_prev[a + j]; break; }
-      }
-    }
-    // the lower id is particle i of the pair (FineSearch2, Prtcl_NBS_Munjiza.f90:525-529)
+    // particle-particle (AddContactPP) or local-image (AddContactPPG) pair; the
+    // lower id is particle i of the force law either way
+    // (Prtcl_NBS_Munjiza.f90:525-529, Prtcl_CL_and_CF.f90:773-797)
+    const bool img = (m >= nloc) || (q >= nloc);
+    const int loc = (m >= nloc) ? q : m;     // the local particle of an image pair
+    const int oth = (loc == m) ? q : m;
     bool m_lo = gm < gq;
     int pid = m_lo ? m : q, pjd = m_lo ? q : m;
-    const double* P = d.bpp + ((size_t)(d.ptype[pjd] - 1) * d.nT + (d.ptype[pid] - 1)) * SDEM_BP_SIZE;
+    // Find_insert's bucket: the lower id's for PP, the local particle's for PPG
+    const int owner = img ? d.gid[loc] : (m_lo ? gm : gq);
+    const int partner = img ? d.gid[oth] : (m_lo ? gq : gm);
+    dbl4 hist = make_dbl4(0.0, 0.0, 0.0, -2.0);
+    {
+      const int k = d.own_cnt_prev[owner];
+      for (int j = 0; j < k; j++) {
+        const int e = d.own_c_prev[(size_t)owner * d.Ko + j];
+        if (d.c_pgid_prev[e] == partner) { hist = d.c_hist_prev[e]; break; }
+      }
+    }
+    // Prtcl_BnryProp(pType(lower id), pType(higher id)) for PP (:743),
+    // (pType(local), pType(image)) for PPG (:772)
+    const int ta = img ? d.ptype[loc] : d.ptype[pid];
+    const int tb = img ? d.ptype[oth] : d.ptype[pjd];
+    const double* P = d.bpp + ((size_t)(tb - 1) * d.nT + (ta - 1)) * SDEM_BP_SIZE;
     dbl4 Pi = d.posr[pid], Pj = d.posr[pjd];
     // Norm_v = Posj .nv. Posi (real4_nv, Prtcl_TypeDef.f90:268-281) and
-    // ovrlp = dr - sqrt(d2sum) (NBSM_FineSearch2, Prtcl_NBS_Munjiza.f90:514-522)
+    // ovrlp = dr - sqrt(d2sum) (NBSM_FineSearch2/3, Prtcl_NBS_Munjiza.f90:514-522)
     // share one length: d2sum = dz*dz + (dy*dy + dx*dx) is bitwise
     // (sx*sx + sy*sy) + sz*sz for s = Posj - Posi (squares ignore the sign and
     // a two-term IEEE sum is commutative).
@@ -575,14 +693,20 @@ __global__ void __launch_bounds__(kThreads) k_force(Dev d) {
     r3 S, M, Mr;
     sdem::force_law(d.law, P, sdem::xyz(d.vel0[pid]), sdem::xyz(d.vel0[pjd]), sdem::xyz(d.rv0[pid]),
                     sdem::xyz(d.rv0[pjd]), Pi.w, Pj.w, Norm_v, ovrlp, hist, S, M, Mr);
-    d.c_ogid[c] = gm;
-    d.c_pgid[c] = gq;
+    d.c_ogid[c] = owner | (img ? kImgFlag : 0);
+    d.c_pgid[c] = partner;
     d.c_hist[c] = hist;
     d.c_S[c] = sdem::d4(S, m_lo ? 1.0 : 0.0);  // .w: is the row's target particle i
     d.c_M[c] = sdem::d4(sdem::scale3(M, Pi.w), 0.0);   // ri*Moment
     d.c_Mj[c] = sdem::d4(sdem::scale3(M, Pj.w), 0.0);  // rj*Moment
     d.c_Mr[c] = sdem::d4(Mr, 0.0);
+    const int os = atomicAdd(&d.own_cnt[owner], 1);
+    if (os < d.Ko) d.own_c[(size_t)owner * d.Ko + os] = c;
+    else raise(d, SDEM_E_CL_FULL, owner);
+    nimg += img ? 1ull : 0ull;
   }
+  for (int o = 16; o > 0; o >>= 1) nimg += __shfl_down_sync(0xffffffffu, nimg, o);
+  if ((threadIdx.x & 31) == 0 && nimg) atomicAdd(&d.counters[5], nimg);
 }
 
 // ---------------------------------------------------------------------------
@@ -787,9 +911,28 @@ __global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
   }
   d.theta[p] = sdem::d4(th, 0.0);
 
-  // out-of-domain candidates for the delete passes (Prtcl_Comm.f90:1569-1840)
-  if (x.y >= d.dmax.y || x.y < d.dmin.y || x.x >= d.dmax.x || x.x < d.dmin.x || x.z >= d.dmax.z ||
-      x.z < d.dmin.z) {
+  // Comm_For_Exchange, y pencil, one rank (Prtcl_Comm.f90:1569-1840): a periodic
+  // direction wraps the position (passes y, +x, -x, +z, -z); the others delete
+  // what left [min, max), in k_delete.
+  if (d.per[0] || d.per[1] || d.per[2]) {
+    dbl4 Q = d.posr[p];
+    if (d.per[1]) {
+      if (Q.y >= d.dmax.y) Q.y = Q.y - d.Lbox.y;
+      else if (Q.y < d.dmin.y) Q.y = Q.y + d.Lbox.y;
+    }
+    if (d.per[0]) {
+      if (Q.x >= d.dmax.x) Q.x = Q.x - d.Lbox.x;
+      if (Q.x < d.dmin.x) Q.x = Q.x + d.Lbox.x;
+    }
+    if (d.per[2]) {
+      if (Q.z >= d.dmax.z) Q.z = Q.z - d.Lbox.z;
+      if (Q.z < d.dmin.z) Q.z = Q.z + d.Lbox.z;
+    }
+    d.posr[p] = Q;
+    x = sdem::xyz(Q);
+  }
+  if ((!d.per[1] && (x.y >= d.dmax.y || x.y < d.dmin.y)) || (!d.per[0] && (x.x >= d.dmax.x || x.x < d.dmin.x)) ||
+      (!d.per[2] && (x.z >= d.dmax.z || x.z < d.dmin.z))) {
     int k2 = atomicAdd(d.out_cnt, 1);
     if (k2 < kOutCap) d.out_list[k2] = p;
     else raise(d, SDEM_E_CAPACITY, p);
@@ -802,6 +945,7 @@ __global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
 // candidates only (positions of untouched particles equal their index).
 __device__ __forceinline__ bool out_pass(const Dev& d, int id, int pass) {
   dbl4 P = d.posr[id];
+  if (d.per[pass == 0 ? 1 : (pass <= 2 ? 0 : 2)]) return false;   // wrapped, not deleted
   switch (pass) {
     case 0: return P.y >= d.dmax.y || P.y < d.dmin.y;
     case 1: return P.x >= d.dmax.x;
@@ -903,8 +1047,9 @@ __global__ void k_apply_moves(Dev d) {
 }
 
 __global__ void k_step_end(Dev d, int* counters_out) {
-  counters_out[SDEM_CNT_PP] = d.row_off[d.n_launch];
-  counters_out[SDEM_CNT_PPG] = 0;
+  const int C = d.row_off[d.nall_launch];
+  counters_out[SDEM_CNT_PP] = C - (int)d.counters[5];
+  counters_out[SDEM_CNT_PPG] = (int)d.counters[5];
   counters_out[SDEM_CNT_PPFIX] = 0;
   counters_out[SDEM_CNT_PW] = (int)d.counters[1];
   counters_out[SDEM_CNT_CNSV] = (int)d.counters[0];
@@ -912,11 +1057,12 @@ __global__ void k_step_end(Dev d, int* counters_out) {
   *d.iter += 1;
   counters_out[SDEM_CNT_ITER] = *d.iter;
   counters_out[SDEM_CNT_NEXTWALL] = *d.next_update;
-  d.counters[2] += (unsigned long long)d.row_off[d.n_launch];
+  d.counters[2] += (unsigned long long)(C - (int)d.counters[5]);
   d.counters[3] += d.counters[1];
   d.counters[4] += 1ull;
   d.counters[0] = 0;
   d.counters[1] = 0;
+  d.counters[5] = 0;
   *d.out_cnt = 0;
   *d.wl_cnt = 0;
 }
@@ -1079,7 +1225,13 @@ struct sdem_h {
   int *row_cnt = nullptr, *row_partner = nullptr, *row_off = nullptr, *in_cnt = nullptr;
   unsigned* in_list = nullptr;
   int ccap = 0;
-  int *c_ogid = nullptr, *c_pgid[2] = {}, *sbg[2] = {}, *cbg[2] = {};
+  int *c_ogid = nullptr, *c_pgid[2] = {}, *own_cnt[2] = {}, *own_c[2] = {};
+  int nall = 0, gcap = 0;
+  int *gflag = nullptr, *goff = nullptr;
+  // particle-particle records as uploaded (reported until the first step):
+  // owner id, partner id, listed under the partner too
+  struct UpRec { int owner, partner; bool both; dbl4 hist; };
+  std::vector<UpRec> h_up;
   dbl4 *c_hist[2] = {}, *c_S = nullptr, *c_M = nullptr, *c_Mj = nullptr, *c_Mr = nullptr;
   int *wh_cnt[2] = {}, *wh_wall[2] = {};
   dbl4* wh_hist[2] = {};
@@ -1140,7 +1292,8 @@ int dalloc(sdem_h* h, T** p, size_t count) {
   return 0;
 }
 
-enum { S_N = 0, S_STATUS = 1, S_ITER = 3, S_NEXT = 4, S_OUTCNT = 5, S_WLCNT = 6, S_COUNTERS = 8, S_SIZE = 16 };
+enum { S_N = 0, S_STATUS = 1, S_ITER = 3, S_NEXT = 4, S_OUTCNT = 5, S_WLCNT = 6, S_NG = 7, S_COUNTERS = 8,
+       S_NT = 16, S_SIZE = 24 };
 
 Dev make_dev(sdem_h* h) {
   Dev d{};
@@ -1148,6 +1301,18 @@ Dev make_dev(sdem_h* h) {
   d.ncap = c.n_capacity;
   d.n_launch = h->n_host;
   d.n = h->scal + S_N;
+  d.nall = h->nall;
+  d.gcap = h->gcap;
+  d.nall_launch = h->n_host + h->gcap;
+  d.ng = h->scal + S_NG;
+  d.nt = h->scal + S_NT;
+  for (int k = 0; k < 3; k++) d.per[k] = c.periodic[k];
+  d.Lbox = make_double3(c.dom_max[0] - c.dom_min[0], c.dom_max[1] - c.dom_min[1], c.dom_max[2] - c.dom_min[2]);
+  d.lencs = h->cell;
+  d.dmin = make_double3(c.dom_min[0], c.dom_min[1], c.dom_min[2]);
+  d.dmax = make_double3(c.dom_max[0], c.dom_max[1], c.dom_max[2]);
+  d.gflag = h->gflag;
+  d.goff = h->goff;
   d.max_gid = c.max_gid;
   d.K = h->K;
   d.Kin = h->K;
@@ -1246,10 +1411,11 @@ Dev make_dev(sdem_h* h) {
   d.c_M = h->c_M;
   d.c_Mj = h->c_Mj;
   d.c_Mr = h->c_Mr;
-  d.sbg = h->sbg[cu];
-  d.cbg = h->cbg[cu];
-  d.sbg_prev = h->sbg[pv];
-  d.cbg_prev = h->cbg[pv];
+  d.Ko = h->K;
+  d.own_cnt = h->own_cnt[cu];
+  d.own_c = h->own_c[cu];
+  d.own_cnt_prev = h->own_cnt[pv];
+  d.own_c_prev = h->own_c[pv];
   d.wh_cnt = h->wh_cnt[cu];
   d.wh_wall = h->wh_wall[cu];
   d.wh_hist = h->wh_hist[cu];
@@ -1289,26 +1455,41 @@ int enqueue_step(sdem_h* h) {
   };
   long long L = 0;
   mark(PH_WALL);
-  if (h->nw > 0) {
-    k_wall_refresh<<<grid_for(n), kThreads, 0, st>>>(d);
-    k_wall_refresh_end<<<1, 1, 0, st>>>(d);
-    L += 2;
-  }
+  // the refresh schedule (Next_iter_update) advances with or without walls
+  k_wall_refresh<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_wall_refresh_end<<<1, 1, 0, st>>>(d);
+  L += 2;
   mark(PH_BIN);
+  const int na = n + h->gcap;   // search arrays: locals and their periodic images
+  k_ghost_begin<<<1, 1, 0, st>>>(d);
+  L += 1;
+  if (h->gcap > 0) {
+    const int per[3] = {h->cfg.periodic[0], h->cfg.periodic[1], h->cfg.periodic[2]};
+    const int passes[5] = {GP_Y, GP_XP, GP_XM, GP_ZP, GP_ZM};
+    const int pdir[5] = {1, 0, 0, 2, 2};
+    for (int k = 0; k < 5; k++) {
+      if (!per[pdir[k]]) continue;
+      k_ghost_flag<<<grid_for(na), kThreads, 0, st>>>(d, passes[k]);
+      scan(h, h->gflag, na, h->goff);
+      k_ghost_scatter<<<grid_for(na), kThreads, 0, st>>>(d, passes[k]);
+      k_ghost_count<<<1, 1, 0, st>>>(d);
+      L += 6;
+    }
+  }
   cudaMemsetAsync(h->cell_cnt, 0, sizeof(int) * (size_t)h->ncell, st);
   cudaMemsetAsync(h->in_cnt, 0, sizeof(int) * (size_t)std::max(n, 1), st);
-  k_bin<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_bin<<<grid_for(na), kThreads, 0, st>>>(d);
   mark(PH_SCAN_CELLS);
   scan(h, h->cell_cnt, h->ncell, h->cell_start);
   mark(PH_SCATTER);
-  k_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_scatter<<<grid_for(na), kThreads, 0, st>>>(d);
   mark(PH_CELLORDER);
-  k_cellorder<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_cellorder<<<grid_for(na), kThreads, 0, st>>>(d);
   mark(PH_SEARCH);
-  k_search<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_search<<<grid_for(na), kThreads, 0, st>>>(d);
   k_wall_detect<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_SCAN_ROWS);
-  scan(h, h->row_cnt, n, h->row_off);
+  scan(h, h->row_cnt, na, h->row_off);
   mark(PH_GID_INDEX);
   k_gid_index<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_FORCE);
@@ -1418,13 +1599,12 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
     *out = h;
     return SDEM_E_UNSUPPORTED;
   }
-  if (c.periodic[0] || c.periodic[1] || c.periodic[2]) {
-    h->err = "periodic directions are not implemented on the GPU";
-    *out = h;
-    return SDEM_E_UNSUPPORTED;
-  }
+  if (c.max_gid >= kImgFlag) return bad("max_gid must be < 2^30");
   if (!(c.cs_ratio >= 1.0)) return bad("Prtcl_cs_ratio must be >= 1 for the one-level NBS search");
-  if (c.n_capacity >= (1 << 26)) return bad("n_capacity must be < 2^26");
+  const int nper = (c.periodic[0] != 0) + (c.periodic[1] != 0) + (c.periodic[2] != 0);
+  // search positions pack into 26 bits; each periodic direction at most
+  // doubles the particles the search sees (locals + images)
+  if (((long long)c.n_capacity << nper) >= (1LL << 26)) return bad("n_capacity * 2^(periodic directions) must be < 2^26");
   if ((long long)std::max(1, c.cntct_list_size) * c.n_capacity >= (1ll << 30))
     return bad("cntct_list_size * n_capacity must be < 2^30");
   h->K = c.max_contacts_per_particle > 0 ? c.max_contacts_per_particle : 24;
@@ -1434,25 +1614,36 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->dev));
   CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   int N = c.n_capacity;
+  // Periodic images need room beside the particles in the search arrays.  A
+  // periodic side longer than two search cells gives every point at most one
+  // image per direction (the bands at both faces are disjoint), so the
+  // points after the y, x and z passes number at most 2^(directions) per particle.
+  h->gcap = (int)(((long long)N << nper) - N);
+  const int NA = N + h->gcap;
+  h->nall = NA;
   int rc = 0;
-  rc |= dalloc(h, &h->gid, N);
-  rc |= dalloc(h, &h->ptype, N);
+  rc |= dalloc(h, &h->gid, NA);
+  rc |= dalloc(h, &h->ptype, NA);
   rc |= dalloc(h, &h->usrmark, N);
-  rc |= dalloc(h, &h->posr, N);
+  rc |= dalloc(h, &h->posr, NA);
   for (int k = 0; k < 3; k++) {
-    if (k < c.tsize) { rc |= dalloc(h, &h->vel[k], N); rc |= dalloc(h, &h->acc[k], N); }
-    if (k < c.rsize) { rc |= dalloc(h, &h->rv[k], N); rc |= dalloc(h, &h->ra[k], N); }
+    if (k < c.tsize) { rc |= dalloc(h, &h->vel[k], k == 0 ? NA : N); rc |= dalloc(h, &h->acc[k], N); }
+    if (k < c.rsize) { rc |= dalloc(h, &h->rv[k], k == 0 ? NA : N); rc |= dalloc(h, &h->ra[k], N); }
+  }
+  if (h->gcap > 0) {
+    rc |= dalloc(h, &h->gflag, (size_t)NA);
+    rc |= dalloc(h, &h->goff, (size_t)NA + 1);
   }
   rc |= dalloc(h, &h->theta, N);
   rc |= dalloc(h, &h->F, N);
   rc |= dalloc(h, &h->T, N);
   rc |= dalloc(h, &h->near_mask, N);
-  rc |= dalloc(h, &h->cell_of, N);
-  rc |= dalloc(h, &h->tmp_rank, N);
-  rc |= dalloc(h, &h->tmp_sorted, N);
-  rc |= dalloc(h, &h->sorted, N);
-  rc |= dalloc(h, &h->sortpos, N);
-  rc |= dalloc(h, &h->spos, N);
+  rc |= dalloc(h, &h->cell_of, NA);
+  rc |= dalloc(h, &h->tmp_rank, NA);
+  rc |= dalloc(h, &h->tmp_sorted, NA);
+  rc |= dalloc(h, &h->sorted, NA);
+  rc |= dalloc(h, &h->sortpos, NA);
+  rc |= dalloc(h, &h->spos, NA);
   rc |= dalloc(h, &h->deg_cnt, kDegBuckets);
   rc |= dalloc(h, &h->deg_start, kDegBuckets);
   rc |= dalloc(h, &h->deg_of, N);
@@ -1465,9 +1656,9 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->w_S, (size_t)N * kKw);
   rc |= dalloc(h, &h->w_M, (size_t)N * kKw);
   rc |= dalloc(h, &h->w_Mr, (size_t)N * kKw);
-  rc |= dalloc(h, &h->row_cnt, N);
-  rc |= dalloc(h, &h->row_off, (size_t)N + 1);
-  rc |= dalloc(h, &h->row_partner, (size_t)N * h->K);
+  rc |= dalloc(h, &h->row_cnt, NA);
+  rc |= dalloc(h, &h->row_off, (size_t)NA + 1);
+  rc |= dalloc(h, &h->row_partner, (size_t)NA * h->K);
   rc |= dalloc(h, &h->in_cnt, N);
   rc |= dalloc(h, &h->in_list, (size_t)N * h->K);
   h->ccap = std::max(1, c.cntct_list_size) * N;
@@ -1480,8 +1671,8 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   for (int b = 0; b < 2; b++) {
     rc |= dalloc(h, &h->c_pgid[b], h->ccap);
     rc |= dalloc(h, &h->c_hist[b], h->ccap);
-    rc |= dalloc(h, &h->sbg[b], G);
-    rc |= dalloc(h, &h->cbg[b], G);
+    rc |= dalloc(h, &h->own_cnt[b], G);
+    rc |= dalloc(h, &h->own_c[b], G * h->K);
     rc |= dalloc(h, &h->wh_cnt[b], G);
     rc |= dalloc(h, &h->wh_wall[b], G * kKw);
     rc |= dalloc(h, &h->wh_hist[b], G * kKw);
@@ -1547,6 +1738,13 @@ int sdem_set_types(sdem_h* h, int nT, const double* radius, const double* mass, 
   h->ny = (int)((yed - h->y0) / h->cell) + 1;
   h->nz = (int)((zed - h->z0) / h->cell) + 1;
   h->ncell = (long long)h->nx * h->ny * h->nz;
+  {
+    double mn = std::min(c.dom_max[0] - c.dom_min[0], std::min(c.dom_max[1] - c.dom_min[1], c.dom_max[2] - c.dom_min[2]));
+    if (1.02 * h->cell > mn) return set_err(h, SDEM_E_ARG, "PC_InitComm: so big Diameter (domain narrower than 1.02 cells)");
+    for (int k = 0; k < 3; k++)
+      if (c.periodic[k] && !(c.dom_max[k] - c.dom_min[k] > 2.0 * h->cell))
+        return set_err(h, SDEM_E_UNSUPPORTED, "a periodic side must be longer than two search cells on the GPU");
+  }
   // Single-precision prefilter of the search: coordinates are stored relative to
   // their cell corner (|value| < 1 cell), so each rounding (coordinate, radius,
   // cell size, differences, squares and sums) is below cell*2^-23; their sum
@@ -1557,7 +1755,7 @@ int sdem_set_types(sdem_h* h, int nT, const double* radius, const double* mass, 
   rc |= dalloc(h, &h->cell_cnt, (size_t)h->ncell);
   rc |= dalloc(h, &h->cell_start, (size_t)h->ncell + 1);
   if (rc) return SDEM_E_NOMEM;
-  long long nb = std::max<long long>((h->ncell + kScanTile - 1) / kScanTile, (h->cfg.n_capacity + kScanTile - 1) / kScanTile);
+  long long nb = std::max<long long>((h->ncell + kScanTile - 1) / kScanTile, ((long long)h->nall + kScanTile - 1) / kScanTile);
   if (nb > 65536) {
     rc |= dalloc(h, &h->scan_tmp, (size_t)nb);
     if (rc) return SDEM_E_NOMEM;
@@ -1650,15 +1848,16 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   // history reset: both buffers empty; near-wall list refreshed at the next step
   size_t G = (size_t)c.max_gid + 1;
   for (int b = 0; b < 2; b++) {
-    CK(cudaMemset(h->cbg[b], 0, sizeof(int) * G));
-    CK(cudaMemset(h->sbg[b], 0, sizeof(int) * G));
+    CK(cudaMemset(h->own_cnt[b], 0, sizeof(int) * G));
     CK(cudaMemset(h->wh_cnt[b], 0, sizeof(int) * G));
   }
+  h->h_up.clear();
   CK(cudaMemset(h->F, 0, sizeof(dbl4) * c.n_capacity));
   CK(cudaMemset(h->T, 0, sizeof(dbl4) * c.n_capacity));
   CK(cudaMemset(h->near_mask, 0, sizeof(unsigned long long) * c.n_capacity));
   int sc[S_SIZE] = {0};
   sc[S_N] = n;
+  sc[S_NT] = n;
   CK(cudaMemcpy(h->scal, sc, sizeof sc, cudaMemcpyHostToDevice));
   CK(cudaMemset(h->ull, 0, sizeof(unsigned long long) * 8));
   h->n_host = n;
@@ -1679,9 +1878,18 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
   int n = h->n_host;
   // The history the next step reads is the "previous" buffer.
   int pv = 1 - h->cur;
-  struct PP { int lo, hi; dbl4 hist; };
-  std::vector<PP> pp;
   std::vector<std::vector<std::pair<int, dbl4>>> wl(n);
+  std::vector<sdem_h::UpRec> pp;
+  std::unordered_map<int, int> idx_of;
+  for (int i = 0; i < n; i++) idx_of[h->h_gid[i]] = i;
+  std::vector<double> posr(4 * (size_t)std::max(n, 1));
+  if (n > 0) {
+    std::vector<dbl4> pb(n);
+    CK(cudaMemcpy(pb.data(), h->posr, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) {
+      posr[4 * i] = pb[i].x; posr[4 * i + 1] = pb[i].y; posr[4 * i + 2] = pb[i].z; posr[4 * i + 3] = pb[i].w;
+    }
+  }
   for (int i = 0; i < nc; i++) {
     int o = owner_idx[i];
     if (o < 0 || o >= n) return set_err(h, SDEM_E_ARG, "sdem_upload_contacts: owner index out of range");
@@ -1695,30 +1903,54 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
       bool dup = false;
       for (auto& e : wl[o]) dup |= (e.first == wi);
       if (!dup) wl[o].push_back({wi, hist});
-    } else {
-      // Only the lower id's record is ever found by Find_insert (its bucket).
-      if (go < pid) pp.push_back({go, pid, hist});
+      continue;
     }
+    // CL_Add_RestartCntctlink (Prtcl_CL_and_CF.f90:577-622): a pair whose
+    // partner is local and lies within 1.5*(r1+r2) is kept once, in the lower
+    // id's bucket; any other record (a partner across a periodic boundary or
+    // absent) stays in the owner's bucket
+    bool both = false;
+    auto it = idx_of.find(pid);
+    if (it != idx_of.end()) {
+      const double* a = &posr[4 * (size_t)o];
+      const double* q = &posr[4 * (size_t)it->second];
+      double dx = a[0] - q[0], dy = a[1] - q[1], dz = a[2] - q[2];
+      double dist = std::sqrt(dx * dx + dy * dy + dz * dz) - 1.5 * (a[3] + q[3]);
+      if (go > pid && dist <= 0.0) continue;
+      both = (go < pid && dist <= 0.0);
+    }
+    pp.push_back({go, pid, both, hist});
   }
-  // rows keyed by the lower id
-  std::stable_sort(pp.begin(), pp.end(), [](const PP& a, const PP& b) { return a.lo < b.lo || (a.lo == b.lo && a.hi < b.hi); });
-  pp.erase(std::unique(pp.begin(), pp.end(), [](const PP& a, const PP& b) { return a.lo == b.lo && a.hi == b.hi; }), pp.end());
+  // Find_insert walks a bucket from its newest record: of two records with
+  // one key the later one is found
+  std::stable_sort(pp.begin(), pp.end(), [](const sdem_h::UpRec& a, const sdem_h::UpRec& b) {
+    return a.owner < b.owner || (a.owner == b.owner && a.partner < b.partner);
+  });
+  {
+    std::vector<sdem_h::UpRec> u;
+    for (size_t i = 0; i < pp.size(); i++)
+      if (i + 1 == pp.size() || pp[i + 1].owner != pp[i].owner || pp[i + 1].partner != pp[i].partner) u.push_back(pp[i]);
+    pp.swap(u);
+  }
   if ((long long)pp.size() > h->ccap) return set_err(h, SDEM_E_CL_FULL, "sdem_upload_contacts: more records than contact capacity");
   size_t G = (size_t)c.max_gid + 1;
-  std::vector<int> sbg(G, 0), cbg(G, 0), pg(pp.size());
+  std::vector<int> ocnt(G, 0), oc(G * h->K, 0), pg(pp.size());
   std::vector<dbl4> hs(pp.size());
   for (size_t i = 0; i < pp.size(); i++) {
-    if (i == 0 || pp[i].lo != pp[i - 1].lo) sbg[pp[i].lo] = (int)i;
-    cbg[pp[i].lo]++;
-    pg[i] = pp[i].hi;
+    int g = pp[i].owner;
+    if (ocnt[g] >= h->K)
+      return set_err(h, SDEM_E_CL_FULL, "sdem_upload_contacts: more records on one particle than max_contacts_per_particle");
+    oc[(size_t)g * h->K + ocnt[g]++] = (int)i;
+    pg[i] = pp[i].partner;
     hs[i] = pp[i].hist;
   }
-  CK(cudaMemcpy(h->sbg[pv], sbg.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->cbg[pv], cbg.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->own_cnt[pv], ocnt.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->own_c[pv], oc.data(), sizeof(int) * G * h->K, cudaMemcpyHostToDevice));
   if (!pp.empty()) {
     CK(cudaMemcpy(h->c_pgid[pv], pg.data(), sizeof(int) * pp.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->c_hist[pv], hs.data(), sizeof(dbl4) * pp.size(), cudaMemcpyHostToDevice));
   }
+  h->h_up = pp;
   std::vector<int> whc(G, 0), whw(G * kKw, 0);
   std::vector<dbl4> whh(G * kKw);
   for (int o = 0; o < n; o++) {
@@ -1889,7 +2121,7 @@ int gather_contacts(sdem_h* h, std::vector<CRec>& out) {
   size_t G = (size_t)c.max_gid + 1;
   if (h->stepped) {
     int C = 0;
-    CK(cudaMemcpy(&C, h->row_off + h->n_host, sizeof C, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&C, h->row_off + h->n_host + h->gcap, sizeof C, cudaMemcpyDeviceToHost));
     std::vector<int> og(std::max(C, 1)), pg(std::max(C, 1));
     std::vector<dbl4> hs(std::max(C, 1));
     if (C > 0) {
@@ -1897,35 +2129,26 @@ int gather_contacts(sdem_h* h, std::vector<CRec>& out) {
       CK(cudaMemcpy(pg.data(), h->c_pgid[lw], sizeof(int) * C, cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(hs.data(), h->c_hist[lw], sizeof(dbl4) * C, cudaMemcpyDeviceToHost));
     }
+    // a local pair is listed under both particles (bucket + Head_Cp), a pair
+    // with a periodic image under its local particle only
     for (int i = 0; i < C; i++) {
-      int a = idx_of[og[i]], b = idx_of[pg[i]];
+      const bool img = (og[i] & kImgFlag) != 0;
+      const int o = og[i] & ~kImgFlag;
+      int a = idx_of[o], b = img ? -1 : idx_of[pg[i]];
       CRec r;
       r.t[0] = hs[i].x; r.t[1] = hs[i].y; r.t[2] = hs[i].z; r.vr = hs[i].w;
       if (a >= 0) { r.owner = a; r.partner = pg[i]; out.push_back(r); }
-      if (b >= 0) { r.owner = b; r.partner = og[i]; out.push_back(r); }
+      if (b >= 0) { r.owner = b; r.partner = o; out.push_back(r); }
     }
   } else {
     // not stepped since upload: report the uploaded history
-    std::vector<int> sbg(G), cbg(G);
-    CK(cudaMemcpy(sbg.data(), h->sbg[lw], sizeof(int) * G, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(cbg.data(), h->cbg[lw], sizeof(int) * G, cudaMemcpyDeviceToHost));
-    long long tot = 0;
-    for (size_t g = 0; g < G; g++) tot += cbg[g];
-    std::vector<int> pg(std::max<long long>(tot, 1));
-    std::vector<dbl4> hs(std::max<long long>(tot, 1));
-    if (tot > 0) {
-      CK(cudaMemcpy(pg.data(), h->c_pgid[lw], sizeof(int) * tot, cudaMemcpyDeviceToHost));
-      CK(cudaMemcpy(hs.data(), h->c_hist[lw], sizeof(dbl4) * tot, cudaMemcpyDeviceToHost));
+    for (const auto& u : h->h_up) {
+      int a = idx_of[u.owner], b = u.both ? idx_of[u.partner] : -1;
+      CRec r;
+      r.t[0] = u.hist.x; r.t[1] = u.hist.y; r.t[2] = u.hist.z; r.vr = u.hist.w;
+      if (a >= 0) { r.owner = a; r.partner = u.partner; out.push_back(r); }
+      if (b >= 0) { r.owner = b; r.partner = u.owner; out.push_back(r); }
     }
-    for (size_t g = 0; g < G; g++)
-      for (int j = 0; j < cbg[g]; j++) {
-        int e = sbg[g] + j;
-        int a = idx_of[g], b = idx_of[pg[e]];
-        CRec r;
-        r.t[0] = hs[e].x; r.t[1] = hs[e].y; r.t[2] = hs[e].z; r.vr = hs[e].w;
-        if (a >= 0) { r.owner = a; r.partner = pg[e]; out.push_back(r); }
-        if (b >= 0) { r.owner = b; r.partner = (int)g; out.push_back(r); }
-      }
   }
   std::vector<int> whc(G), whw(G * kKw);
   std::vector<dbl4> whh(G * kKw);
@@ -2101,6 +2324,7 @@ int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, c
   d.ncap = kNaMaxN;
   d.n_launch = n;
   d.n = &S->n;
+  d.nt = &S->n;   // no periodic images here
   d.status = S->status;
   d.cell = cell;
   d.rcell = 1.0 / cell;

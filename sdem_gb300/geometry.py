@@ -67,23 +67,24 @@ def plane_wall(p1, p2, p3, p4, wall_id: int, wall_type: int = 1, both: bool = Fa
 
 
 def box_walls(dmin: Sequence[float], dmax: Sequence[float], infinite: bool = True, top: bool = False,
-              wall_type: int = 1, base_wall_id: int = 10000000) -> WallSet:
+              wall_type: int = 1, base_wall_id: int = 10000000, skip_axes: Sequence[int] = ()) -> WallSet:
     """Floor (y = min) and four side walls (x and z), normals pointing into the
-    box, as &GeometryMakingParam planes.  top=True adds a lid."""
+    box, as &GeometryMakingParam planes.  top=True adds a lid.  Faces normal to
+    an axis in skip_axes (a periodic direction) are left out."""
     x0, y0, z0 = dmin
     x1, y1, z1 = dmax
     ws = WallSet()
     kw = dict(wall_type=wall_type, infinite=infinite, base_wall_id=base_wall_id)
-    # floor: normal +y  ((p2-p1) x (p3-p1) points along +y)
-    ws.add((x0, y0, z0), (x0, y0, z1), (x1, y0, z1), (x1, y0, z0), **kw)
-    # x = x0, normal +x
-    ws.add((x0, y0, z0), (x0, y1, z0), (x0, y1, z1), (x0, y0, z1), **kw)
-    # x = x1, normal -x
-    ws.add((x1, y0, z0), (x1, y0, z1), (x1, y1, z1), (x1, y1, z0), **kw)
-    # z = z0, normal +z
-    ws.add((x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0), **kw)
-    # z = z1, normal -z
-    ws.add((x0, y0, z1), (x0, y1, z1), (x1, y1, z1), (x1, y0, z1), **kw)
+    faces = [
+        (1, ((x0, y0, z0), (x0, y0, z1), (x1, y0, z1), (x1, y0, z0))),   # floor: normal +y
+        (0, ((x0, y0, z0), (x0, y1, z0), (x0, y1, z1), (x0, y0, z1))),   # x = x0, normal +x
+        (0, ((x1, y0, z0), (x1, y0, z1), (x1, y1, z1), (x1, y1, z0))),   # x = x1, normal -x
+        (2, ((x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0))),   # z = z0, normal +z
+        (2, ((x0, y0, z1), (x0, y1, z1), (x1, y1, z1), (x1, y0, z1))),   # z = z1, normal -z
+    ]
     if top:
-        ws.add((x0, y1, z0), (x1, y1, z0), (x1, y1, z1), (x0, y1, z1), **kw)
+        faces.append((1, ((x0, y1, z0), (x1, y1, z0), (x1, y1, z1), (x0, y1, z1))))
+    for axis, pts in faces:
+        if axis not in skip_axes:
+            ws.add(*pts, **kw)
     return ws

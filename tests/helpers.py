@@ -5,14 +5,16 @@ import numpy as np
 
 
 def keyed_contacts(system, base_wall_id: int):
-    """{(id_lo, id_hi) or (id, wall_id): (tx, ty, tz, velrel)} of the live contact list."""
+    """{(listing id, partner id or wall id): (tx, ty, tz, velrel)} of the live
+    contact list.  A local pair appears under both ids, a pair with a periodic
+    image under its local sphere only, so the keys tell the two apart."""
     ids = system.state().id
     o, q, t, v = system.contacts()
     out = {}
     for k in range(len(o)):
-        g = int(ids[o[k]])
-        p = int(q[k])
-        key = (g, p) if p > base_wall_id else (min(g, p), max(g, p))
+        key = (int(ids[o[k]]), int(q[k]))
+        if key in out:
+            raise AssertionError(f"contact {key} listed twice")
         out[key] = (t[k, 0], t[k, 1], t[k, 2], v[k])
     return out
 

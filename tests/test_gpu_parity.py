@@ -33,6 +33,11 @@ CASES = {
     "lsd_fe": lambda: cloud(seed=15, cf_type=props.CFT_LSD, pi=1, pri=1),
     "hertz_ct2_noquirk": lambda: beds.scaled(cloud(seed=16), ct_model=2, quirk_ab2_rot=0),
     "mono_one_type": lambda: cloud(seed=17, ntypes=1, nn=0.995e-3),
+    # periodic images (PC_Comm_For_Cntct, FineSearch3, ContactForce_PPG)
+    "periodic_xyz": lambda: beds.periodic_lattice_case(800, 31, (1, 1, 1)),
+    "periodic_y": lambda: beds.periodic_lattice_case(800, 32, (0, 1, 0)),
+    "periodic_xz": lambda: beds.periodic_lattice_case(800, 33, (1, 0, 1)),
+    "periodic_x_lsd": lambda: beds.periodic_lattice_case(800, 34, (1, 0, 0), cf_type=props.CFT_LSD, ntypes=3),
 }
 
 
@@ -70,7 +75,7 @@ def test_one_step_from_identical_inputs(gpu_lib, name):
     compare_step(g, o, case, name)
 
 
-@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "hertz_finite_walls"])
+@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "hertz_finite_walls", "periodic_xyz", "periodic_xz"])
 def test_twenty_steps_resynchronised(gpu_lib, name):
     """A chain of single steps, each from the oracle's state and contact list
     (restart-file style), so chaos cannot hide or create a mismatch."""
@@ -86,7 +91,7 @@ def test_twenty_steps_resynchronised(gpu_lib, name):
         g.close()
 
 
-@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2"])
+@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "periodic_xyz"])
 def test_free_run_trajectory(gpu_lib, name):
     """50 free-running steps: contact sets stay identical and the state within
     a loose bound (differences start at ~1 ulp per step)."""
@@ -178,7 +183,56 @@ def test_row_capacity_error(gpu_lib):
 
 
 def test_unsupported_options_are_refused(gpu_lib):
-    case = beds.scaled(cloud(seed=24, n=20), periodic=(1, 0, 0))
+    case = beds.scaled(cloud(seed=24, n=20), cs_method=2)
+    with pytest.raises(SdemError) as e:
+        DEMSystem(case)
+    assert e.value.code == 10
+
+
+def test_periodic_wrap_matches_oracle(gpu_lib):
+    """Fast spheres cross the periodic faces: the GPU wraps them in place
+    (Comm_For_Exchange) with the same ids, positions and image contacts."""
+    case = beds.periodic_lattice_case(800, 35, (1, 1, 1), vmax=25.0)
+    g, o = DEMSystem(case), OracleSystem(case)
+    for k in range(40):
+        g.step(1)
+        o.step(1)
+        kg = keyed_contacts(g, case.opts.base_wall_id)
+        ko = keyed_contacts(o, case.opts.base_wall_id)
+        assert_same_contact_sets(kg, ko, f"wrap step {k}")
+        assert g.counters() == o.counters()
+    sg, so = g.state(), o.state()
+    np.testing.assert_array_equal(sg.id, so.id)
+    lo, hi = np.array(case.opts.minpoint), np.array(case.opts.maxpoint)
+    assert np.all(sg.posR[:, :3] >= lo) and np.all(sg.posR[:, :3] < hi)
+    moved = np.abs(sg.posR[:, :3] - case.particles.posR[:, :3]).max()
+    assert moved > 0.5 * (hi - lo).min(), "some sphere should have wrapped"
+    np.testing.assert_allclose(sg.posR, so.posR, rtol=1e-11, atol=1e-15)
+
+
+def test_periodic_history_roundtrip(gpu_lib):
+    """Image contacts are listed under their local sphere only and come back
+    through sdem_upload_contacts with their spring history."""
+    case = beds.periodic_lattice_case(800, 36, (1, 0, 1))
+    o = OracleSystem(case)
+    o.step(2)
+    c = beds.Case(case.name, case.opts, case.tables, case.walls, o.state(), contacts=o.contacts())
+    g = DEMSystem(c)
+    kg0 = keyed_contacts(g, case.opts.base_wall_id)
+    ko0 = keyed_contacts(o, case.opts.base_wall_id)
+    assert_same_contact_sets(kg0, ko0, "after upload")
+    compare_history(kg0, ko0, 0.0)
+    g.step(1)
+    o.step(1)
+    assert g.counters()["ppg"] > 0
+    compare_step(g, o, case, "periodic restart chain")
+
+
+def test_periodic_side_of_two_cells_is_refused(gpu_lib):
+    case = beds.periodic_lattice_case(100, 37, (1, 0, 0))
+    hi = list(case.opts.maxpoint)
+    hi[0] = 2.4e-3   # about two search cells
+    case = beds.scaled(case, maxpoint=tuple(hi))
     with pytest.raises(SdemError) as e:
         DEMSystem(case)
     assert e.value.code == 10
