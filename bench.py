@@ -38,7 +38,12 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s, 1M Hertz spheres"
 UNIT = "particle-steps/s"
 WORKLOAD = "hertz_poly_1m"
-MEASURED_FP64_TFLOPS = 1.198   # DFMA-chain probe on this machine's GB300 (2 flops per DFMA)
+MEASURED_FP64_TFLOPS = 1.198   # DFMA-chain probe on GB300 (2 flops per DFMA)
+# From the ncu capture in profiles/k_force_search_gather_hertz_poly_500k.txt:
+FORCE_DRAM_BYTES_PER_CONTACT = 481.0     # dram__bytes_read.sum + dram__bytes_write.sum per contact
+FORCE_FP64_INST_PER_CONTACT = 217.8      # DADD + DMUL + DFMA thread instructions per contact
+FP64_INST_PER_SM_CLK = 2.0               # sm__sass_thread_inst_executed_op_dfma_pred_on peak per SM
+NUM_SMS = 152
 
 
 def make_case(n: int, seed: int):
@@ -246,12 +251,10 @@ def our_arm(args):
     except Exception:
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = None
-    try:
-        tj = json.load(open(os.path.join(ROOT, "profiles", "force_traffic.json")))
-        traffic = tj["dram_bytes_per_contact"] * C
-    except Exception:
-        pass
+    # DRAM bytes of k_force per contact from one ncu capture of the same kernel
+    # on the 500k-sphere bed (profiles/k_force_search_gather_hertz_poly_500k.txt),
+    # scaled to this launch by its contacts
+    traffic = FORCE_DRAM_BYTES_PER_CONTACT * C
     # algorithmic FP64 operations of one Hertz contact (force law + normal vector):
     # 127 add/sub/mul, 8 sqrt, 7 divisions, each sqrt/div counted as one operation
     fp64_per_contact = 142
@@ -292,6 +295,8 @@ def our_arm(args):
                "sample": "CPU restatement of the reference (oracle/sdem_oracle.c): " + sample}
 
     if rank == 0:
+        clocks = clk.summary()
+        clk_mhz = float(clocks.get("sm_mhz") or 2070.0)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
             "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -310,14 +315,20 @@ def our_arm(args):
                          "note": "k_force is FP64-ALU bound on GB300, see fp64 below"},
             "fp64": {"kernel": "k_force", "achieved_tflops": fp64_per_contact * C / t_force / 1e12,
                      "peak_tflops": MEASURED_FP64_TFLOPS, "frac": fp64_per_contact * C / t_force / 1e12 /
-                     MEASURED_FP64_TFLOPS},
+                     MEASURED_FP64_TFLOPS,
+                     "algorithmic_ops_per_contact": fp64_per_contact,
+                     "executed_inst_per_contact": FORCE_FP64_INST_PER_CONTACT,
+                     "pipe_frac": FORCE_FP64_INST_PER_CONTACT * C / t_force /
+                     (FP64_INST_PER_SM_CLK * NUM_SMS * clk_mhz * 1e6),
+                     "note": "pipe_frac: executed DADD/DMUL/DFMA per second over the pipe's peak "
+                             "(2 per SM per clock) at the sampled SM clock"},
             "step_roofline": {"achieved": step_bytes / t_step / 1e9, "peak": hbm, "unit": "GB/s",
                               "frac": step_bytes / t_step / 1e9 / hbm,
                               "algorithmic_bytes": "352 B per particle + 80 B per contact per step"},
             "phases_ms_per_step": {k: v / nprof for k, v in phases.items()},
             "dominant_phase": dom,
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
     sysm.close()

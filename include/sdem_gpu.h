@@ -88,7 +88,7 @@ extern "C" {
 
 /* counters returned by sdem_counters() */
 #define SDEM_CNT_PP        0  /* numCntcts(1): exact particle-particle contacts          */
-#define SDEM_CNT_PPG       1  /* numCntcts(2): particle-ghost (0 on one GPU, no periodic) */
+#define SDEM_CNT_PPG       1  /* numCntcts(2): particle-image pairs (periodic directions) */
 #define SDEM_CNT_PPFIX     2  /* numCntcts(3): particle-fixed particle                    */
 #define SDEM_CNT_PW        3  /* numCntcts(4): particle-wall                              */
 #define SDEM_CNT_CNSV      4  /* num_Cnsv_cntct: conservative candidate pairs             */
@@ -110,7 +110,7 @@ typedef struct sdem_cfg {
   int    cntct_list_size;       /* CntctList_Size (contact records = size * mlocal)  */
   int    base_wall_id;          /* Base_wall_id                                      */
   int    wall_max_update_iter;  /* Wall_max_update_iter                              */
-  int    periodic[3];           /* IsPeriodic                                        */
+  int    periodic[3];           /* IsPeriodic; each periodic side > 2 search cells   */
   int    quirk_ab2_rot;         /* 1: AB2 rotation starts from linVel (Prtcl_Integration.f90:64) */
   int    max_contacts_per_particle; /* GPU row capacity per particle, 0 = default (24), <= 64 */
   double dt;                    /* dtDEM                                             */
