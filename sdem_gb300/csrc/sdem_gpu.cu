@@ -5,24 +5,31 @@
 // One step (the body of DEMS_iterate, Prtcl_DEMSystem.f90:214-247) is:
 //   k_wall_refresh/k_wall_refresh_end  UpdateNearPrtclsPW (Prtcl_ContactSearchPW.f90:159-235),
 //                                      device-predicated on iter >= Next_iter_update
+//   k_ghost_*                          PC_Comm_For_Cntct on one rank (periodic directions only):
+//                                      images of the particles near periodic faces, in the
+//                                      reference's pass order, as ordered stream compactions
 //   k_bin, scan, k_scatter, k_cellorder
 //                                      NBSM_clcBoxIndex + Y/X/Z lists (Prtcl_NBS_Munjiza.f90:163-296)
 //                                      as a counting sort; within a cell particles are ordered by
 //                                      decreasing index, the order the reference's Z lists walk
-//   k_search                           LoopNBSMask + FineSearch2 (:302-473, :503-530): one thread per
+//   k_search                           LoopNBSMask + FineSearch2/3 (:302-473, :503-557): one thread per
 //                                      target particle, same 13-cell half shell + same-cell tail, same
 //                                      exact FP64 overlap test; contacts go to the target's row (in visit
 //                                      order) and an entry (target, slot) to the partner's in-list
-//   scan, k_gid_index                  row offsets (CSR) and per-id row tables for the next step's
-//                                      history lookup
-//   k_force                            Find_insert history lookup + ContactForce_PP
-//                                      (Prtcl_CL_and_CF.f90:142-168, 256-296, 732-756): one thread per
+//   k_wall_detect                      FindContactsPW's detection (:298-319) over the near-wall mask,
+//                                      and the contact count of every particle for the gather order
+//   scan, k_gid_index                  row offsets (CSR), each contact's row, an empty owner table
+//   k_force                            Find_insert history lookup + ContactForce_PP / _PPG
+//                                      (Prtcl_CL_and_CF.f90:142-198, 256-296, 732-798): one thread per
 //                                      contact, full warps of FP64 work
-//   k_gather_integrate                 per particle, sums its contact records in the reference's scatter
-//                                      order (a deterministic gather), then wall contacts
-//                                      (FindContactsPW, :298-319) in near-list order, clc_Acceleration
-//                                      (Prtcl_DEMSystem.f90:166-181) and Prtcl_Integrate
-//                                      (Prtcl_Integration.f90:15-88)
+//   k_wall_force                       ContactForce_PW (:832-856), one thread per wall contact
+//   k_degree_scan, k_degree_scatter    particles grouped by contact count (the gather order)
+//   k_gather                           per particle, sums its contact records in the reference's scatter
+//                                      order (a deterministic gather), then its wall contacts in
+//                                      near-list order
+//   k_integrate                        clc_Acceleration (Prtcl_DEMSystem.f90:166-181), Prtcl_Integrate
+//                                      (Prtcl_Integration.f90:15-88) and the periodic wrap, in index
+//                                      order
 //   k_delete, k_apply_moves            one-rank out-of-domain delete (Prtcl_Comm.f90:1569-1840)
 //   k_step_end                         iterNumber += 1, counters
 // RemvReleased/PreIteration have no kernel: the history of step n+1 is exactly
@@ -121,6 +128,7 @@ struct Dev {
   // the lower id for particle-particle pairs, the local particle for a pair
   // with a periodic image; own_c lists this step's contacts of each owner id
   int Ko;
+  int* c_row;   // row (target sort position) of each contact
   int *own_cnt, *own_c;
   const int *own_cnt_prev, *own_c_prev;
   int *wh_cnt, *wh_wall;
@@ -496,26 +504,45 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d) {
         }
         cnt++;
       };
-      // same cell, particles after the target in list order
-      {
-        int b = d.cell_start[key + 1];
-        for (int t = s + 1; t < b; t++) test(t, 0.f, 0.f, 0.f);
-        if (!m_img) cand += (unsigned long long)(b - s - 1);
+      // Cell boundaries of the whole half shell are loaded up front (they do
+      // not depend on one another), then the candidates are walked in the
+      // reference's order.  The three cells iz-1..iz+1 of one (ix, iy) column
+      // are consecutive in the sort, so a column is one range with two inner
+      // boundaries; cells outside the grid are empty ranges.
+      const int nx = d.nx, nz = d.nz;
+      const int* __restrict__ cs = d.cell_start;
+      const int tail_end = cs[key + 1];
+      const int own_lo = iz > 0 ? cs[key - 1] : 0, own_hi = iz > 0 ? cs[key] : 0;   // cell (ix, iy, iz-1)
+      int cb[4][4];
+      const int ccx[4] = {ix - 1, ix - 1, ix, ix + 1}, ccy[4] = {iy, iy - 1, iy - 1, iy - 1};
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int cx = ccx[c], cy = ccy[c];
+        if (cx < 0 || cx >= nx || cy < 0) {
+          cb[c][0] = cb[c][1] = cb[c][2] = cb[c][3] = 0;
+        } else {
+          const long long kb = ((long long)cy * nx + cx) * nz + iz;
+          cb[c][1] = cs[kb];
+          cb[c][2] = cs[kb + 1];
+          cb[c][0] = iz > 0 ? cs[kb - 1] : cb[c][1];
+          cb[c][3] = iz + 1 < nz ? cs[kb + 2] : cb[c][2];
+        }
       }
-      auto visit = [&](int cx, int cy, int cz) {
-        if (cx < 0 || cx >= d.nx || cy < 0 || cz < 0 || cz >= d.nz) return;
-        long long k2 = ((long long)cy * d.nx + cx) * d.nz + cz;
-        int a = d.cell_start[k2], b = d.cell_start[k2 + 1];
-        const float ox = (float)(ix - cx) * d.cellf, oy = (float)(iy - cy) * d.cellf, oz = (float)(iz - cz) * d.cellf;
-        for (int t = a; t < b; t++) test(t, ox, oy, oz);
-        if (!m_img) cand += (unsigned long long)(b - a);
-      };
-      visit(ix, iy, iz - 1);
-      visit(ix - 1, iy, iz - 1);
-      visit(ix - 1, iy, iz);
-      visit(ix - 1, iy, iz + 1);
-      for (int lx = -1; lx <= 1; lx++)
-        for (int i = -1; i <= 1; i++) visit(ix + lx, iy - 1, iz + i);
+      // same cell, particles after the target in list order
+      for (int t = s + 1; t < tail_end; t++) test(t, 0.f, 0.f, 0.f);
+      // (ix, iy, iz-1)
+      for (int t = own_lo; t < own_hi; t++) test(t, 0.f, 0.f, d.cellf);
+      if (!m_img) cand += (unsigned long long)((tail_end - s - 1) + (own_hi - own_lo));
+      // columns (ix-1, iy), then (ix-1..ix+1, iy-1), cells iz-1, iz, iz+1
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const float ox = (float)(ix - ccx[c]) * d.cellf, oy = (float)(iy - ccy[c]) * d.cellf;
+        int t = cb[c][0];
+        for (; t < cb[c][1]; t++) test(t, ox, oy, d.cellf);
+        for (; t < cb[c][2]; t++) test(t, ox, oy, 0.f);
+        for (; t < cb[c][3]; t++) test(t, ox, oy, -d.cellf);
+        if (!m_img) cand += (unsigned long long)(cb[c][3] - cb[c][0]);
+      }
       d.row_cnt[s] = cnt < K ? cnt : K;
 
     }
@@ -622,27 +649,23 @@ __global__ void __launch_bounds__(kThreads) k_wall_force(Dev d) {
   }
 }
 
-// Empties this step's owner table for every local id (images never own).
+// Empties this step's owner table for every local id (images never own), and
+// writes each contact's row (its target's sort position), so that the
+// one-thread-per-contact force kernel reads its row instead of searching the
+// row offsets.
 __global__ void k_gid_index(Dev d) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= *d.n) return;
-  d.own_cnt[d.gid[p]] = 0;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < *d.n) d.own_cnt[d.gid[p]] = 0;
+  if (p < *d.nt) {
+    const int a = d.row_off[p], k = d.row_cnt[p];
+    for (int j = 0; j < k; j++)
+      if (a + j < d.ccap) d.c_row[a + j] = p;
+  }
 }
 
 // ---------------------------------------------------------------------------
 // One thread per contact: Find_insert's history lookup + ContactForce_PP.
-__device__ __forceinline__ int find_row(const int* __restrict__ off, int n, int c) {
-  int lo = 0, hi = n;  // off[lo] <= c < off[hi]
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (off[mid] <= c) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
-__global__ void __launch_bounds__(kThreads) k_force(Dev d) {
-  const int nt = *d.nt;
+__global__ void __launch_bounds__(kThreads, 3) k_force(Dev d) {
   const int nloc = *d.n;
   const int C = d.row_off[d.nall_launch];
   if (C > d.ccap) {
@@ -651,8 +674,8 @@ __global__ void __launch_bounds__(kThreads) k_force(Dev d) {
   }
   unsigned long long nimg = 0;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
-    int s = find_row(d.row_off, nt, c);
-    int slot = c - d.row_off[s];
+    const int s = d.c_row[c];
+    const int slot = c - d.row_off[s];
     int m = d.sorted[s];
     int q = d.row_partner[(size_t)slot * d.nall + s];
     int gm = d.gid[m], gq = d.gid[q];
@@ -667,6 +690,14 @@ __global__ void __launch_bounds__(kThreads) k_force(Dev d) {
     // Find_insert's bucket: the lower id's for PP, the local particle's for PPG
     const int owner = img ? d.gid[loc] : (m_lo ? gm : gq);
     const int partner = img ? d.gid[oth] : (m_lo ? gq : gm);
+    // particle state first: these loads do not depend on the history lookup
+    // below, so their latency overlaps its chain of dependent loads
+    const dbl4 Pi = d.posr[pid], Pj = d.posr[pjd];
+    const dbl4 Vi = d.vel0[pid], Vj = d.vel0[pjd], Wi = d.rv0[pid], Wj = d.rv0[pjd];
+    // Prtcl_BnryProp(pType(lower id), pType(higher id)) for PP (:743),
+    // (pType(local), pType(image)) for PPG (:772)
+    const int ta = img ? d.ptype[loc] : d.ptype[pid];
+    const int tb = img ? d.ptype[oth] : d.ptype[pjd];
     dbl4 hist = make_dbl4(0.0, 0.0, 0.0, -2.0);
     {
       const int k = d.own_cnt_prev[owner];
@@ -675,12 +706,7 @@ __global__ void __launch_bounds__(kThreads) k_force(Dev d) {
         if (d.c_pgid_prev[e] == partner) { hist = d.c_hist_prev[e]; break; }
       }
     }
-    // Prtcl_BnryProp(pType(lower id), pType(higher id)) for PP (:743),
-    // (pType(local), pType(image)) for PPG (:772)
-    const int ta = img ? d.ptype[loc] : d.ptype[pid];
-    const int tb = img ? d.ptype[oth] : d.ptype[pjd];
     const double* P = d.bpp + ((size_t)(tb - 1) * d.nT + (ta - 1)) * SDEM_BP_SIZE;
-    dbl4 Pi = d.posr[pid], Pj = d.posr[pjd];
     // Norm_v = Posj .nv. Posi (real4_nv, Prtcl_TypeDef.f90:268-281) and
     // ovrlp = dr - sqrt(d2sum) (NBSM_FineSearch2/3, Prtcl_NBS_Munjiza.f90:514-522)
     // share one length: d2sum = dz*dz + (dy*dy + dx*dx) is bitwise
@@ -691,8 +717,8 @@ __global__ void __launch_bounds__(kThreads) k_force(Dev d) {
     const double ovrlp = (Pi.w + Pj.w) - normv;
     r3 Norm_v = (normv > 1.0000E-10) ? sdem::div3_rcp(sv, normv) : sdem::mk3(0.0, 0.0, 0.0);
     r3 S, M, Mr;
-    sdem::force_law(d.law, P, sdem::xyz(d.vel0[pid]), sdem::xyz(d.vel0[pjd]), sdem::xyz(d.rv0[pid]),
-                    sdem::xyz(d.rv0[pjd]), Pi.w, Pj.w, Norm_v, ovrlp, hist, S, M, Mr);
+    sdem::force_law(d.law, P, sdem::xyz(Vi), sdem::xyz(Vj), sdem::xyz(Wi), sdem::xyz(Wj), Pi.w, Pj.w, Norm_v, ovrlp,
+                    hist, S, M, Mr);
     d.c_ogid[c] = owner | (img ? kImgFlag : 0);
     d.c_pgid[c] = partner;
     d.c_hist[c] = hist;
@@ -737,13 +763,13 @@ __device__ __forceinline__ void sort_net(unsigned (&v)[N]) {
       }
 }
 
-__global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
+template <bool kByDegree>
+__global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= *d.n) return;
-  const int p = d.gorder[tid];
+  const int p = kByDegree ? d.gorder[tid] : tid;
   const int ncap = d.ncap;
   const int s = d.sortpos[p];
-  const dbl4 Pp = d.posr[p];
   r3 F = sdem::mk3(0.0, 0.0, 0.0), T = sdem::mk3(0.0, 0.0, 0.0);
 
   // The contact records of p in the reference's scatter order: in-list
@@ -832,6 +858,15 @@ __global__ void __launch_bounds__(kThreads) k_gather_integrate(Dev d) {
   }
   d.F[p] = sdem::d4(F, 0.0);
   d.T[p] = sdem::d4(T, 0.0);
+}
+
+// Per particle in index order (coalesced state): clc_Acceleration,
+// Prtcl_Integrate and the periodic wrap / out-of-domain flag.
+__global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *d.n) return;
+  const dbl4 Pp = d.posr[p];
+  const r3 F = sdem::xyz(d.F[p]), T = sdem::xyz(d.T[p]);
   const dbl4 v1 = d.vel0[p];
   const dbl4 w1 = d.rv0[p];
   const int ti = d.ptype[p];
@@ -1225,7 +1260,7 @@ struct sdem_h {
   int *row_cnt = nullptr, *row_partner = nullptr, *row_off = nullptr, *in_cnt = nullptr;
   unsigned* in_list = nullptr;
   int ccap = 0;
-  int *c_ogid = nullptr, *c_pgid[2] = {}, *own_cnt[2] = {}, *own_c[2] = {};
+  int *c_ogid = nullptr, *c_pgid[2] = {}, *own_cnt[2] = {}, *own_c[2] = {}, *c_row = nullptr;
   int nall = 0, gcap = 0;
   int *gflag = nullptr, *goff = nullptr;
   // particle-particle records as uploaded (reported until the first step):
@@ -1412,6 +1447,7 @@ Dev make_dev(sdem_h* h) {
   d.c_Mj = h->c_Mj;
   d.c_Mr = h->c_Mr;
   d.Ko = h->K;
+  d.c_row = h->c_row;
   d.own_cnt = h->own_cnt[cu];
   d.own_c = h->own_c[cu];
   d.own_cnt_prev = h->own_cnt[pv];
@@ -1491,7 +1527,7 @@ int enqueue_step(sdem_h* h) {
   mark(PH_SCAN_ROWS);
   scan(h, h->row_cnt, na, h->row_off);
   mark(PH_GID_INDEX);
-  k_gid_index<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_gid_index<<<grid_for(na), kThreads, 0, st>>>(d);
   mark(PH_FORCE);
   k_force<<<h->num_sms * 8, kThreads, 0, st>>>(d);
   mark(PH_WALL_FORCE);
@@ -1499,14 +1535,15 @@ int enqueue_step(sdem_h* h) {
   mark(PH_GATHER);
   k_degree_scan<<<1, 32, 0, st>>>(d);
   k_degree_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
-  k_gather_integrate<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_gather<true><<<grid_for(n), kThreads, 0, st>>>(d);
+  k_integrate<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_DELETE);
   k_delete<<<1, 1, 0, st>>>(d);
   k_apply_moves<<<16, kThreads, 0, st>>>(d);
   mark(PH_END);
   k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS);
   mark(kPhases);
-  L += 1 + 3 + 1 + 1 + 2 + 3 + 1 + 1 + 1 + 3 + 2 + 1;
+  L += 1 + 3 + 1 + 1 + 2 + 3 + 1 + 1 + 1 + 4 + 2 + 1;
   h->launches += L;
   if (ev) h->prof_steps++;
   h->cur = 1 - h->cur;
@@ -1663,6 +1700,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->in_list, (size_t)N * h->K);
   h->ccap = std::max(1, c.cntct_list_size) * N;
   rc |= dalloc(h, &h->c_ogid, h->ccap);
+  rc |= dalloc(h, &h->c_row, h->ccap);
   rc |= dalloc(h, &h->c_S, h->ccap);
   rc |= dalloc(h, &h->c_M, h->ccap);
   rc |= dalloc(h, &h->c_Mj, h->ccap);
