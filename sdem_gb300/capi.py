@@ -207,18 +207,32 @@ class DEMSystem:
         self._check(self.lib.sdem_get_stream(self.h, C.byref(s)))
         return s.value or 0
 
-    def state(self) -> Particles:
+    def state(self, out: Optional[Particles] = None) -> Particles:
+        """The particle state.  With `out` (arrays of at least n_capacity rows,
+        C-contiguous, e.g. in pinned host memory) the download lands there and
+        views of its first n rows are returned."""
         cap = self.cfg.n_capacity
         ts, rs = self.cfg.tsize, self.cfg.rsize
         n = C.c_int()
-        out = Particles(np.zeros(cap, np.int32), np.zeros(cap, np.int32), np.zeros(cap, np.int32),
-                        np.zeros((cap, 4)), np.zeros((cap, ts, 3)), np.zeros((cap, ts, 3)), np.zeros((cap, 3)),
-                        np.zeros((cap, rs, 3)), np.zeros((cap, rs, 3)))
+        fresh = out is None
+        if fresh:
+            out = Particles(np.zeros(cap, np.int32), np.zeros(cap, np.int32), np.zeros(cap, np.int32),
+                            np.zeros((cap, 4)), np.zeros((cap, ts, 3)), np.zeros((cap, ts, 3)), np.zeros((cap, 3)),
+                            np.zeros((cap, rs, 3)), np.zeros((cap, rs, 3)))
+        else:
+            for a, shape, dt in ((out.id, (cap,), np.int32), (out.posR, (cap, 4), np.float64),
+                                 (out.linVel, (cap, ts, 3), np.float64), (out.rotVel, (cap, rs, 3), np.float64)):
+                if a.shape[0] < cap or a.shape[1:] != shape[1:] or a.dtype != dt or not a.flags.c_contiguous:
+                    raise ValueError("state(out=...): arrays must be C-contiguous with n_capacity rows")
         self._check(self.lib.sdem_download_particles(self.h, C.byref(n), iptr(out.id), iptr(out.ptype),
                                                      iptr(out.usrmark), dptr(out.posR), dptr(out.linVel),
                                                      dptr(out.linAcc), dptr(out.theta), dptr(out.rotVel),
                                                      dptr(out.rotAcc)))
-        return out.take(slice(0, n.value))
+        k = n.value
+        if fresh:
+            return out.take(slice(0, k))
+        return Particles(out.id[:k], out.ptype[:k], out.usrmark[:k], out.posR[:k], out.linVel[:k], out.linAcc[:k],
+                         out.theta[:k], out.rotVel[:k], out.rotAcc[:k])
 
     def forces(self):
         n = self.counters()["nlocal"]

@@ -1081,6 +1081,30 @@ __global__ void k_apply_moves(Dev d) {
   }
 }
 
+// Host layout <-> device layout of the per-particle 3-vectors: the ABI's
+// [(i*levels + k)*3 + c] doubles against one 32-byte record per particle and
+// level.  A null source writes zeros.
+__global__ void k_unpack3(dbl4* __restrict__ dst, const double* __restrict__ src, int n, int levels, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!src) {
+    dst[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+    return;
+  }
+  const double* v = src + ((size_t)i * levels + k) * 3;
+  dst[i] = make_dbl4(v[0], v[1], v[2], 0.0);
+}
+
+__global__ void k_pack3(double* __restrict__ dst, const dbl4* __restrict__ src, int n, int levels, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const dbl4 a = src[i];
+  double* v = dst + ((size_t)i * levels + k) * 3;
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+}
+
 __global__ void k_step_end(Dev d, int* counters_out) {
   const int C = d.row_off[d.nall_launch];
   counters_out[SDEM_CNT_PP] = C - (int)d.counters[5];
@@ -1281,6 +1305,8 @@ struct sdem_h {
   unsigned long long* ull = nullptr;  // counters[5] (see Dev::counters), unused, red[2]
   int *out_list = nullptr, *moves = nullptr, *map_pos = nullptr, *map_id = nullptr;
   int* h_counters = nullptr;  // pinned
+  double* stage = nullptr;    // device staging of host-layout 3-vectors (upload, download)
+  size_t stage_n = 0;
   bool stepped = false;
   // two consecutive steps captured as one CUDA graph (the contact buffers
   // alternate every step, so two steps return to the same buffer parity)
@@ -1324,6 +1350,26 @@ int dalloc(sdem_h* h, T** p, size_t count) {
   cudaMemsetAsync(q, 0, bytes, h->stream);
   h->allocs.push_back(q);
   *p = (T*)q;
+  return 0;
+}
+
+// Grows the staging buffer to hold `count` doubles (upload/download only).
+int ensure_stage(sdem_h* h, size_t count) {
+  if (count <= h->stage_n) return 0;
+  if (h->stage) {
+    cudaStreamSynchronize(h->stream);
+    cudaFree(h->stage);
+    h->stage = nullptr;
+    h->stage_n = 0;
+  }
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(double));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(h, SDEM_E_NOMEM, "cudaMalloc of the upload/download staging buffer failed");
+  }
+  h->stage = (double*)q;
+  h->stage_n = count;
   return 0;
 }
 
@@ -1575,7 +1621,8 @@ int sync_and_check(sdem_h* h) {
     }
     // clear so the handle stays usable for downloads
     int z[2] = {0, 0};
-    cudaMemcpy(h->scal + S_STATUS, z, sizeof z, cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(h->scal + S_STATUS, z, sizeof z, cudaMemcpyHostToDevice, h->stream);
+    cudaStreamSynchronize(h->stream);
     return set_err(h, code, msg);
   }
   return 0;
@@ -1747,20 +1794,21 @@ int sdem_set_types(sdem_h* h, int nT, const double* radius, const double* mass, 
   rc |= dalloc(h, &h->bpp, (size_t)nT * nT * SDEM_BP_SIZE);
   rc |= dalloc(h, &h->bpw, (size_t)nT * nWT * SDEM_BP_SIZE);
   if (rc) return SDEM_E_NOMEM;
-  CK(cudaMemcpy(h->radius, radius, sizeof(double) * nT, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->mass, mass, sizeof(double) * nT, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->inertia, inertia, sizeof(double) * nT, cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(h->radius, radius, sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->mass, mass, sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->inertia, inertia, sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
   {
     std::vector<double> rm(nT), ri(nT);
     for (int t = 0; t < nT; t++) {
       rm[t] = 1.0 / mass[t];
       ri[t] = 1.0 / inertia[t];
     }
-    CK(cudaMemcpy(h->rmass, rm.data(), sizeof(double) * nT, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->rinertia, ri.data(), sizeof(double) * nT, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(h->rmass, rm.data(), sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->rinertia, ri.data(), sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
   }
-  CK(cudaMemcpy(h->bpp, bnry_pp, sizeof(double) * nT * nT * SDEM_BP_SIZE, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->bpw, bnry_pw, sizeof(double) * nT * nWT * SDEM_BP_SIZE, cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(h->bpp, bnry_pp, sizeof(double) * nT * nT * SDEM_BP_SIZE, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->bpw, bnry_pw, sizeof(double) * nT * nWT * SDEM_BP_SIZE, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   // Init_NBSM, Prtcl_NBS_Munjiza.f90:66-77 (one rank: subdomain = domain)
   double maxR = radius[0];
   for (int t = 1; t < nT; t++) maxR = std::max(maxR, radius[t]);
@@ -1826,13 +1874,14 @@ int sdem_set_walls(sdem_h* h, int nw, const double* wall, const int* flags) {
     if (rc) return SDEM_E_NOMEM;
   }
   if (nw > 0) {
-    CK(cudaMemcpy(h->walls, wall, sizeof(double) * nw * SDEM_W_SIZE, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->wflags, flags, sizeof(int) * nw * SDEM_WF_SIZE, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(h->walls, wall, sizeof(double) * nw * SDEM_W_SIZE, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->wflags, flags, sizeof(int) * nw * SDEM_WF_SIZE, cudaMemcpyHostToDevice, h->stream));
   }
   drop_graph(h);
   // the near-wall list is rebuilt at the next step
   int zero = 0;
-  CK(cudaMemcpy(h->scal + S_NEXT, &zero, sizeof zero, cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(h->scal + S_NEXT, &zero, sizeof zero, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   return 0;
 }
 
@@ -1852,52 +1901,52 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
     if (ptype[i] < 1 || ptype[i] > h->nT) return set_err(h, SDEM_E_ARG, "particle type outside 1..nT");
   }
   h->h_gid.assign(id, id + n);
-  std::vector<int> um(n, 0);
-  if (usrmark) std::copy(usrmark, usrmark + n, um.begin());
-  CK(cudaMemcpy(h->gid, id, sizeof(int) * n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->ptype, ptype, sizeof(int) * n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->usrmark, um.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-  std::vector<dbl4> buf(std::max(n, 1));
-  for (int i = 0; i < n; i++) buf[i] = make_dbl4(posR[4 * i], posR[4 * i + 1], posR[4 * i + 2], posR[4 * i + 3]);
-  CK(cudaMemcpy(h->posr, buf.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice));
-  auto put3 = [&](dbl4* dst, const double* src, int levels, int k) -> int {
-    for (int i = 0; i < n; i++) {
-      if (src) {
-        const double* v = src + ((size_t)i * levels + k) * 3;
-        buf[i] = make_dbl4(v[0], v[1], v[2], 0.0);
-      } else {
-        buf[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
-      }
-    }
-    CK(cudaMemcpy(dst, buf.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice));
-    return 0;
-  };
-  int rc = 0;
-  for (int k = 0; k < c.tsize; k++) {
-    rc |= put3(h->vel[k], linVel, c.tsize, k);
-    rc |= put3(h->acc[k], linAcc, c.tsize, k);
+  // Stream-ordered copies: a step still in flight finishes before the state
+  // is replaced, and the call returns after the last copy has landed.
+  cudaStream_t st = h->stream;
+  CK(cudaStreamSynchronize(st));
+  if (n > 0) {
+    CK(cudaMemcpyAsync(h->gid, id, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->ptype, ptype, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    if (usrmark) CK(cudaMemcpyAsync(h->usrmark, usrmark, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    else CK(cudaMemsetAsync(h->usrmark, 0, sizeof(int) * n, st));
+    // (x, y, z, r) per particle is also the device record
+    CK(cudaMemcpyAsync(h->posr, posR, sizeof(dbl4) * n, cudaMemcpyHostToDevice, st));
+    const size_t per = 3 * (size_t)(2 * c.tsize + 2 * c.rsize + 1);
+    int rs = ensure_stage(h, per * n);
+    if (rs) return rs;
+    double* sp = h->stage;
+    auto put = [&](const double* src, int levels, dbl4* const* dst) -> int {
+      if (src) CK(cudaMemcpyAsync(sp, src, sizeof(double) * 3 * levels * (size_t)n, cudaMemcpyHostToDevice, st));
+      for (int k = 0; k < levels; k++) k_unpack3<<<grid_for(n), kThreads, 0, st>>>(dst[k], src ? sp : nullptr, n, levels, k);
+      sp += 3 * (size_t)levels * n;
+      return 0;
+    };
+    dbl4* th[1] = {h->theta};
+    int rc = put(linVel, c.tsize, h->vel);
+    rc |= put(linAcc, c.tsize, h->acc);
+    rc |= put(theta, 1, th);
+    rc |= put(rotVel, c.rsize, h->rv);
+    rc |= put(rotAcc, c.rsize, h->ra);
+    if (rc) return rc;
   }
-  for (int k = 0; k < c.rsize; k++) {
-    rc |= put3(h->rv[k], rotVel, c.rsize, k);
-    rc |= put3(h->ra[k], rotAcc, c.rsize, k);
-  }
-  rc |= put3(h->theta, theta, 1, 0);
-  if (rc) return rc;
   // history reset: both buffers empty; near-wall list refreshed at the next step
   size_t G = (size_t)c.max_gid + 1;
   for (int b = 0; b < 2; b++) {
-    CK(cudaMemset(h->own_cnt[b], 0, sizeof(int) * G));
-    CK(cudaMemset(h->wh_cnt[b], 0, sizeof(int) * G));
+    CK(cudaMemsetAsync(h->own_cnt[b], 0, sizeof(int) * G, st));
+    CK(cudaMemsetAsync(h->wh_cnt[b], 0, sizeof(int) * G, st));
   }
   h->h_up.clear();
-  CK(cudaMemset(h->F, 0, sizeof(dbl4) * c.n_capacity));
-  CK(cudaMemset(h->T, 0, sizeof(dbl4) * c.n_capacity));
-  CK(cudaMemset(h->near_mask, 0, sizeof(unsigned long long) * c.n_capacity));
+  CK(cudaMemsetAsync(h->F, 0, sizeof(dbl4) * c.n_capacity, st));
+  CK(cudaMemsetAsync(h->T, 0, sizeof(dbl4) * c.n_capacity, st));
+  CK(cudaMemsetAsync(h->near_mask, 0, sizeof(unsigned long long) * c.n_capacity, st));
   int sc[S_SIZE] = {0};
   sc[S_N] = n;
   sc[S_NT] = n;
-  CK(cudaMemcpy(h->scal, sc, sizeof sc, cudaMemcpyHostToDevice));
-  CK(cudaMemset(h->ull, 0, sizeof(unsigned long long) * 8));
+  CK(cudaMemcpyAsync(h->scal, sc, sizeof sc, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(h->ull, 0, sizeof(unsigned long long) * 8, st));
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
   h->n_host = n;
   h->cur = 0;
   h->stepped = false;
@@ -1914,6 +1963,7 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
     return set_err(h, SDEM_E_ARG, "sdem_upload_contacts: bad arguments");
   const sdem_cfg& c = h->cfg;
   int n = h->n_host;
+  CK(cudaStreamSynchronize(h->stream));
   // The history the next step reads is the "previous" buffer.
   int pv = 1 - h->cur;
   std::vector<std::vector<std::pair<int, dbl4>>> wl(n);
@@ -1982,11 +2032,11 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
     pg[i] = pp[i].partner;
     hs[i] = pp[i].hist;
   }
-  CK(cudaMemcpy(h->own_cnt[pv], ocnt.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->own_c[pv], oc.data(), sizeof(int) * G * h->K, cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(h->own_cnt[pv], ocnt.data(), sizeof(int) * G, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->own_c[pv], oc.data(), sizeof(int) * G * h->K, cudaMemcpyHostToDevice, h->stream));
   if (!pp.empty()) {
-    CK(cudaMemcpy(h->c_pgid[pv], pg.data(), sizeof(int) * pp.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->c_hist[pv], hs.data(), sizeof(dbl4) * pp.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(h->c_pgid[pv], pg.data(), sizeof(int) * pp.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->c_hist[pv], hs.data(), sizeof(dbl4) * pp.size(), cudaMemcpyHostToDevice, h->stream));
   }
   h->h_up = pp;
   std::vector<int> whc(G, 0), whw(G * kKw, 0);
@@ -2002,9 +2052,10 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
     }
     whc[g] = k;
   }
-  CK(cudaMemcpy(h->wh_cnt[pv], whc.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->wh_wall[pv], whw.data(), sizeof(int) * G * kKw, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->wh_hist[pv], whh.data(), sizeof(dbl4) * G * kKw, cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(h->wh_cnt[pv], whc.data(), sizeof(int) * G, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->wh_wall[pv], whw.data(), sizeof(int) * G * kKw, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->wh_hist[pv], whh.data(), sizeof(dbl4) * G * kKw, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));   // the host tables above go out of scope
   return 0;
 }
 
@@ -2093,33 +2144,33 @@ int sdem_download_particles(sdem_h* h, int* n_out, int* id, int* ptype, int* usr
   CK(cudaMemcpy(&n, h->scal + S_N, sizeof n, cudaMemcpyDeviceToHost));
   if (n_out) *n_out = n;
   const sdem_cfg& c = h->cfg;
-  if (id) CK(cudaMemcpy(id, h->gid, sizeof(int) * n, cudaMemcpyDeviceToHost));
-  if (ptype) CK(cudaMemcpy(ptype, h->ptype, sizeof(int) * n, cudaMemcpyDeviceToHost));
-  if (usrmark) CK(cudaMemcpy(usrmark, h->usrmark, sizeof(int) * n, cudaMemcpyDeviceToHost));
-  std::vector<dbl4> buf(std::max(n, 1));
-  if (posR) {
-    CK(cudaMemcpy(buf.data(), h->posr, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < n; i++) { posR[4 * i] = buf[i].x; posR[4 * i + 1] = buf[i].y; posR[4 * i + 2] = buf[i].z; posR[4 * i + 3] = buf[i].w; }
-  }
-  auto get3 = [&](double* dst, dbl4* src, int levels, int k) -> int {
-    CK(cudaMemcpy(buf.data(), src, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < n; i++) {
-      double* v = dst + ((size_t)i * levels + k) * 3;
-      v[0] = buf[i].x; v[1] = buf[i].y; v[2] = buf[i].z;
-    }
+  cudaStream_t st = h->stream;
+  if (n <= 0) return 0;
+  if (id) CK(cudaMemcpyAsync(id, h->gid, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  if (ptype) CK(cudaMemcpyAsync(ptype, h->ptype, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  if (usrmark) CK(cudaMemcpyAsync(usrmark, h->usrmark, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  if (posR) CK(cudaMemcpyAsync(posR, h->posr, sizeof(dbl4) * n, cudaMemcpyDeviceToHost, st));
+  const size_t per = 3 * (size_t)(2 * c.tsize + 2 * c.rsize + 1);
+  rc = ensure_stage(h, per * n);
+  if (rc) return rc;
+  double* sp = h->stage;
+  auto get = [&](double* dst, int levels, dbl4* const* src) -> int {
+    if (!dst) return 0;
+    for (int k = 0; k < levels; k++) k_pack3<<<grid_for(n), kThreads, 0, st>>>(sp, src[k], n, levels, k);
+    CK(cudaMemcpyAsync(dst, sp, sizeof(double) * 3 * levels * (size_t)n, cudaMemcpyDeviceToHost, st));
+    sp += 3 * (size_t)levels * n;
     return 0;
   };
-  rc = 0;
-  for (int k = 0; k < c.tsize; k++) {
-    if (linVel) rc |= get3(linVel, h->vel[k], c.tsize, k);
-    if (linAcc) rc |= get3(linAcc, h->acc[k], c.tsize, k);
-  }
-  for (int k = 0; k < c.rsize; k++) {
-    if (rotVel) rc |= get3(rotVel, h->rv[k], c.rsize, k);
-    if (rotAcc) rc |= get3(rotAcc, h->ra[k], c.rsize, k);
-  }
-  if (theta) rc |= get3(theta, h->theta, 1, 0);
-  return rc;
+  dbl4* th[1] = {h->theta};
+  rc = get(linVel, c.tsize, h->vel);
+  rc |= get(linAcc, c.tsize, h->acc);
+  rc |= get(theta, 1, th);
+  rc |= get(rotVel, c.rsize, h->rv);
+  rc |= get(rotAcc, c.rsize, h->ra);
+  if (rc) return rc;
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  return 0;
 }
 
 int sdem_download_forces(sdem_h* h, double* F, double* T) {
@@ -2128,15 +2179,20 @@ int sdem_download_forces(sdem_h* h, double* F, double* T) {
   if (rc) return rc;
   int n = 0;
   CK(cudaMemcpy(&n, h->scal + S_N, sizeof n, cudaMemcpyDeviceToHost));
-  std::vector<dbl4> buf(std::max(n, 1));
+  if (n <= 0) return 0;
+  cudaStream_t st = h->stream;
+  rc = ensure_stage(h, 6 * (size_t)n);
+  if (rc) return rc;
   if (F) {
-    CK(cudaMemcpy(buf.data(), h->F, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < n; i++) { F[3 * i] = buf[i].x; F[3 * i + 1] = buf[i].y; F[3 * i + 2] = buf[i].z; }
+    k_pack3<<<grid_for(n), kThreads, 0, st>>>(h->stage, h->F, n, 1, 0);
+    CK(cudaMemcpyAsync(F, h->stage, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, st));
   }
   if (T) {
-    CK(cudaMemcpy(buf.data(), h->T, sizeof(dbl4) * n, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < n; i++) { T[3 * i] = buf[i].x; T[3 * i + 1] = buf[i].y; T[3 * i + 2] = buf[i].z; }
+    k_pack3<<<grid_for(n), kThreads, 0, st>>>(h->stage + 3 * (size_t)n, h->T, n, 1, 0);
+    CK(cudaMemcpyAsync(T, h->stage + 3 * (size_t)n, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, st));
   }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
   return 0;
 }
 
@@ -2419,6 +2475,7 @@ void sdem_destroy(sdem_h* h) {
   for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
+  if (h->stage) cudaFree(h->stage);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
