@@ -27,8 +27,19 @@ EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls
             "sdem_upload_contacts", "sdem_step", "sdem_step_async", "sdem_get_stream",
             "sdem_download_particles", "sdem_download_contacts", "sdem_check_restart_limit",
             "sdem_download_forces", "sdem_counters", "sdem_counter_sums", "sdem_launch_count", "sdem_profile_begin",
-            "sdem_profile_end", "sdem_profile_phase_name", "sdem_count_contacts_noalloc", "sdem_last_error",
-            "sdem_destroy")
+            "sdem_profile_end", "sdem_profile_phase_name", "sdem_count_contacts_noalloc", "sdem_selftest_fp64",
+            "sdem_last_error", "sdem_destroy")
+
+
+def selftest_fp64(n: int, seed: int = 1) -> int:
+    """Mismatching operand pairs of the library's integer-pipe binary64
+    arithmetic against the GPU's own instructions (0 expected)."""
+    lib = load()
+    out = C.c_longlong()
+    rc = lib.sdem_selftest_fp64(int(n), int(seed), C.byref(out))
+    if rc:
+        raise SdemError(rc, f"sdem_selftest_fp64 failed ({ERRORS.get(rc, rc)})")
+    return int(out.value)
 
 
 class SdemCfg(C.Structure):
@@ -112,6 +123,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_profile_phase_name.argtypes = [C.c_int]
     lib.sdem_profile_phase_name.restype = C.c_char_p
     lib.sdem_count_contacts_noalloc.argtypes = [C.POINTER(SdemCfg), C.c_double, C.c_int, P, P, P]
+    lib.sdem_selftest_fp64.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
     lib.sdem_last_error.argtypes = [P]
     lib.sdem_last_error.restype = C.c_char_p
     lib.sdem_destroy.argtypes = [P]

@@ -3,10 +3,13 @@
 // operations.  The translation unit that includes this file is compiled with
 // -fmad=false, so no a*b+c below is contracted into an FMA: every result is
 // the IEEE-rounded value of the reference's expression (gfortran, x86-64,
-// default flags).  Division and sqrt are the correctly rounded CUDA defaults.
+// default flags).  Division and sqrt are correctly rounded; they run on the
+// integer pipes (fp64_int.cuh), which GB300 has in plenty while its FP64 pipe
+// bounds the force law, and give the IEEE results bit for bit.
 #pragma once
 #include <cuda_runtime.h>
 #include "../../include/sdem_gpu.h"
+#include "fp64_int.cuh"
 
 namespace sdem {
 
@@ -39,31 +42,18 @@ __device__ __forceinline__ dbl4 d4(r3 a, double w) { return make_dbl4(a.x, a.y, 
 __device__ __forceinline__ r3 add3(r3 a, r3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ r3 sub3(r3 a, r3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ r3 scale3(r3 p, double v) { return mk3(p.x * v, p.y * v, p.z * v); }
-__device__ __forceinline__ r3 div3(r3 p, double v) { return mk3(p.x / v, p.y / v, p.z / v); }
+__device__ __forceinline__ r3 div3(r3 p, double v) {
+  return mk3(fpi::div_rn(p.x, v), fpi::div_rn(p.y, v), fpi::div_rn(p.z, v));
+}
 __device__ __forceinline__ double dot3(r3 a, r3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ r3 cross3(r3 u, r3 v) {
   return mk3(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
 }
-__device__ __forceinline__ double norm3(r3 p) { return sqrt(p.x * p.x + p.y * p.y + p.z * p.z); }
-// a/b for a divisor b whose correctly rounded reciprocal y = RN(1/b) is known:
-// q = RN(a*y), r = a - q*b (exact with an FMA), q' = RN(q + r*y) is the
-// correctly rounded quotient (Markstein's correction, IBM J. Res. Dev. 34(1),
-// 1990), i.e. bit-identical to IEEE a/b; checked against a/b on the CPU in
-// tests/test_division_correction.py.  Three such quotients by one divisor cost
-// one reciprocal and nine FP64 instructions instead of three divisions.
-__device__ __forceinline__ double div_by(double a, double b, double y) {
-  double q = a * y;
-  double r = __fma_rn(-q, b, a);
-  return __fma_rn(r, y, q);
-}
-__device__ __forceinline__ r3 div3_rcp(r3 p, double v) {
-  const double y = 1.0 / v;
-  return mk3(div_by(p.x, v, y), div_by(p.y, v, y), div_by(p.z, v, y));
-}
+__device__ __forceinline__ double norm3(r3 p) { return fpi::sqrt_rn(p.x * p.x + p.y * p.y + p.z * p.z); }
 // real4_nv / real3_nv: s/|s| with the 1e-10 guard
 __device__ __forceinline__ r3 nv3(r3 s) {
   double n = norm3(s);
-  if (n > 1.0000E-10) return div3_rcp(s, n);
+  if (n > 1.0000E-10) return div3(s, n);
   return mk3(0.0, 0.0, 0.0);
 }
 
@@ -113,10 +103,10 @@ __device__ __forceinline__ bool line_point(r3 lp1, r3 lp2, dbl4 dpos, r3& nv, do
   r3 v = sub3(lp2, lp1);
   double length = norm3(sub3(lp1, lp2));
   double r = dpos.w;
-  double t = dot3(w, v) / dot3(v, v);
+  double t = fpi::div_rn(dot3(w, v), dot3(v, v));
   if (t >= 0.0 && t <= 1.0) cp = add3(scale3(v, t), lp1);
-  else if (t >= (-r / length) && t < 0.0) cp = lp1;
-  else if (t > 1.0 && t >= (1.0 + r / length)) cp = lp2;
+  else if (t >= fpi::div_rn(-r, length) && t < 0.0) cp = lp1;
+  else if (t > 1.0 && t >= (1.0 + fpi::div_rn(r, length))) cp = lp2;
   else return false;
   ovrlp = r - norm3(sub3(cp, pos));
   if (ovrlp >= 0.0) {
@@ -187,7 +177,7 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
   double normTan1 = norm3(Ovlp_t);
   Ovlp_t = sub3(Ovlp_t, scale3(Norm_v, dot3(Ovlp_t, Norm_v)));
   double normTan2 = norm3(Ovlp_t);
-  if (normTan2 > 1.0E-10) Ovlp_t = scale3(Ovlp_t, normTan1 / normTan2);
+  if (normTan2 > 1.0E-10) Ovlp_t = scale3(Ovlp_t, fpi::div_rn(normTan1, normTan2));
   else Ovlp_t = mk3(0.0, 0.0, 0.0);
   Ovlp_t = add3(scale3(Vij_t, L.dt), Ovlp_t);
 
@@ -208,9 +198,9 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
   } else {
     double k_n = -P[SDEM_BP_KN];
     double d_n = -P[SDEM_BP_CN];
-    double sq = sqrt(ovrlp);
+    double sq = fpi::sqrt_rn(ovrlp);
     double o15 = ovrlp * sq;   // ovrlp**1.5
-    double o025 = sqrt(sq);    // ovrlp**0.25
+    double o025 = fpi::sqrt_rn(sq);    // ovrlp**0.25
     fn = k_n * o15 + d_n * o025 * vrn;
     k_t = -(P[SDEM_BP_KT] * sq);
     Ftij = scale3(Ovlp_t, k_t);
@@ -221,13 +211,13 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
   double ft_fric = P[SDEM_BP_MUS] * fabs(fn);
   if (ft > ft_fric) {
     ft_fric = P[SDEM_BP_MUK] * fabs(fn);
-    Ftij = scale3(Ftij, ft_fric / ft);
-    Ovlp_t = div3_rcp(Ftij, k_t);
+    Ftij = scale3(Ftij, fpi::div_rn(ft_fric, ft));
+    Ovlp_t = div3(Ftij, k_t);
   }
 
   r3 W_hat = sub3(Rvei, Rvej);
   double w_hat_mag = norm3(W_hat);
-  if (w_hat_mag > 1.0E-10) W_hat = div3_rcp(W_hat, w_hat_mag);
+  if (w_hat_mag > 1.0E-10) W_hat = div3(W_hat, w_hat_mag);
   else W_hat = mk3(0.0, 0.0, 0.0);
   if (L.ct_model == SDEM_CTM_CONSTANT)
     Mr = scale3(W_hat, -(P[SDEM_BP_MUR] * fabs(fn) * P[SDEM_BP_RADEFF]));

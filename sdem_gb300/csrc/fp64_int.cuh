@@ -174,4 +174,188 @@ __host__ __device__ __forceinline__ double add(double x, double y) {
 
 __host__ __device__ __forceinline__ double sub(double x, double y) { return add(x, from_bits(bits(y) ^ kSign)); }
 
+__host__ __device__ __forceinline__ double hw_sqrt(double x) {
+#ifdef __CUDA_ARCH__
+  return __dsqrt_rn(x);
+#else
+  return __builtin_sqrt(x);
+#endif
+}
+__host__ __device__ __forceinline__ double hw_div(double x, double y) {
+#ifdef __CUDA_ARCH__
+  return __ddiv_rn(x, y);
+#else
+  return x / y;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t fbits(float x) {
+#ifdef __CUDA_ARCH__
+  return (uint32_t)__float_as_uint(x);
+#else
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  return u;
+#endif
+}
+__host__ __device__ __forceinline__ float ffrom(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float x;
+  memcpy(&x, &u, 4);
+  return x;
+#endif
+}
+// single-precision seeds: ~22 correct bits are all the refinement needs
+__host__ __device__ __forceinline__ float rsqrt_seed(float x) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  float r = 1.0f / __builtin_sqrtf(x);
+#ifdef FPI_HOST_SEED_HOOK
+  r = FPI_HOST_SEED_HOOK(r);
+#endif
+  return r;
+#endif
+}
+__host__ __device__ __forceinline__ float rcp_seed(float x) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  float r = 1.0f / x;
+#ifdef FPI_HOST_SEED_HOOK
+  r = FPI_HOST_SEED_HOOK(r);
+#endif
+  return r;
+#endif
+}
+__host__ __device__ __forceinline__ int64_t smulhi(int64_t a, int64_t b) {
+#ifdef __CUDA_ARCH__
+  return __mul64hi(a, b);
+#else
+  return (int64_t)(((__int128)a * b) >> 64);
+#endif
+}
+// Q2.62 fixed point: value * 2^62 in a 64-bit word (values below 4)
+__host__ __device__ __forceinline__ uint64_t q62_from_seed(float r) {
+  // r = 1.m * 2^k, k in [-3, 1]: (2^23 + m) * 2^(39 + k) = r * 2^62
+  const uint32_t rb = fbits(r);
+  const int k = (int)(rb >> 23) - 127;
+  return ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u)) << (39 + k);
+}
+
+// sqrt(x), correctly rounded.  Positive normal x take the integer path:
+// x = M * 2^(2h) with M in [1, 4); a single-precision seed of 1/sqrt(M) is
+// refined by two coupled Newton (Goldschmidt) steps in Q3.61 fixed point,
+// g -> sqrt(M), h -> 1/(2 sqrt(M)), residual d = 1/2 - g*h (Goldschmidt,
+// 1964; Markstein, IBM J. Res. Dev. 34(1), 1990), which leave g within a
+// few 2^-58 of sqrt(M).  The candidate S = round(g * 2^52) is then settled by
+// the exact integer test of round-to-nearest, S^2 - S < M*2^104 <= S^2 + S,
+// and moved by one unit while it fails.  Other x take the hardware sqrt.
+__host__ __device__ __forceinline__ double sqrt_rn(double x) {
+  const uint64_t u = bits(x);
+  const uint32_t e = (uint32_t)(u >> 52);      // the sign bit makes negatives large
+  if (e - 1u >= 2046u) {
+    if ((u << 1) == 0) return x;               // sqrt(+-0) = +-0
+    return hw_sqrt(x);
+  }
+  const uint64_t f = u & kMant;
+  const int E = (int)e - 1023;
+  const uint32_t odd = (uint32_t)E & 1u;
+  const uint64_t A = ((f | kHid) << 10) << odd;            // M in Q2.62
+  const float fm = ffrom(((127u + odd) << 23) | (uint32_t)(f >> 29));
+  const uint64_t R0 = q62_from_seed(rsqrt_seed(fm));       // ~1/sqrt(M), Q2.62
+  // g and h in Q3.61: sqrt(M) reaches 2, and a seed error must not overflow
+  int64_t g = (int64_t)(mulhi(A, R0) << 1);                 // ~sqrt(M)
+  int64_t hh = (int64_t)(R0 >> 2);                          // ~1/(2 sqrt(M))
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const int64_t p = (int64_t)(mulhi((uint64_t)g, (uint64_t)hh) << 3);
+    const int64_t d = ((int64_t)1 << 60) - p;
+    g += (int64_t)((uint64_t)smulhi(g, d) << 3);
+    hh += (int64_t)((uint64_t)smulhi(hh, d) << 3);
+  }
+  uint64_t S = ((uint64_t)g + (1u << 8)) >> 9;              // ~sqrt(M) * 2^52
+  // D = M*2^104 - S^2, exact in 64 bits while S is within a few units
+  const uint64_t Nlo = A << 42;
+  int64_t D = (int64_t)(Nlo - S * S);
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    if (D > (int64_t)S) { D -= (int64_t)(2 * S + 1); S += 1; }
+    else if (D <= -(int64_t)S) { D += (int64_t)(2 * S - 1); S -= 1; }
+  }
+  const int er = ((E - (int)odd) >> 1) + 1023;
+  return from_bits((((uint64_t)(er - 1)) << 52) + S);
+}
+
+// x / y, correctly rounded.  Normal x and y with a normal quotient take the
+// integer path: the significand ratio Q = (mx/my) * 2^k in [1, 2) comes from a
+// single-precision seed of 1/my refined by two Newton steps in Q2.62
+// (z <- z + z*(1 - my*z)), the candidate S = round(Q * 2^52) is settled by the
+// exact remainder R = mx*2^(52+k) - S*my (round to nearest: |R| <= my/2, ties
+// to the even S) and moved by one unit while the test fails.  Zeros,
+// subnormals, infinities, NaNs and quotients outside the normal range take
+// the hardware division.
+__host__ __device__ __forceinline__ double div_rn(double x, double y) {
+  const uint64_t a = bits(x), b = bits(y);
+  const uint32_t ea = (uint32_t)(a >> 52) & 0x7FFu, eb = (uint32_t)(b >> 52) & 0x7FFu;
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u) {
+    if ((a << 1) == 0 && eb - 1u < 2046u) return from_bits((a ^ b) & kSign);   // +-0 / normal
+    return hw_div(x, y);
+  }
+  const uint64_t ma = (a & kMant) | kHid, mb = (b & kMant) | kHid;
+  const uint32_t k = ma < mb ? 1u : 0u;                    // Q = ma*2^k/mb in [1, 2)
+  const int eq = (int)ea - (int)eb + 1023 - (int)k;
+  if (eq < 1 || eq > 2046) return hw_div(x, y);
+  const uint64_t B = mb << 10;                             // my in Q2.62, [1, 2)
+  const float fb = ffrom((127u << 23) | (uint32_t)((mb & kMant) >> 29));
+  int64_t z = (int64_t)q62_from_seed(rcp_seed(fb));         // ~1/my
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const int64_t t = ((int64_t)1 << 62) - (int64_t)(mulhi(B, (uint64_t)z) << 2);   // 1 - my*z
+    z += (int64_t)((uint64_t)smulhi(z, t) << 2);
+  }
+  const uint64_t Aq = (ma << 10) << k;                     // mx*2^k in Q2.62 (below 4)
+  const uint64_t q = mulhi(Aq, (uint64_t)z) << 2;          // ~Q in Q2.62
+  uint64_t S = (q + (1u << 9)) >> 10;                      // ~Q * 2^52
+  // R = ma*2^(52+k) - S*mb, exact in 64 bits while S is within a few units
+  int64_t R = (int64_t)(((ma << 52) << k) - S * mb);
+  const int64_t hb = (int64_t)mb;
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    if (2 * R > hb || (2 * R == hb && (S & 1u))) { R -= hb; S += 1; }
+    else if (2 * R < -hb || (2 * R == -hb && (S & 1u))) { R += hb; S -= 1; }
+  }
+  const uint64_t sg = (a ^ b) & kSign;
+  return from_bits(sg | ((((uint64_t)(eq - 1)) << 52) + S));
+}
+
+// floor(q) as an int when 0 <= floor(q) < n (q = -0 counts as 0), else -1;
+// NaN and infinities give -1.  Integer work only.
+__host__ __device__ __forceinline__ int floor_in_range(double q, int n) {
+  const uint64_t u = bits(q);
+  if ((u << 1) == 0) return n > 0 ? 0 : -1;
+  if (u >> 63) return -1;                        // negative
+  const uint32_t e = (uint32_t)(u >> 52);
+  if (e < 1023u) return n > 0 ? 0 : -1;          // 0 < q < 1
+  if (e > 1023u + 30u) return -1;                // >= 2^31, infinity, NaN
+  const uint64_t v = ((u & kMant) | kHid) >> (1075u - e);
+  return v < (uint64_t)n ? (int)v : -1;
+}
+
+// x * (-0.5), exact for every x whose half is a normal number or zero: the
+// exponent field drops by one and the sign flips.  Subnormal halves (which
+// round), infinities and NaNs take the hardware multiplication.
+__host__ __device__ __forceinline__ double mul_neg_half(double x) {
+  const uint64_t u = bits(x);
+  const uint32_t e = (uint32_t)(u >> 52) & 0x7FFu;
+  if (e - 2u < 2045u) return from_bits((u - (1ull << 52)) ^ kSign);
+  if ((u << 1) == 0) return from_bits(u ^ kSign);
+  return hw_mul(x, -0.5);
+}
+
 }  // namespace fpi

@@ -23,7 +23,8 @@
 //                                      (Prtcl_CL_and_CF.f90:142-198, 256-296, 732-798): one thread per
 //                                      contact, full warps of FP64 work
 //   k_wall_force                       ContactForce_PW (:832-856), one thread per wall contact
-//   k_degree_scan, k_degree_scatter    particles grouped by contact count (the gather order)
+//   k_degree_scatter                   particles grouped by contact count (the gather order; the
+//                                      bucket starts come from k_gid_index)
 //   k_gather                           per particle, sums its contact records in the reference's scatter
 //                                      order (a deterministic gather), then its wall contacts in
 //                                      near-list order
@@ -48,6 +49,7 @@
 
 #include "../../include/sdem_gpu.h"
 #include "dem_device.cuh"
+#include "fp64_int.cuh"
 
 using sdem::dbl4;
 using sdem::make_dbl4;
@@ -89,14 +91,13 @@ struct Dev {
   int tsize, rsize, pi, pri, quirk;
   sdem::LawCfg law;
   double3 g;
-  double cell, rcell, x0, y0, z0;
+  double cell, x0, y0, z0;
   int nx, ny, nz;
   long long ncell;
   double3 dmin, dmax;
   // tables
   int nT, nWT;
   const double *radius, *mass, *inertia, *bpp, *bpw;
-  const double *rmass, *rinertia;   // RN(1/mass), RN(1/inertia) per type
   int nw;
   const double* walls;
   const int* wflags;
@@ -386,13 +387,13 @@ __global__ void k_ghost_count(Dev d) {
 __global__ void k_bin(Dev d) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= *d.nt) return;
-  dbl4 P = d.posr[p];
-  double rpdx = P.x - d.x0, rpdy = P.y - d.y0, rpdz = P.z - d.z0;
-  // rpd/cell_len, IEEE-exact through the reciprocal of the cell size
-  double fx = floor(sdem::div_by(rpdx, d.cell, d.rcell)), fy = floor(sdem::div_by(rpdy, d.cell, d.rcell)),
-         fz = floor(sdem::div_by(rpdz, d.cell, d.rcell));
-  // grid index is floor()+1 in [1, n]; 0-based here
-  if (!(fx >= 0.0 && fx < (double)d.nx && fy >= 0.0 && fy < (double)d.ny && fz >= 0.0 && fz < (double)d.nz)) {
+  const dbl4 P = d.posr[p];
+  // floor((x - x0) / cell_len) with IEEE rounding of the subtraction and the
+  // division, all on the integer pipes; the reference's index is this + 1
+  const int fx = fpi::floor_in_range(fpi::div_rn(fpi::sub(P.x, d.x0), d.cell), d.nx);
+  const int fy = fpi::floor_in_range(fpi::div_rn(fpi::sub(P.y, d.y0), d.cell), d.ny);
+  const int fz = fpi::floor_in_range(fpi::div_rn(fpi::sub(P.z, d.z0), d.cell), d.nz);
+  if (fx < 0 || fy < 0 || fz < 0) {
     raise(d, SDEM_E_GRID, p);
     d.cell_of[p] = -1;
     return;
@@ -600,18 +601,6 @@ __global__ void __launch_bounds__(kThreads) k_wall_detect(Dev d) {
   if ((threadIdx.x & 31) == 0 && nwc) atomicAdd(&d.counters[1], (unsigned long long)nwc);
 }
 
-__global__ void k_degree_scan(Dev d) {
-  // one warp: exclusive scan of the kDegBuckets counts, highest degree first
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int b = kDegBuckets - 1; b >= 0; b--) {
-      d.deg_start[b] = acc;
-      acc += d.deg_cnt[b];
-      d.deg_cnt[b] = 0;   // ready for the next step
-    }
-  }
-}
-
 __global__ void k_degree_scatter(Dev d) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= *d.n) return;
@@ -654,6 +643,24 @@ __global__ void __launch_bounds__(kThreads) k_wall_force(Dev d) {
 // one-thread-per-contact force kernel reads its row instead of searching the
 // row offsets.
 __global__ void k_gid_index(Dev d) {
+  static_assert(kDegBuckets == 64, "two buckets per lane of one warp");
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    // start of every degree bucket of the gather order, highest degree first
+    // (k_wall_detect has counted them); the counts are cleared for the next step
+    const int l = threadIdx.x;
+    const int b0 = kDegBuckets - 1 - 2 * l, b1 = b0 - 1;
+    const int c0 = d.deg_cnt[b0], c1 = d.deg_cnt[b1];
+    const int v = c0 + c1;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (l >= o) incl += t;
+    }
+    d.deg_start[b0] = incl - v;
+    d.deg_start[b1] = incl - v + c0;
+    d.deg_cnt[b0] = 0;
+    d.deg_cnt[b1] = 0;
+  }
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p < *d.n) d.own_cnt[d.gid[p]] = 0;
   if (p < *d.nt) {
@@ -715,7 +722,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d) {
     const r3 sv = sdem::sub3(sdem::xyz(Pj), sdem::xyz(Pi));
     const double normv = sdem::norm3(sv);
     const double ovrlp = (Pi.w + Pj.w) - normv;
-    r3 Norm_v = (normv > 1.0000E-10) ? sdem::div3_rcp(sv, normv) : sdem::mk3(0.0, 0.0, 0.0);
+    r3 Norm_v = (normv > 1.0000E-10) ? sdem::div3(sv, normv) : sdem::mk3(0.0, 0.0, 0.0);
     r3 S, M, Mr;
     sdem::force_law(d.law, P, sdem::xyz(Vi), sdem::xyz(Vj), sdem::xyz(Wi), sdem::xyz(Wj), Pi.w, Pj.w, Norm_v, ovrlp,
                     hist, S, M, Mr);
@@ -872,14 +879,16 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
   const int ti = d.ptype[p];
 
   // clc_Acceleration, Prtcl_DEMSystem.f90:174-180
-  // F/Mass and T/Inertia, IEEE-exact through the per-type reciprocals
+  // F/Mass and T/Inertia (IEEE quotients)
   const double Mass = d.mass[ti - 1], Inertia = d.inertia[ti - 1];
-  const double rM = d.rmass[ti - 1], rI = d.rinertia[ti - 1];
-  r3 a1 = sdem::add3(sdem::mk3(sdem::div_by(F.x, Mass, rM), sdem::div_by(F.y, Mass, rM), sdem::div_by(F.z, Mass, rM)),
+  r3 a1 = sdem::add3(sdem::div3(F, Mass),
                      sdem::mk3(d.g.x, d.g.y, d.g.z));
-  r3 al1 = sdem::mk3(sdem::div_by(T.x, Inertia, rI), sdem::div_by(T.y, Inertia, rI), sdem::div_by(T.z, Inertia, rI));
+  r3 al1 = sdem::div3(T, Inertia);
   const double dt = d.law.dt;
-  const double AB2C1 = 3.0 / 2.0, AB2C2 = -1.0 / 2.0;
+  const double AB2C1 = 3.0 / 2.0;
+  // AB2's second coefficient is -1/2: v * (-1/2) is exact, an exponent
+  // decrement on the integer pipe instead of a multiplication on the FP64 pipe
+  auto nh3 = [](r3 v) { return sdem::mk3(fpi::mul_neg_half(v.x), fpi::mul_neg_half(v.y), fpi::mul_neg_half(v.z)); };
   const double AB3C1 = 23.0 / 12.0, AB3C2 = -16.0 / 12.0, AB3C3 = 5.0 / 12.0;
 
   // Prtcl_Integrate, linear part (Prtcl_Integration.f90:25-53)
@@ -893,8 +902,8 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
   } else if (d.pi == SDEM_PIM_AB2) {
     r3 lv2 = sdem::xyz(d.vel1[p]);
     r3 la2 = sdem::xyz(d.acc1[p]);
-    x = sdem::add3(x, sdem::scale3(sdem::add3(sdem::scale3(lv1, AB2C1), sdem::scale3(lv2, AB2C2)), dt));
-    lv1_new = sdem::add3(lv1, sdem::scale3(sdem::add3(sdem::scale3(a1, AB2C1), sdem::scale3(la2, AB2C2)), dt));
+    x = sdem::add3(x, sdem::scale3(sdem::add3(sdem::scale3(lv1, AB2C1), nh3(lv2)), dt));
+    lv1_new = sdem::add3(lv1, sdem::scale3(sdem::add3(sdem::scale3(a1, AB2C1), nh3(la2)), dt));
     d.vel1[p] = sdem::d4(lv1, 0.0);
     d.acc1[p] = sdem::d4(a1, 0.0);
     d.acc0[p] = sdem::d4(a1, 0.0);
@@ -926,8 +935,8 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
     r3 wa = d.quirk ? lv1_new : rw1;
     r3 rw2 = sdem::xyz(d.rv1[p]);
     r3 ra2 = sdem::xyz(d.ra1[p]);
-    th = sdem::add3(th, sdem::scale3(sdem::add3(sdem::scale3(wa, AB2C1), sdem::scale3(rw2, AB2C2)), dt));
-    d.rv0[p] = sdem::d4(sdem::add3(wa, sdem::scale3(sdem::add3(sdem::scale3(al1, AB2C1), sdem::scale3(ra2, AB2C2)), dt)), 0.0);
+    th = sdem::add3(th, sdem::scale3(sdem::add3(sdem::scale3(wa, AB2C1), nh3(rw2)), dt));
+    d.rv0[p] = sdem::d4(sdem::add3(wa, sdem::scale3(sdem::add3(sdem::scale3(al1, AB2C1), nh3(ra2)), dt)), 0.0);
     d.rv1[p] = sdem::d4(wa, 0.0);
     d.ra1[p] = sdem::d4(al1, 0.0);
     d.ra0[p] = sdem::d4(al1, 0.0);
@@ -1079,6 +1088,65 @@ __global__ void k_apply_moves(Dev d) {
     if (d.rsize > 2) { d.rv2[dst] = d.rv2[src]; d.ra2[dst] = d.ra2[src]; }
     d.near_mask[dst] = d.near_mask[src];
   }
+}
+
+// Self-test of the integer-pipe arithmetic against the hardware instructions:
+// operand pairs from a counter-based generator in five families (random bit
+// patterns, the physics range, perfect squares and neighbours, exact
+// quotients and neighbours, grid coordinates near cell edges).
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b) || (a != a && b != b);
+}
+__global__ void k_selftest_fp64(long long n, unsigned long long seed, unsigned long long* bad) {
+  unsigned long long nb = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long r0 = splitmix(seed ^ (unsigned long long)i), r1 = splitmix(r0), r2 = splitmix(r1);
+    unsigned long long ua, ub;
+    switch (i % 5) {
+      case 0: ua = r0; ub = r1; break;
+      case 1: {
+        const unsigned long long ea = 983 + r2 % 60, eb = 983 + (r2 >> 8) % 60;
+        ua = ((r2 >> 20) & 1ull) << 63 | ea << 52 | (r0 & fpi::kMant);
+        ub = ((r2 >> 21) & 1ull) << 63 | eb << 52 | (r1 & fpi::kMant);
+        break;
+      }
+      case 2: {
+        const unsigned long long k = (r0 >> 38) | 1ull;
+        const double sq = (double)k * (double)k;
+        ua = (unsigned long long)__double_as_longlong(sq) + (r2 % 5) - 2;
+        ub = (unsigned long long)__double_as_longlong((double)k);
+        break;
+      }
+      case 3: {
+        const unsigned long long m1 = (r0 >> 40) | 1ull, m2 = (r1 >> 40) | 1ull;
+        ua = (unsigned long long)__double_as_longlong((double)m1 * (double)m2) + (r2 % 3) - 1;
+        ub = (unsigned long long)__double_as_longlong((double)m2);
+        break;
+      }
+      default: {
+        const double cell = 1.2e-3 * (1.0 + (double)(r2 % 1000) * 1e-4);
+        const double x = ((double)(long long)(r0 % 4000) - 100.0) * cell + ((double)(r1 % 2001) - 1000.0) * 1e-19;
+        ua = (unsigned long long)__double_as_longlong(x);
+        ub = (unsigned long long)__double_as_longlong(cell);
+      }
+    }
+    const double x = __longlong_as_double((long long)ua), y = __longlong_as_double((long long)ub);
+    bool ok = same_bits(fpi::sqrt_rn(x), __dsqrt_rn(x)) && same_bits(fpi::div_rn(x, y), __ddiv_rn(x, y)) &&
+              same_bits(fpi::div_rn(y, x), __ddiv_rn(y, x)) && same_bits(fpi::add(x, y), __dadd_rn(x, y)) &&
+              same_bits(fpi::sub(x, y), __dsub_rn(x, y)) && same_bits(fpi::mul(x, y), __dmul_rn(x, y)) &&
+              same_bits(fpi::mul_neg_half(x), __dmul_rn(x, -0.5));
+    const double q = __ddiv_rn(x, y), f = floor(q);
+    const int want = (f >= 0.0 && f < 4000.0) ? (int)f : -1;
+    ok = ok && fpi::floor_in_range(q, 4000) == want;
+    nb += ok ? 0ull : 1ull;
+  }
+  if (nb) atomicAdd(bad, nb);
 }
 
 // Host layout <-> device layout of the per-particle 3-vectors: the ABI's
@@ -1259,7 +1327,6 @@ struct sdem_h {
   double maxR = 0.0;
   std::vector<double> h_radius;
   double *radius = nullptr, *mass = nullptr, *inertia = nullptr, *bpp = nullptr, *bpw = nullptr;
-  double *rmass = nullptr, *rinertia = nullptr;
   int nw = 0;
   double* walls = nullptr;
   int* wflags = nullptr;
@@ -1408,7 +1475,6 @@ Dev make_dev(sdem_h* h) {
   d.law.dt = c.dt;
   d.g = make_double3(c.gravity[0], c.gravity[1], c.gravity[2]);
   d.cell = h->cell;
-  d.rcell = 1.0 / h->cell;
   d.x0 = h->x0;
   d.y0 = h->y0;
   d.z0 = h->z0;
@@ -1423,8 +1489,6 @@ Dev make_dev(sdem_h* h) {
   d.radius = h->radius;
   d.mass = h->mass;
   d.inertia = h->inertia;
-  d.rmass = h->rmass;
-  d.rinertia = h->rinertia;
   d.bpp = h->bpp;
   d.bpw = h->bpw;
   d.nw = h->nw;
@@ -1579,7 +1643,6 @@ int enqueue_step(sdem_h* h) {
   mark(PH_WALL_FORCE);
   k_wall_force<<<std::max(1, h->num_sms * 2), kThreads, 0, st>>>(d);
   mark(PH_GATHER);
-  k_degree_scan<<<1, 32, 0, st>>>(d);
   k_degree_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
   k_gather<true><<<grid_for(n), kThreads, 0, st>>>(d);
   k_integrate<<<grid_for(n), kThreads, 0, st>>>(d);
@@ -1589,7 +1652,7 @@ int enqueue_step(sdem_h* h) {
   mark(PH_END);
   k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS);
   mark(kPhases);
-  L += 1 + 3 + 1 + 1 + 2 + 3 + 1 + 1 + 1 + 4 + 2 + 1;
+  L += 1 + 3 + 1 + 1 + 2 + 3 + 1 + 1 + 1 + 3 + 2 + 1;
   h->launches += L;
   if (ev) h->prof_steps++;
   h->cur = 1 - h->cur;
@@ -1789,23 +1852,12 @@ int sdem_set_types(sdem_h* h, int nT, const double* radius, const double* mass, 
   rc |= dalloc(h, &h->radius, nT);
   rc |= dalloc(h, &h->mass, nT);
   rc |= dalloc(h, &h->inertia, nT);
-  rc |= dalloc(h, &h->rmass, nT);
-  rc |= dalloc(h, &h->rinertia, nT);
   rc |= dalloc(h, &h->bpp, (size_t)nT * nT * SDEM_BP_SIZE);
   rc |= dalloc(h, &h->bpw, (size_t)nT * nWT * SDEM_BP_SIZE);
   if (rc) return SDEM_E_NOMEM;
   CK(cudaMemcpyAsync(h->radius, radius, sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->mass, mass, sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->inertia, inertia, sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
-  {
-    std::vector<double> rm(nT), ri(nT);
-    for (int t = 0; t < nT; t++) {
-      rm[t] = 1.0 / mass[t];
-      ri[t] = 1.0 / inertia[t];
-    }
-    CK(cudaMemcpyAsync(h->rmass, rm.data(), sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->rinertia, ri.data(), sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream));
-  }
   CK(cudaMemcpyAsync(h->bpp, bnry_pp, sizeof(double) * nT * nT * SDEM_BP_SIZE, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->bpw, bnry_pw, sizeof(double) * nT * nWT * SDEM_BP_SIZE, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -2421,7 +2473,6 @@ int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, c
   d.nt = &S->n;   // no periodic images here
   d.status = S->status;
   d.cell = cell;
-  d.rcell = 1.0 / cell;
   d.x0 = x0;
   d.y0 = y0;
   d.z0 = z0;
@@ -2465,6 +2516,26 @@ int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, c
   if (status == SDEM_E_GRID)
     return noalloc_fail(SDEM_E_GRID, "sdem_count_contacts_noalloc: a particle is outside the padded search grid");
   if (status != 0) return noalloc_fail(status, "sdem_count_contacts_noalloc: device error");
+  return 0;
+}
+
+int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatches) {
+  if (n < 0 || !mismatches) return SDEM_E_ARG;
+  unsigned long long* bad = nullptr;
+  if (cudaMalloc(&bad, sizeof *bad) != cudaSuccess) {
+    cudaGetLastError();
+    return SDEM_E_NOMEM;
+  }
+  unsigned long long hb = 0;
+  cudaError_t e = cudaMemset(bad, 0, sizeof *bad);
+  if (e == cudaSuccess) {
+    k_selftest_fp64<<<1216, 256>>>(n, seed, bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&hb, bad, sizeof hb, cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (e != cudaSuccess) return SDEM_E_CUDA;
+  *mismatches = (long long)hb;
   return 0;
 }
 

@@ -9,6 +9,25 @@
 #include <cstdint>
 #include <random>
 
+// The device seeds (rsqrt.approx / rcp.approx) carry a few ulp of error that
+// the host's 1/sqrtf and 1/x do not: with NOISE set, every host seed is moved
+// by a pseudo-random amount of up to +-64 ulp (relative 2^-17), far beyond
+// the device's error, so the refinement and the final rounding test are
+// exercised with worse seeds than the GPU ever produces.
+#include <cstdint>
+#include <cstring>
+static uint64_t g_noise = 0x9E3779B97F4A7C15ull;
+static int g_noise_on = 0;
+static float seed_noise(float r) {
+  if (!g_noise_on) return r;
+  g_noise ^= g_noise << 13; g_noise ^= g_noise >> 7; g_noise ^= g_noise << 17;
+  uint32_t u;
+  memcpy(&u, &r, 4);
+  u += (uint32_t)((int32_t)(g_noise % 129) - 64);
+  memcpy(&r, &u, 4);
+  return r;
+}
+#define FPI_HOST_SEED_HOOK seed_noise
 #include "../../sdem_gb300/csrc/fp64_int.cuh"
 
 static uint64_t B(double x) { uint64_t u; memcpy(&u, &x, 8); return u; }
@@ -20,10 +39,26 @@ static bool same(double a, double b) {
 
 static long bad = 0, checked = 0;
 static void check(double x, double y) {
-  const double r[4] = {fpi::add(x, y), fpi::sub(x, y), fpi::mul(x, y), fpi::add(y, x)};
-  const double e[4] = {x + y, x - y, x * y, y + x};
-  const char* nm[4] = {"add", "sub", "mul", "add(y,x)"};
-  for (int k = 0; k < 4; k++) {
+  const double r[8] = {fpi::add(x, y), fpi::sub(x, y), fpi::mul(x, y), fpi::add(y, x), fpi::mul_neg_half(x),
+                       fpi::sqrt_rn(x), fpi::div_rn(x, y), fpi::div_rn(y, x)};
+  const double e[8] = {x + y, x - y, x * y, y + x, x * -0.5, std::sqrt(x), x / y, y / x};
+  const char* nm[8] = {"add", "sub", "mul", "add(y,x)", "mul_neg_half", "sqrt", "div", "div(y,x)"};
+  {
+    // floor_in_range against floor() and a range test, for a few grid sizes
+    const int ns[3] = {1, 37, 1000000};
+    for (int j = 0; j < 3; j++) {
+      for (double q : {x, y, x * 1e-300, y * 1e300, (double)(int64_t)(x) }) {
+        const double f = std::floor(q);
+        const int want = (f >= 0.0 && f < (double)ns[j]) ? (int)f : -1;
+        checked++;
+        if (fpi::floor_in_range(q, ns[j]) != want) {
+          if (bad < 20) printf("MISMATCH floor_in_range q=%a n=%d got=%d want=%d\n", q, ns[j], fpi::floor_in_range(q, ns[j]), want);
+          bad++;
+        }
+      }
+    }
+  }
+  for (int k = 0; k < 8; k++) {
     checked++;
     if (!same(r[k], e[k])) {
       if (bad < 20)
@@ -45,7 +80,26 @@ int main(int argc, char** argv) {
                        2.2250738585072009e-308, 1.7976931348623157e308, -1.7976931348623157e308, 0.5, 3.0, 1e-300};
   for (double a : sp)
     for (double b : sp) check(a, b);
+  if (argc > 3) g_noise_on = atoi(argv[3]);
   for (long i = 0; i < n; i++) {
+    // 0) perfect squares and their neighbours (exact and near-exact roots),
+    //    exact quotients and their neighbours
+    {
+      const uint64_t k = (g() >> 38) | 1u;            // up to 26 bits
+      const double sq = (double)k * (double)k;          // exact
+      uint64_t sb = B(sq) + (g() % 5) - 2;
+      check(D(sb), (double)k);
+      const uint64_t m1 = (g() >> 40) | 1u, m2 = (g() >> 40) | 1u;
+      check((double)m1 * (double)m2, (double)m2);     // exact quotient m1
+      check(D(B((double)m1 * (double)m2) + 1), (double)m2);
+    }
+    // grid coordinates: q = (x - x0) / cell around integers and cell edges
+    {
+      const double cell = 1.2e-3 * (1.0 + (g() % 1000) * 1e-4);
+      const double xx = ((double)(int64_t)(g() % 4000) - 100.0) * cell + ((double)(g() % 2001) - 1000.0) * 1e-19;
+      check(xx, cell);
+      check(-0.0, cell);
+    }
     // 1) uniformly random bit patterns (every exponent, specials included)
     check(D(u64()), D(u64()));
     // 2) operands of the physics range (|x| in 1e-12..1e6), close exponents
