@@ -43,7 +43,8 @@ __device__ __forceinline__ r3 add3(r3 a, r3 b) { return mk3(a.x + b.x, a.y + b.y
 __device__ __forceinline__ r3 sub3(r3 a, r3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ r3 scale3(r3 p, double v) { return mk3(p.x * v, p.y * v, p.z * v); }
 __device__ __forceinline__ r3 div3(r3 p, double v) {
-  return mk3(fpi::div_rn(p.x, v), fpi::div_rn(p.y, v), fpi::div_rn(p.z, v));
+  const fpi::Divisor dv = fpi::divisor(v);   // one reciprocal refinement for three quotients
+  return mk3(fpi::div_by(p.x, dv), fpi::div_by(p.y, dv), fpi::div_by(p.z, dv));
 }
 __device__ __forceinline__ double dot3(r3 a, r3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ r3 cross3(r3 u, r3 v) {
@@ -53,7 +54,7 @@ __device__ __forceinline__ double norm3(r3 p) { return fpi::sqrt_rn(p.x * p.x + 
 // real4_nv / real3_nv: s/|s| with the 1e-10 guard
 __device__ __forceinline__ r3 nv3(r3 s) {
   double n = norm3(s);
-  if (n > 1.0000E-10) return div3(s, n);
+  if (fpi::gt(n, 1.0000E-10)) return div3(s, n);
   return mk3(0.0, 0.0, 0.0);
 }
 
@@ -168,7 +169,8 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
   r3 Vrij = add3(sub3(Veli, Velj), Vel_w);
   double vrn = dot3(Vrij, Norm_v);
   double VelRel = hist.w;
-  if (VelRel < -1.0) VelRel = fabs(vrn);
+  // comparisons run on the integer pipes (fpi::gt/lt: IEEE semantics)
+  if (fpi::lt(VelRel, -1.0)) VelRel = fabs(vrn);
 
   r3 Vij_n = scale3(Norm_v, vrn);
   r3 Vij_t = sub3(Vrij, Vij_n);
@@ -177,7 +179,7 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
   double normTan1 = norm3(Ovlp_t);
   Ovlp_t = sub3(Ovlp_t, scale3(Norm_v, dot3(Ovlp_t, Norm_v)));
   double normTan2 = norm3(Ovlp_t);
-  if (normTan2 > 1.0E-10) Ovlp_t = scale3(Ovlp_t, fpi::div_rn(normTan1, normTan2));
+  if (fpi::gt(normTan2, 1.0E-10)) Ovlp_t = scale3(Ovlp_t, fpi::div_rn(normTan1, normTan2));
   else Ovlp_t = mk3(0.0, 0.0, 0.0);
   Ovlp_t = add3(scale3(Vij_t, L.dt), Ovlp_t);
 
@@ -188,7 +190,7 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
   double fn, k_t;
   r3 Ftij;
   if (L.cf_type == SDEM_CFT_LSD) {
-    double Vel_in = (VelRel > 0.01) ? VelRel : 0.01;
+    double Vel_in = fpi::gt(VelRel, 0.01) ? VelRel : 0.01;
     double v04 = pow(Vel_in, 0.4);
     double k_n = -(P[SDEM_BP_KN] * v04);
     double d_n = -(P[SDEM_BP_CN] * pow(Vel_in, 0.2));
@@ -209,7 +211,7 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
 
   double ft = norm3(Ftij);
   double ft_fric = P[SDEM_BP_MUS] * fabs(fn);
-  if (ft > ft_fric) {
+  if (fpi::gt(ft, ft_fric)) {
     ft_fric = P[SDEM_BP_MUK] * fabs(fn);
     Ftij = scale3(Ftij, fpi::div_rn(ft_fric, ft));
     Ovlp_t = div3(Ftij, k_t);
@@ -217,7 +219,7 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
 
   r3 W_hat = sub3(Rvei, Rvej);
   double w_hat_mag = norm3(W_hat);
-  if (w_hat_mag > 1.0E-10) W_hat = div3(W_hat, w_hat_mag);
+  if (fpi::gt(w_hat_mag, 1.0E-10)) W_hat = div3(W_hat, w_hat_mag);
   else W_hat = mk3(0.0, 0.0, 0.0);
   if (L.ct_model == SDEM_CTM_CONSTANT)
     Mr = scale3(W_hat, -(P[SDEM_BP_MUR] * fabs(fn) * P[SDEM_BP_RADEFF]));

@@ -299,28 +299,48 @@ __host__ __device__ __forceinline__ double sqrt_rn(double x) {
 // exact remainder R = mx*2^(52+k) - S*my (round to nearest: |R| <= my/2, ties
 // to the even S) and moved by one unit while the test fails.  Zeros,
 // subnormals, infinities, NaNs and quotients outside the normal range take
-// the hardware division.
-__host__ __device__ __forceinline__ double div_rn(double x, double y) {
-  const uint64_t a = bits(x), b = bits(y);
-  const uint32_t ea = (uint32_t)(a >> 52) & 0x7FFu, eb = (uint32_t)(b >> 52) & 0x7FFu;
-  if (ea - 1u >= 2046u || eb - 1u >= 2046u) {
-    if ((a << 1) == 0 && eb - 1u < 2046u) return from_bits((a ^ b) & kSign);   // +-0 / normal
-    return hw_div(x, y);
-  }
-  const uint64_t ma = (a & kMant) | kHid, mb = (b & kMant) | kHid;
-  const uint32_t k = ma < mb ? 1u : 0u;                    // Q = ma*2^k/mb in [1, 2)
-  const int eq = (int)ea - (int)eb + 1023 - (int)k;
-  if (eq < 1 || eq > 2046) return hw_div(x, y);
-  const uint64_t B = mb << 10;                             // my in Q2.62, [1, 2)
-  const float fb = ffrom((127u << 23) | (uint32_t)((mb & kMant) >> 29));
-  int64_t z = (int64_t)q62_from_seed(rcp_seed(fb));         // ~1/my
+// the hardware division.  The refined reciprocal depends on y only, so
+// several quotients by one divisor share it (Divisor).
+struct Divisor {
+  double y;
+  uint64_t mb;    // significand of y, [2^52, 2^53)
+  int64_t z;      // ~1/my in Q2.62
+  uint32_t eb;    // biased exponent of y
+  bool normal;
+};
+
+__host__ __device__ __forceinline__ Divisor divisor(double y) {
+  Divisor v;
+  v.y = y;
+  const uint64_t b = bits(y);
+  v.eb = (uint32_t)(b >> 52) & 0x7FFu;
+  v.normal = v.eb - 1u < 2046u;
+  v.mb = (b & kMant) | kHid;
+  const uint64_t B = v.mb << 10;                           // my in Q2.62, [1, 2)
+  const float fb = ffrom((127u << 23) | (uint32_t)((v.mb & kMant) >> 29));
+  int64_t z = (int64_t)q62_from_seed(rcp_seed(fb));
 #pragma unroll
   for (int it = 0; it < 2; it++) {
     const int64_t t = ((int64_t)1 << 62) - (int64_t)(mulhi(B, (uint64_t)z) << 2);   // 1 - my*z
     z += (int64_t)((uint64_t)smulhi(z, t) << 2);
   }
+  v.z = z;
+  return v;
+}
+
+__host__ __device__ __forceinline__ double div_by(double x, const Divisor& v) {
+  const uint64_t a = bits(x);
+  const uint32_t ea = (uint32_t)(a >> 52) & 0x7FFu;
+  if (ea - 1u >= 2046u || !v.normal) {
+    if ((a << 1) == 0 && v.normal) return from_bits((a ^ bits(v.y)) & kSign);   // +-0 / normal
+    return hw_div(x, v.y);
+  }
+  const uint64_t ma = (a & kMant) | kHid, mb = v.mb;
+  const uint32_t k = ma < mb ? 1u : 0u;                    // Q = ma*2^k/mb in [1, 2)
+  const int eq = (int)ea - (int)v.eb + 1023 - (int)k;
+  if (eq < 1 || eq > 2046) return hw_div(x, v.y);
   const uint64_t Aq = (ma << 10) << k;                     // mx*2^k in Q2.62 (below 4)
-  const uint64_t q = mulhi(Aq, (uint64_t)z) << 2;          // ~Q in Q2.62
+  const uint64_t q = mulhi(Aq, (uint64_t)v.z) << 2;        // ~Q in Q2.62
   uint64_t S = (q + (1u << 9)) >> 10;                      // ~Q * 2^52
   // R = ma*2^(52+k) - S*mb, exact in 64 bits while S is within a few units
   int64_t R = (int64_t)(((ma << 52) << k) - S * mb);
@@ -330,9 +350,35 @@ __host__ __device__ __forceinline__ double div_rn(double x, double y) {
     if (2 * R > hb || (2 * R == hb && (S & 1u))) { R -= hb; S += 1; }
     else if (2 * R < -hb || (2 * R == -hb && (S & 1u))) { R += hb; S -= 1; }
   }
-  const uint64_t sg = (a ^ b) & kSign;
+  const uint64_t sg = (a ^ bits(v.y)) & kSign;
   return from_bits(sg | ((((uint64_t)(eq - 1)) << 52) + S));
 }
+
+__host__ __device__ __forceinline__ double div_rn(double x, double y) { return div_by(x, divisor(y)); }
+
+// IEEE comparisons on the integer pipes (false with a NaN; +0 == -0): the
+// bit patterns, with the magnitude bits of negatives flipped, order like the
+// values.
+__host__ __device__ __forceinline__ int64_t order_key(uint64_t u) {
+  return (int64_t)(u ^ ((uint64_t)((int64_t)u >> 63) >> 1));
+}
+__host__ __device__ __forceinline__ bool unordered_or_zeros(uint64_t a, uint64_t b) {
+  const uint64_t aa = a << 1, bb = b << 1;     // magnitudes, shifted out sign
+  return aa > 0xFFE0000000000000ull || bb > 0xFFE0000000000000ull || (aa | bb) == 0;
+}
+__host__ __device__ __forceinline__ bool gt(double x, double y) {
+  const uint64_t a = bits(x), b = bits(y);
+  return !unordered_or_zeros(a, b) && order_key(a) > order_key(b);
+}
+__host__ __device__ __forceinline__ bool lt(double x, double y) { return gt(y, x); }
+__host__ __device__ __forceinline__ bool ge(double x, double y) {
+  const uint64_t a = bits(x), b = bits(y);
+  const uint64_t aa = a << 1, bb = b << 1;
+  if (aa > 0xFFE0000000000000ull || bb > 0xFFE0000000000000ull) return false;   // NaN
+  if ((aa | bb) == 0) return true;                                                // +-0 >= +-0
+  return order_key(a) >= order_key(b);
+}
+__host__ __device__ __forceinline__ bool le(double x, double y) { return ge(y, x); }
 
 // floor(q) as an int when 0 <= floor(q) < n (q = -0 counts as 0), else -1;
 // NaN and infinities give -1.  Integer work only.

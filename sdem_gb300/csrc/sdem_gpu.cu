@@ -722,7 +722,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d) {
     const r3 sv = sdem::sub3(sdem::xyz(Pj), sdem::xyz(Pi));
     const double normv = sdem::norm3(sv);
     const double ovrlp = (Pi.w + Pj.w) - normv;
-    r3 Norm_v = (normv > 1.0000E-10) ? sdem::div3(sv, normv) : sdem::mk3(0.0, 0.0, 0.0);
+    r3 Norm_v = fpi::gt(normv, 1.0000E-10) ? sdem::div3(sv, normv) : sdem::mk3(0.0, 0.0, 0.0);
     r3 S, M, Mr;
     sdem::force_law(d.law, P, sdem::xyz(Vi), sdem::xyz(Vj), sdem::xyz(Wi), sdem::xyz(Wj), Pi.w, Pj.w, Norm_v, ovrlp,
                     hist, S, M, Mr);
@@ -794,10 +794,10 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   auto push = [&](int c, bool p_lo) { list[nl++] = (c << 1) | (p_lo ? 1 : 0); };
   auto push_in = [&](unsigned key) {
     const int c = d.row_off[key >> 6] + (int)(key & 63u);
-    push(c, d.c_S[c].w == 0.0);   // p is the row's partner: particle i iff the target is not
+    push(c, (__double_as_longlong(d.c_S[c].w) << 1) == 0);   // p is the row's partner: particle i iff the target is not
   };
   auto push_own = [&]() {
-    for (int j = 0; j < own_n; j++) push(own_a + j, d.c_S[own_a + j].w != 0.0);
+    for (int j = 0; j < own_n; j++) push(own_a + j, (__double_as_longlong(d.c_S[own_a + j].w) << 1) != 0);
   };
   if (nin <= 8) {
     unsigned u[8];
@@ -961,22 +961,23 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
   if (d.per[0] || d.per[1] || d.per[2]) {
     dbl4 Q = d.posr[p];
     if (d.per[1]) {
-      if (Q.y >= d.dmax.y) Q.y = Q.y - d.Lbox.y;
-      else if (Q.y < d.dmin.y) Q.y = Q.y + d.Lbox.y;
+      if (fpi::ge(Q.y, d.dmax.y)) Q.y = Q.y - d.Lbox.y;
+      else if (fpi::lt(Q.y, d.dmin.y)) Q.y = Q.y + d.Lbox.y;
     }
     if (d.per[0]) {
-      if (Q.x >= d.dmax.x) Q.x = Q.x - d.Lbox.x;
-      if (Q.x < d.dmin.x) Q.x = Q.x + d.Lbox.x;
+      if (fpi::ge(Q.x, d.dmax.x)) Q.x = Q.x - d.Lbox.x;
+      if (fpi::lt(Q.x, d.dmin.x)) Q.x = Q.x + d.Lbox.x;
     }
     if (d.per[2]) {
-      if (Q.z >= d.dmax.z) Q.z = Q.z - d.Lbox.z;
-      if (Q.z < d.dmin.z) Q.z = Q.z + d.Lbox.z;
+      if (fpi::ge(Q.z, d.dmax.z)) Q.z = Q.z - d.Lbox.z;
+      if (fpi::lt(Q.z, d.dmin.z)) Q.z = Q.z + d.Lbox.z;
     }
     d.posr[p] = Q;
     x = sdem::xyz(Q);
   }
-  if ((!d.per[1] && (x.y >= d.dmax.y || x.y < d.dmin.y)) || (!d.per[0] && (x.x >= d.dmax.x || x.x < d.dmin.x)) ||
-      (!d.per[2] && (x.z >= d.dmax.z || x.z < d.dmin.z))) {
+  if ((!d.per[1] && (fpi::ge(x.y, d.dmax.y) || fpi::lt(x.y, d.dmin.y))) ||
+      (!d.per[0] && (fpi::ge(x.x, d.dmax.x) || fpi::lt(x.x, d.dmin.x))) ||
+      (!d.per[2] && (fpi::ge(x.z, d.dmax.z) || fpi::lt(x.z, d.dmin.z)))) {
     int k2 = atomicAdd(d.out_cnt, 1);
     if (k2 < kOutCap) d.out_list[k2] = p;
     else raise(d, SDEM_E_CAPACITY, p);
@@ -1140,7 +1141,8 @@ __global__ void k_selftest_fp64(long long n, unsigned long long seed, unsigned l
     bool ok = same_bits(fpi::sqrt_rn(x), __dsqrt_rn(x)) && same_bits(fpi::div_rn(x, y), __ddiv_rn(x, y)) &&
               same_bits(fpi::div_rn(y, x), __ddiv_rn(y, x)) && same_bits(fpi::add(x, y), __dadd_rn(x, y)) &&
               same_bits(fpi::sub(x, y), __dsub_rn(x, y)) && same_bits(fpi::mul(x, y), __dmul_rn(x, y)) &&
-              same_bits(fpi::mul_neg_half(x), __dmul_rn(x, -0.5));
+              same_bits(fpi::mul_neg_half(x), __dmul_rn(x, -0.5)) && fpi::gt(x, y) == (x > y) &&
+              fpi::ge(x, y) == (x >= y) && fpi::lt(x, y) == (x < y) && fpi::le(x, y) == (x <= y);
     const double q = __ddiv_rn(x, y), f = floor(q);
     const int want = (f >= 0.0 && f < 4000.0) ? (int)f : -1;
     ok = ok && fpi::floor_in_range(q, 4000) == want;

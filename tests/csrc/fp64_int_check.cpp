@@ -58,6 +58,23 @@ static void check(double x, double y) {
       }
     }
   }
+  {
+    const bool cg[4] = {fpi::gt(x, y), fpi::lt(x, y), fpi::ge(x, y), fpi::le(x, y)};
+    const bool cw[4] = {x > y, x < y, x >= y, x <= y};
+    for (int j = 0; j < 4; j++) {
+      checked++;
+      if (cg[j] != cw[j]) {
+        if (bad < 20) printf("MISMATCH compare %d x=%a y=%a got=%d want=%d\n", j, x, y, (int)cg[j], (int)cw[j]);
+        bad++;
+      }
+    }
+    const fpi::Divisor v = fpi::divisor(y);
+    checked++;
+    if (!same(fpi::div_by(x, v), x / y)) {
+      if (bad < 20) printf("MISMATCH div_by x=%a y=%a\n", x, y);
+      bad++;
+    }
+  }
   for (int k = 0; k < 8; k++) {
     checked++;
     if (!same(r[k], e[k])) {
@@ -99,6 +116,14 @@ int main(int argc, char** argv) {
       const double xx = ((double)(int64_t)(g() % 4000) - 100.0) * cell + ((double)(g() % 2001) - 1000.0) * 1e-19;
       check(xx, cell);
       check(-0.0, cell);
+    }
+    // equal values, signed zeros and neighbours for the comparisons
+    {
+      const double x = D(u64());
+      check(x, x);
+      check(x, D(B(x) + 1));
+      check(0.0, -0.0);
+      check(-0.0, D(g() & 1 ? 0x8000000000000001ull : 1ull));
     }
     // 1) uniformly random bit patterns (every exponent, specials included)
     check(D(u64()), D(u64()));
