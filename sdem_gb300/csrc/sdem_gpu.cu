@@ -18,13 +18,16 @@
 //                                      order) and an entry (target, slot) to the partner's in-list
 //   k_wall_detect                      FindContactsPW's detection (:298-319) over the near-wall mask,
 //                                      and the contact count of every particle for the gather order
-//   scan, k_gid_index                  row offsets (CSR), each contact's row, an empty owner table
+//   scan, k_row_fill                   row offsets (CSR) and each contact's row
 //   k_force                            Find_insert history lookup + ContactForce_PP / _PPG
 //                                      (Prtcl_CL_and_CF.f90:142-198, 256-296, 732-798): one thread per
 //                                      contact, full warps of FP64 work
 //   k_wall_force                       ContactForce_PW (:832-856), one thread per wall contact
-//   k_degree_scatter                   particles grouped by contact count (the gather order; the
-//                                      bucket starts come from k_gid_index)
+//   k_degree_scatter                   particles grouped by contact count (the gather order)
+//
+// Search, row offsets, row fill and forces run in chunks of target sort
+// positions on two streams, so that the search of one chunk (integer and
+// memory work) overlaps the force kernel of the one before (FP64 work).
 //   k_gather                           per particle, sums its contact records in the reference's scatter
 //                                      order (a deterministic gather), then its wall contacts in
 //                                      near-list order
@@ -64,13 +67,14 @@ constexpr int kMaxWalls = 64;     // near-wall mask is 64 bits
 constexpr int kOutCap = 4096;     // out-of-domain deletions per step
 constexpr int kScanTile = 4096;   // elements per scan block (1024 threads x 4)
 constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact records
+constexpr int kChunks = 2;        // search/force pipeline chunks per step
 constexpr int kImgFlag = 1 << 30; // c_ogid bit: a pair with a periodic image (ids < 2^30)
 
 // Phases of one step, for the optional per-phase timing (sdem_profile_*).
-enum Phase { PH_WALL, PH_BIN, PH_SCAN_CELLS, PH_SCATTER, PH_CELLORDER, PH_SEARCH, PH_SCAN_ROWS, PH_GID_INDEX,
+enum Phase { PH_WALL, PH_BIN, PH_SCAN_CELLS, PH_SCATTER, PH_CELLORDER, PH_SEARCH, PH_SCAN_ROWS, PH_ROW_FILL,
              PH_FORCE, PH_WALL_FORCE, PH_GATHER, PH_DELETE, PH_END, kPhases };
 const char* const kPhaseNames[kPhases] = {"wall_refresh", "bin", "scan_cells", "scatter", "cellorder", "search",
-                                          "scan_rows", "gid_index", "force", "wall_force", "gather_integrate",
+                                          "scan_rows", "row_fill", "force", "wall_force", "gather_integrate",
                                           "delete", "step_end"};
 
 // ---------------------------------------------------------------------------
@@ -144,7 +148,7 @@ struct Dev {
   int* wl_cnt;
   // gather order: particles bucketed by their number of contact records, so a
   // warp's summation loops run the same trip count
-  int *deg_cnt, *deg_start, *deg_of, *deg_rank, *gorder;
+  int *deg_cnt, *deg_of, *deg_rank, *gorder;
   const int *wh_cnt_prev, *wh_wall_prev;
   const dbl4* wh_hist_prev;
   // status and scalars
@@ -225,11 +229,12 @@ __global__ void k_scan_blocks(int* bsum, int nb) {
   }
 }
 
+// out[i] = *offset + sum of in[0..i), out[n] = the total (offset may be null)
 __global__ void k_scan_apply(const int* __restrict__ in, long long n, const int* __restrict__ bsum,
-                             int* __restrict__ out) {
+                             int* __restrict__ out, const int* __restrict__ offset) {
   __shared__ int sh[33];
   long long base = (long long)blockIdx.x * kScanTile;
-  int carry = bsum[blockIdx.x];
+  int carry = bsum[blockIdx.x] + (offset ? *offset : 0);
   for (int k = 0; k < 4; k++) {
     long long i = base + (long long)k * 1024 + threadIdx.x;
     int v = (i < n) ? in[i] : 0;
@@ -319,6 +324,7 @@ __device__ __forceinline__ int ghost_count(const Dev& d, int pass, const dbl4& P
 __global__ void k_ghost_begin(Dev d) {
   *d.ng = 0;
   *d.nt = *d.n;
+  for (int b = 0; b < kDegBuckets; b++) d.deg_cnt[b] = 0;   // gather-order buckets of this step
 }
 
 __global__ void k_ghost_flag(Dev d, int pass) {
@@ -405,6 +411,9 @@ __global__ void k_bin(Dev d) {
 
 __global__ void k_scatter(Dev d) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
+  // this step's owner table starts empty (images never own; the count-only
+  // entry point has no table)
+  if (d.own_cnt && p < *d.n) d.own_cnt[d.gid[p]] = 0;
   if (p >= *d.nt) return;
   int key = d.cell_of[p];
   if (key < 0) return;
@@ -437,12 +446,12 @@ __global__ void k_cellorder(Dev d) {
 // position s).  Visit order per target: the tail of its own cell, then
 // (ix,iy,iz-1), (ix-1,iy,iz-1..iz+1), then row iy-1: columns ix-1..ix+1,
 // cells iz-1..iz+1 -- the order of Prtcl_NBS_Munjiza.f90:409-468.
-__global__ void __launch_bounds__(kThreads) k_search(Dev d) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_end) {
+  int s = s_begin + blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = *d.nt;
   const int nloc = *d.n;
   unsigned long long cand = 0;
-  if (s < d.nall_launch) {
+  if (s < s_end) {
     if (s >= nt) {
       d.row_cnt[s] = 0;
     } else {
@@ -601,10 +610,28 @@ __global__ void __launch_bounds__(kThreads) k_wall_detect(Dev d) {
   if ((threadIdx.x & 31) == 0 && nwc) atomicAdd(&d.counters[1], (unsigned long long)nwc);
 }
 
+// Gather order: bucket starts (highest degree first; every block scans the
+// 64 bucket counts itself), then each particle to its bucket slot.
 __global__ void k_degree_scatter(Dev d) {
+  static_assert(kDegBuckets == 64, "two buckets per lane of one warp");
+  __shared__ int start[kDegBuckets];
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
+    const int b0 = kDegBuckets - 1 - 2 * l, b1 = b0 - 1;
+    const int c0 = d.deg_cnt[b0], c1 = d.deg_cnt[b1];
+    const int v = c0 + c1;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (l >= o) incl += t;
+    }
+    start[b0] = incl - v;
+    start[b1] = incl - v + c0;
+  }
+  __syncthreads();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= *d.n) return;
-  d.gorder[d.deg_start[d.deg_of[p]] + d.deg_rank[p]] = p;
+  d.gorder[start[d.deg_of[p]] + d.deg_rank[p]] = p;
 }
 
 // One thread per wall contact: Find_insert on the particle's bucket (key = wall)
@@ -638,49 +665,29 @@ __global__ void __launch_bounds__(kThreads) k_wall_force(Dev d) {
   }
 }
 
-// Empties this step's owner table for every local id (images never own), and
-// writes each contact's row (its target's sort position), so that the
-// one-thread-per-contact force kernel reads its row instead of searching the
-// row offsets.
-__global__ void k_gid_index(Dev d) {
-  static_assert(kDegBuckets == 64, "two buckets per lane of one warp");
-  if (blockIdx.x == 0 && threadIdx.x < 32) {
-    // start of every degree bucket of the gather order, highest degree first
-    // (k_wall_detect has counted them); the counts are cleared for the next step
-    const int l = threadIdx.x;
-    const int b0 = kDegBuckets - 1 - 2 * l, b1 = b0 - 1;
-    const int c0 = d.deg_cnt[b0], c1 = d.deg_cnt[b1];
-    const int v = c0 + c1;
-    int incl = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (l >= o) incl += t;
-    }
-    d.deg_start[b0] = incl - v;
-    d.deg_start[b1] = incl - v + c0;
-    d.deg_cnt[b0] = 0;
-    d.deg_cnt[b1] = 0;
-  }
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < *d.n) d.own_cnt[d.gid[p]] = 0;
-  if (p < *d.nt) {
-    const int a = d.row_off[p], k = d.row_cnt[p];
-    for (int j = 0; j < k; j++)
-      if (a + j < d.ccap) d.c_row[a + j] = p;
-  }
+// Each contact's row (its target's sort position) for the rows [s_begin, s_end),
+// so that the one-thread-per-contact force kernel reads its row instead of
+// searching the row offsets.
+__global__ void k_row_fill(Dev d, int s_begin, int s_end) {
+  const int s = s_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= s_end) return;
+  const int a = d.row_off[s], k = d.row_cnt[s];
+  for (int j = 0; j < k; j++)
+    if (a + j < d.ccap) d.c_row[a + j] = s;
 }
 
 // ---------------------------------------------------------------------------
 // One thread per contact: Find_insert's history lookup + ContactForce_PP.
-__global__ void __launch_bounds__(kThreads, 3) k_force(Dev d) {
+// Contacts of the rows [s_begin, s_end).
+__global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s_end) {
   const int nloc = *d.n;
-  const int C = d.row_off[d.nall_launch];
+  const int c0 = d.row_off[s_begin], C = d.row_off[s_end];
   if (C > d.ccap) {
     if (blockIdx.x == 0 && threadIdx.x == 0) raise(d, SDEM_E_CL_FULL, C);
     return;
   }
   unsigned long long nimg = 0;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+  for (int c = c0 + blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
     const int s = d.c_row[c];
     const int slot = c - d.row_off[s];
     int m = d.sorted[s];
@@ -1367,7 +1374,10 @@ struct sdem_h {
   dbl4 *w_geo = nullptr, *w_S = nullptr, *w_M = nullptr, *w_Mr = nullptr;
   float4* spos = nullptr;
   float pf_margin = 0.f;
-  int *deg_cnt = nullptr, *deg_start = nullptr, *deg_of = nullptr, *deg_rank = nullptr, *gorder = nullptr;
+  int *deg_cnt = nullptr, *deg_of = nullptr, *deg_rank = nullptr, *gorder = nullptr;
+  // second stream and events of the chunked search/force pipeline
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chunk[kChunks] = {};
   int cur = 0;  // buffer written by the next step
   // device scalars
   int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
@@ -1529,7 +1539,6 @@ Dev make_dev(sdem_h* h) {
   d.sortpos = h->sortpos;
   d.spos = h->spos;
   d.deg_cnt = h->deg_cnt;
-  d.deg_start = h->deg_start;
   d.deg_of = h->deg_of;
   d.deg_rank = h->deg_rank;
   d.gorder = h->gorder;
@@ -1585,11 +1594,11 @@ Dev make_dev(sdem_h* h) {
 
 int grid_for(long long n) { return (int)std::max<long long>(1, (n + kThreads - 1) / kThreads); }
 
-void scan(sdem_h* h, const int* in, long long n, int* out) {
+void scan(sdem_h* h, const int* in, long long n, int* out, const int* offset = nullptr) {
   int nb = (int)std::max<long long>(1, (n + kScanTile - 1) / kScanTile);
   k_scan_reduce<<<nb, 1024, 0, h->stream>>>(in, n, h->scan_tmp);
   k_scan_blocks<<<1, 1024, 0, h->stream>>>(h->scan_tmp, nb);
-  k_scan_apply<<<nb, 1024, 0, h->stream>>>(in, n, h->scan_tmp, out);
+  k_scan_apply<<<nb, 1024, 0, h->stream>>>(in, n, h->scan_tmp, out, offset);
 }
 
 int enqueue_step(sdem_h* h) {
@@ -1634,16 +1643,45 @@ int enqueue_step(sdem_h* h) {
   mark(PH_CELLORDER);
   k_cellorder<<<grid_for(na), kThreads, 0, st>>>(d);
   mark(PH_SEARCH);
-  k_search<<<grid_for(na), kThreads, 0, st>>>(d);
-  k_wall_detect<<<grid_for(n), kThreads, 0, st>>>(d);
-  mark(PH_SCAN_ROWS);
-  scan(h, h->row_cnt, na, h->row_off);
-  mark(PH_GID_INDEX);
-  k_gid_index<<<grid_for(na), kThreads, 0, st>>>(d);
-  mark(PH_FORCE);
-  k_force<<<h->num_sms * 8, kThreads, 0, st>>>(d);
-  mark(PH_WALL_FORCE);
-  k_wall_force<<<std::max(1, h->num_sms * 2), kThreads, 0, st>>>(d);
+  // Chunked pipeline: the searches of all chunks, then wall detection and wall
+  // forces, run on the second stream; each chunk's row offsets (continuing
+  // the previous chunk's total), contact rows and forces run on the main
+  // stream as soon as its search is done.  Profiling runs one chunk on one
+  // stream, so that every phase has its own events.
+  const int nchunk = ev ? 1 : kChunks;
+  cudaStream_t s2 = ev ? st : h->stream2;
+  auto cut = [&](int k) { return (int)((long long)na * k / nchunk); };
+  if (s2 != st) {
+    cudaEventRecord(h->ev_fork, st);
+    cudaStreamWaitEvent(s2, h->ev_fork, 0);
+  }
+  for (int k = 0; k < nchunk; k++) {
+    const int a = cut(k), b = cut(k + 1);
+    k_search<<<grid_for(std::max(b - a, 1)), kThreads, 0, s2>>>(d, a, b);
+    if (s2 != st) cudaEventRecord(h->ev_chunk[k], s2);
+  }
+  k_wall_detect<<<grid_for(n), kThreads, 0, s2>>>(d);
+  if (s2 == st) {
+    mark(PH_SCAN_ROWS);
+    scan(h, h->row_cnt, na, h->row_off);
+    mark(PH_ROW_FILL);
+    k_row_fill<<<grid_for(na), kThreads, 0, st>>>(d, 0, na);
+    mark(PH_FORCE);
+    k_force<<<h->num_sms * 8, kThreads, 0, st>>>(d, 0, na);
+    mark(PH_WALL_FORCE);
+    k_wall_force<<<std::max(1, h->num_sms * 2), kThreads, 0, st>>>(d);
+  } else {
+    k_wall_force<<<std::max(1, h->num_sms * 2), kThreads, 0, s2>>>(d);
+    cudaEventRecord(h->ev_join, s2);
+    for (int k = 0; k < nchunk; k++) {
+      const int a = cut(k), b = cut(k + 1);
+      cudaStreamWaitEvent(st, h->ev_chunk[k], 0);
+      scan(h, h->row_cnt + a, b - a, h->row_off + a, k ? h->row_off + a : nullptr);
+      k_row_fill<<<grid_for(std::max(b - a, 1)), kThreads, 0, st>>>(d, a, b);
+      k_force<<<h->num_sms * 3, kThreads, 0, st>>>(d, a, b);
+    }
+    cudaStreamWaitEvent(st, h->ev_join, 0);
+  }
   mark(PH_GATHER);
   k_degree_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
   k_gather<true><<<grid_for(n), kThreads, 0, st>>>(d);
@@ -1654,7 +1692,10 @@ int enqueue_step(sdem_h* h) {
   mark(PH_END);
   k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS);
   mark(kPhases);
-  L += 1 + 3 + 1 + 1 + 2 + 3 + 1 + 1 + 1 + 3 + 2 + 1;
+  // bin, scan, scatter, cellorder, wall detect, wall force, degree scatter,
+  // gather, integrate, delete (2), step end; per chunk search, scan (3),
+  // row fill, force
+  L += 1 + 3 + 1 + 1 + 1 + 1 + 3 + 2 + 1 + 6 * nchunk;
   h->launches += L;
   if (ev) h->prof_steps++;
   h->cur = 1 - h->cur;
@@ -1762,6 +1803,10 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   if (cudaGetDevice(&h->dev) != cudaSuccess) return set_err(h, SDEM_E_CUDA, "no CUDA device");
   CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->dev));
   CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+  for (int k = 0; k < kChunks; k++) CK(cudaEventCreateWithFlags(&h->ev_chunk[k], cudaEventDisableTiming));
   int N = c.n_capacity;
   // Periodic images need room beside the particles in the search arrays.  A
   // periodic side longer than two search cells gives every point at most one
@@ -1794,7 +1839,6 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->sortpos, NA);
   rc |= dalloc(h, &h->spos, NA);
   rc |= dalloc(h, &h->deg_cnt, kDegBuckets);
-  rc |= dalloc(h, &h->deg_start, kDegBuckets);
   rc |= dalloc(h, &h->deg_of, N);
   rc |= dalloc(h, &h->deg_rank, N);
   rc |= dalloc(h, &h->gorder, N);
@@ -2502,7 +2546,7 @@ int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, c
     const int nb = (int)std::max<long long>(1, (ncell + kScanTile - 1) / kScanTile);
     k_scan_reduce<<<nb, 1024, 0, st>>>(S->cell_cnt, ncell, S->bsum);
     k_scan_blocks<<<1, 1024, 0, st>>>(S->bsum, nb);
-    k_scan_apply<<<nb, 1024, 0, st>>>(S->cell_cnt, ncell, S->bsum, S->cell_start);
+    k_scan_apply<<<nb, 1024, 0, st>>>(S->cell_cnt, ncell, S->bsum, S->cell_start, nullptr);
   }
   k_scatter<<<g, kThreads, 0, st>>>(d);
   k_cellorder<<<g, kThreads, 0, st>>>(d);
@@ -2549,6 +2593,12 @@ void sdem_destroy(sdem_h* h) {
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
   if (h->stage) cudaFree(h->stage);
+  if (h->stream2) cudaStreamSynchronize(h->stream2);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  for (int k = 0; k < kChunks; k++)
+    if (h->ev_chunk[k]) cudaEventDestroy(h->ev_chunk[k]);
+  if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
