@@ -220,8 +220,7 @@ int sdem_profile_end(sdem_h* h, int cap, double* ms, int* nsteps);
 /* Name of phase i ("" outside the range). */
 const char* sdem_profile_phase_name(int i);
 /* Runs the library's integer-pipe binary64 arithmetic (sqrt, division,
- * addition, multiplication, exact x*(-1/2), comparisons, floor into a grid
- * range) against
+ * exact x*(-1/2), comparisons, floor into a grid range) against
  * the hardware instructions on n generated operand pairs on the current
  * device; *mismatches receives the number of pairs whose results differ in
  * any bit (0 expected). */

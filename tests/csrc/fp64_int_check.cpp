@@ -1,5 +1,6 @@
 // CPU check of sdem_gb300/csrc/fp64_int.cuh: the integer-pipe binary64
-// addition and multiplication against the host's IEEE arithmetic.
+// sqrt, division, comparisons, -x/2 and grid floor against the host's IEEE
+// arithmetic.
 // Usage: fp64_int_check <seed> <pairs per family>; prints "ok <n>" or the
 // first mismatches and exits 1.
 #include <cmath>
@@ -39,10 +40,9 @@ static bool same(double a, double b) {
 
 static long bad = 0, checked = 0;
 static void check(double x, double y) {
-  const double r[8] = {fpi::add(x, y), fpi::sub(x, y), fpi::mul(x, y), fpi::add(y, x), fpi::mul_neg_half(x),
-                       fpi::sqrt_rn(x), fpi::div_rn(x, y), fpi::div_rn(y, x)};
-  const double e[8] = {x + y, x - y, x * y, y + x, x * -0.5, std::sqrt(x), x / y, y / x};
-  const char* nm[8] = {"add", "sub", "mul", "add(y,x)", "mul_neg_half", "sqrt", "div", "div(y,x)"};
+  const double r[4] = {fpi::mul_neg_half(x), fpi::sqrt_rn(x), fpi::div_rn(x, y), fpi::div_rn(y, x)};
+  const double e[4] = {x * -0.5, std::sqrt(x), x / y, y / x};
+  const char* nm[4] = {"mul_neg_half", "sqrt", "div", "div(y,x)"};
   {
     // floor_in_range against floor() and a range test, for a few grid sizes
     const int ns[3] = {1, 37, 1000000};
@@ -75,7 +75,7 @@ static void check(double x, double y) {
       bad++;
     }
   }
-  for (int k = 0; k < 8; k++) {
+  for (int k = 0; k < 4; k++) {
     checked++;
     if (!same(r[k], e[k])) {
       if (bad < 20)

@@ -1,7 +1,7 @@
 """On the GPU: the integer-pipe binary64 arithmetic the kernels use for
-sqrt, division, the binning's subtraction and floor and the AB2 -1/2 factor
-gives the same bits as the hardware instructions (__dsqrt_rn, __ddiv_rn,
-__dadd_rn, __dmul_rn), with the device's own rsqrt/rcp approximation seeds."""
+sqrt, division, comparisons, the binning's floor and the AB2 -1/2 factor gives
+the same bits as the hardware instructions (__dsqrt_rn, __ddiv_rn, __dmul_rn,
+the FP64 comparisons), with the device's own rsqrt/rcp approximation seeds."""
 import pytest
 
 from sdem_gb300.capi import selftest_fp64
