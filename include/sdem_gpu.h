@@ -205,6 +205,32 @@ int sdem_download_forces(sdem_h* h, double* F, double* T);
 /* Counters of the last step, SDEM_CNT_SIZE ints (see SDEM_CNT_*). */
 int sdem_counters(sdem_h* h, int* out);
 
+/* ---- asynchronous output for the dump / restart steps ---------------------
+ * Replaces the synchronous downloads before dump_visu and Write_Restart
+ * (Prtcl_DEMSystem.f90:254,261; formats of Prtcl_IOAndVisu.f90:849-1031,
+ * 1193-1267 unchanged).  sdem_snapshot_begin freezes, on the device, the
+ * state after every step enqueued so far (a device-to-device copy of a few
+ * hundred MB, well under a millisecond) and starts its download on a separate
+ * copy stream; sdem_step_async calls made afterwards run while the copy
+ * travels.  The host arrays take the layouts of sdem_download_particles
+ * (n_capacity rows suffice) plus F and T (3 doubles per particle); any may be
+ * NULL.  Page-locked host arrays let the copy run at full speed; others are
+ * staged by the driver.  They must stay valid and untouched until
+ * sdem_snapshot_end returns.  want_contacts != 0 also freezes the contact
+ * list (history included), read after sdem_snapshot_end with
+ * sdem_snapshot_contacts in the listing of sdem_download_contacts.  A new
+ * sdem_snapshot_begin, sdem_download_contacts or sdem_check_restart_limit
+ * first completes a snapshot still in flight and then replaces it. */
+int sdem_snapshot_begin(sdem_h* h, int* id, int* ptype, int* usrmark, double* posR, double* linVel,
+                        double* linAcc, double* theta, double* rotVel, double* rotAcc, double* F, double* T,
+                        int want_contacts);
+/* Waits for the snapshot's download; *n_out = particles in it. */
+int sdem_snapshot_end(sdem_h* h, int* n_out);
+/* Contact records of the last finished snapshot taken with want_contacts
+ * (arguments as sdem_download_contacts). */
+int sdem_snapshot_contacts(sdem_h* h, int cap, int* nc, int* owner_idx, int* partner_id, double* tandelta,
+                           double* velrel);
+
 /* ---- diagnostics (no counterpart in the reference) ---------------------- */
 /* Sums since the last upload: out[0] particle-particle contacts over all
  * steps, out[1] wall contacts, out[2] steps (averages over a timed window). */

@@ -28,7 +28,7 @@ EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls
             "sdem_download_particles", "sdem_download_contacts", "sdem_check_restart_limit",
             "sdem_download_forces", "sdem_counters", "sdem_counter_sums", "sdem_launch_count", "sdem_profile_begin",
             "sdem_profile_end", "sdem_profile_phase_name", "sdem_count_contacts_noalloc", "sdem_selftest_fp64",
-            "sdem_last_error", "sdem_destroy")
+            "sdem_snapshot_begin", "sdem_snapshot_end", "sdem_snapshot_contacts", "sdem_last_error", "sdem_destroy")
 
 
 def selftest_fp64(n: int, seed: int = 1) -> int:
@@ -124,6 +124,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_profile_phase_name.restype = C.c_char_p
     lib.sdem_count_contacts_noalloc.argtypes = [C.POINTER(SdemCfg), C.c_double, C.c_int, P, P, P]
     lib.sdem_selftest_fp64.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
+    lib.sdem_snapshot_begin.argtypes = [P, ip, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp, C.c_int]
+    lib.sdem_snapshot_end.argtypes = [P, ip]
+    lib.sdem_snapshot_contacts.argtypes = [P, C.c_int, ip, ip, ip, dp, dp]
     lib.sdem_last_error.argtypes = [P]
     lib.sdem_last_error.restype = C.c_char_p
     lib.sdem_destroy.argtypes = [P]
@@ -256,14 +259,53 @@ class DEMSystem:
     def contacts(self):
         nc = C.c_int()
         self._check(self.lib.sdem_download_contacts(self.h, 0, C.byref(nc), None, None, None, None))
-        m = nc.value
+        # the records are now the library's finished snapshot: read them there
+        return self._snapshot_records(nc.value)
+
+    def _snapshot_records(self, m: int):
+        nc = C.c_int()
         o = np.zeros(max(m, 1), np.int32)
         q = np.zeros(max(m, 1), np.int32)
         t = np.zeros((max(m, 1), 3))
         v = np.zeros(max(m, 1))
-        self._check(self.lib.sdem_download_contacts(self.h, max(m, 1), C.byref(nc), iptr(o), iptr(q), dptr(t),
+        self._check(self.lib.sdem_snapshot_contacts(self.h, max(m, 1), C.byref(nc), iptr(o), iptr(q), dptr(t),
                                                     dptr(v)))
+        m = nc.value
         return o[:m], q[:m], t[:m], v[:m]
+
+    def snapshot_begin(self, out: Particles, F: Optional[np.ndarray] = None, T: Optional[np.ndarray] = None,
+                       contacts: bool = False) -> None:
+        """Freezes the state after the steps enqueued so far and starts its
+        download into `out` (n_capacity rows, C-contiguous; page-locked memory
+        lets the copy run at full speed) and F, T ((n_capacity, 3) each, or
+        None).  Steps issued before snapshot_end overlap the copy."""
+        cap = self.cfg.n_capacity
+        for a in (out.id, out.posR, out.linVel, out.rotVel) + tuple(x for x in (F, T) if x is not None):
+            if a.shape[0] < cap or not a.flags.c_contiguous:
+                raise ValueError("snapshot_begin: arrays must be C-contiguous with n_capacity rows")
+        self._snap = (out, F, T)
+        self._check(self.lib.sdem_snapshot_begin(self.h, iptr(out.id), iptr(out.ptype), iptr(out.usrmark),
+                                                 dptr(out.posR), dptr(out.linVel), dptr(out.linAcc),
+                                                 dptr(out.theta), dptr(out.rotVel), dptr(out.rotAcc),
+                                                 dptr(F) if F is not None else None,
+                                                 dptr(T) if T is not None else None, 1 if contacts else 0))
+
+    def snapshot_end(self):
+        """Waits for the snapshot; returns (Particles views of its n rows, F[:n], T[:n])."""
+        n = C.c_int()
+        self._check(self.lib.sdem_snapshot_end(self.h, C.byref(n)))
+        out, F, T = self._snap
+        self._snap = None
+        k = n.value
+        p = Particles(out.id[:k], out.ptype[:k], out.usrmark[:k], out.posR[:k], out.linVel[:k], out.linAcc[:k],
+                      out.theta[:k], out.rotVel[:k], out.rotAcc[:k])
+        return p, (F[:k] if F is not None else None), (T[:k] if T is not None else None)
+
+    def snapshot_contacts(self):
+        """Contact records of the last finished snapshot taken with contacts=True."""
+        nc = C.c_int()
+        self._check(self.lib.sdem_snapshot_contacts(self.h, 0, C.byref(nc), None, None, None, None))
+        return self._snapshot_records(nc.value)
 
     def counter_sums(self) -> dict:
         out = (C.c_longlong * 3)()

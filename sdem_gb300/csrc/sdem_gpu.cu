@@ -1158,6 +1158,69 @@ __global__ void k_selftest_fp64(long long n, unsigned long long seed, unsigned l
   if (nb) atomicAdd(bad, nb);
 }
 
+// Contact snapshot (asynchronous output): the records of the last step and
+// each particle's wall records, frozen so that later steps may run while the
+// copy travels to the host.
+struct SnapContacts {
+  int* scal;        // [0] particles, [1] particle-particle records
+  int *gid, *og, *pg;
+  dbl4* hs;
+  int *wcnt, *wwall;  // per particle index: wall record count, kKw wall indices
+  dbl4* whist;        // per particle index: kKw wall records
+};
+
+__global__ void k_snap_contacts(Dev d, const int* __restrict__ pgid, const dbl4* __restrict__ hist,
+                                const int* __restrict__ whc, const int* __restrict__ whw,
+                                const dbl4* __restrict__ whh, SnapContacts out, int nall_launch) {
+  const int n = *d.n;
+  const int C = nall_launch >= 0 ? d.row_off[nall_launch] : 0;   // -1: no step since upload
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    out.scal[0] = n;
+    out.scal[1] = C;
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C || i < n; i += gridDim.x * blockDim.x) {
+    if (i < C) {
+      out.og[i] = d.c_ogid[i];
+      out.pg[i] = pgid[i];
+      out.hs[i] = hist[i];
+    }
+    if (i < n) {
+      const int g = d.gid[i];
+      out.gid[i] = g;
+      const int k = whc[g];
+      out.wcnt[i] = k;
+      for (int j = 0; j < kKw; j++) {
+        out.wwall[(size_t)i * kKw + j] = j < k ? whw[(size_t)g * kKw + j] : -1;
+        out.whist[(size_t)i * kKw + j] = j < k ? whh[(size_t)g * kKw + j] : make_dbl4(0.0, 0.0, 0.0, 0.0);
+      }
+    }
+  }
+}
+
+// Copies a contact snapshot to (mapped) host memory: exactly the records it holds.
+__global__ void k_snap_copy(SnapContacts src, SnapContacts dst) {
+  const int n = src.scal[0], C = src.scal[1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    dst.scal[0] = n;
+    dst.scal[1] = C;
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C || i < n; i += gridDim.x * blockDim.x) {
+    if (i < C) {
+      dst.og[i] = src.og[i];
+      dst.pg[i] = src.pg[i];
+      dst.hs[i] = src.hs[i];
+    }
+    if (i < n) {
+      dst.gid[i] = src.gid[i];
+      dst.wcnt[i] = src.wcnt[i];
+      for (int j = 0; j < kKw; j++) {
+        dst.wwall[(size_t)i * kKw + j] = src.wwall[(size_t)i * kKw + j];
+        dst.whist[(size_t)i * kKw + j] = src.whist[(size_t)i * kKw + j];
+      }
+    }
+  }
+}
+
 // Host layout <-> device layout of the per-particle 3-vectors: the ABI's
 // [(i*levels + k)*3 + c] doubles against one 32-byte record per particle and
 // level.  A null source writes zeros.
@@ -1386,6 +1449,18 @@ struct sdem_h {
   int* h_counters = nullptr;  // pinned
   double* stage = nullptr;    // device staging of host-layout 3-vectors (upload, download)
   size_t stage_n = 0;
+  // asynchronous output: a frozen copy of the state and contacts on the device,
+  // downloaded on the I/O stream while later steps run
+  cudaStream_t stream_io = nullptr;
+  cudaEvent_t ev_snap = nullptr, ev_snap_done = nullptr;
+  bool snap_busy = false, snap_done = false, snap_contacts = false, snap_stepped = false;
+  double* sn_state = nullptr;    // device: posR, 3-vector fields, F, T (host layouts)
+  int* sn_ints = nullptr;        // device: id, ptype, usrmark, n
+  void* sn_cdev = nullptr;       // device contact snapshot (SnapContacts layout)
+  void* sn_chost = nullptr;      // mapped pinned host copy of it
+  SnapContacts sn_dev{}, sn_host{}, sn_host_dptr{};
+  int* sn_n_host = nullptr;      // pinned
+  std::vector<UpRec> sn_up;
   bool stepped = false;
   // two consecutive steps captured as one CUDA graph (the contact buffers
   // alternate every step, so two steps return to the same buffer parity)
@@ -1804,6 +1879,9 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->dev));
   CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&h->stream_io, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&h->ev_snap, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&h->ev_snap_done, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   for (int k = 0; k < kChunks; k++) CK(cudaEventCreateWithFlags(&h->ev_chunk[k], cudaEventDisableTiming));
@@ -2297,66 +2375,186 @@ int sdem_download_forces(sdem_h* h, double* F, double* T) {
 namespace {
 struct CRec { int owner, partner; double t[3]; double vr; };
 
-int gather_contacts(sdem_h* h, std::vector<CRec>& out) {
-  int rc = sync_and_check(h);
+// Lays a contact snapshot for N particles and ccap records over `base`
+// (32-byte aligned pieces); returns the bytes it needs.
+size_t snap_layout(char* base, size_t N, size_t ccap, SnapContacts* sc) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base ? base + off : nullptr;
+    off += (bytes + 31) & ~(size_t)31;
+    return p;
+  };
+  SnapContacts t;
+  t.scal = (int*)take(2 * sizeof(int));
+  t.gid = (int*)take(N * sizeof(int));
+  t.og = (int*)take(ccap * sizeof(int));
+  t.pg = (int*)take(ccap * sizeof(int));
+  t.hs = (dbl4*)take(ccap * sizeof(dbl4));
+  t.wcnt = (int*)take(N * sizeof(int));
+  t.wwall = (int*)take(N * kKw * sizeof(int));
+  t.whist = (dbl4*)take(N * kKw * sizeof(dbl4));
+  if (sc) *sc = t;
+  return off;
+}
+
+int ensure_snapshot_buffers(sdem_h* h, bool contacts) {
+  const sdem_cfg& c = h->cfg;
+  const size_t N = (size_t)c.n_capacity;
+  if (!h->sn_state) {
+    const size_t nd = N * (4 + 3 * (size_t)(2 * c.tsize + 2 * c.rsize + 1) + 6);
+    cudaError_t e = cudaMalloc((void**)&h->sn_state, nd * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->sn_ints, (3 * N + 1) * sizeof(int));
+    if (e == cudaSuccess && !h->sn_n_host) e = cudaHostAlloc((void**)&h->sn_n_host, sizeof(int), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(h, SDEM_E_NOMEM, "allocation of the output snapshot buffers failed");
+    }
+  }
+  if (contacts && !h->sn_cdev) {
+    const size_t bytes = snap_layout(nullptr, N, (size_t)h->ccap, nullptr);
+    cudaError_t e = cudaMalloc(&h->sn_cdev, bytes);
+    if (e == cudaSuccess) e = cudaHostAlloc(&h->sn_chost, bytes, cudaHostAllocMapped);
+    void* hd = nullptr;
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(&hd, h->sn_chost, 0);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(h, SDEM_E_NOMEM, "allocation of the contact snapshot buffers failed");
+    }
+    snap_layout((char*)h->sn_cdev, N, (size_t)h->ccap, &h->sn_dev);
+    snap_layout((char*)h->sn_chost, N, (size_t)h->ccap, &h->sn_host);
+    snap_layout((char*)hd, N, (size_t)h->ccap, &h->sn_host_dptr);
+  }
+  return 0;
+}
+
+// Enqueues a snapshot: the frozen copy on the main stream (after every step
+// enqueued so far), its download on the I/O stream.  Null host pointers are
+// skipped.
+int snapshot_begin(sdem_h* h, int* id, int* ptype, int* usrmark, double* posR, double* linVel, double* linAcc,
+                   double* theta, double* rotVel, double* rotAcc, double* F, double* T, bool contacts) {
+  if (h->snap_busy) {
+    CK(cudaEventSynchronize(h->ev_snap_done));
+    h->snap_busy = false;
+  }
+  int rc = ensure_snapshot_buffers(h, contacts);
   if (rc) return rc;
+  const sdem_cfg& c = h->cfg;
+  const int n = h->n_host;   // rows copied: the device count never exceeds it
+  const size_t N = (size_t)c.n_capacity;
+  cudaStream_t st = h->stream, io = h->stream_io;
+  int* s_id = h->sn_ints;
+  int* s_pt = s_id + N;
+  int* s_um = s_pt + N;
+  int* s_n = s_um + N;
+  double* s_pos = h->sn_state;
+  double* s_vec = s_pos + 4 * N;
+  CK(cudaMemcpyAsync(s_n, h->scal + S_N, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  if (n > 0) {
+    if (id) CK(cudaMemcpyAsync(s_id, h->gid, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+    if (ptype) CK(cudaMemcpyAsync(s_pt, h->ptype, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+    if (usrmark) CK(cudaMemcpyAsync(s_um, h->usrmark, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+    if (posR) CK(cudaMemcpyAsync(s_pos, h->posr, sizeof(dbl4) * n, cudaMemcpyDeviceToDevice, st));
+  }
+  // 3-vector fields in their host layouts, one after another
+  struct Field { double* host; int levels; dbl4* const* dev; };
+  dbl4* th[1] = {h->theta};
+  dbl4* fF[1] = {h->F};
+  dbl4* fT[1] = {h->T};
+  const Field fields[7] = {{linVel, c.tsize, h->vel}, {linAcc, c.tsize, h->acc}, {theta, 1, th},
+                           {rotVel, c.rsize, h->rv}, {rotAcc, c.rsize, h->ra}, {F, 1, fF}, {T, 1, fT}};
+  double* sp = s_vec;
+  double* where[7];
+  for (int f = 0; f < 7; f++) {
+    where[f] = sp;
+    if (fields[f].host && n > 0)
+      for (int k = 0; k < fields[f].levels; k++)
+        k_pack3<<<grid_for(n), kThreads, 0, st>>>(sp, fields[f].dev[k], n, fields[f].levels, k);
+    sp += 3 * (size_t)fields[f].levels * N;
+  }
+  h->snap_contacts = contacts;
+  h->snap_stepped = h->stepped;
+  if (contacts) {
+    const int lw = 1 - h->cur;   // the buffers the last step wrote
+    Dev d = make_dev(h);
+    const int use_rows = h->stepped ? 1 : 0;
+    k_snap_contacts<<<h->num_sms * 4, kThreads, 0, st>>>(d, h->c_pgid[lw], h->c_hist[lw], h->wh_cnt[lw],
+                                                         h->wh_wall[lw], h->wh_hist[lw], h->sn_dev,
+                                                         use_rows ? h->n_host + h->gcap : -1);
+    h->sn_up = h->h_up;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(h->ev_snap, st));
+  // download on the I/O stream
+  CK(cudaStreamWaitEvent(io, h->ev_snap, 0));
+  CK(cudaMemcpyAsync(h->sn_n_host, s_n, sizeof(int), cudaMemcpyDeviceToHost, io));
+  if (n > 0) {
+    if (id) CK(cudaMemcpyAsync(id, s_id, sizeof(int) * n, cudaMemcpyDeviceToHost, io));
+    if (ptype) CK(cudaMemcpyAsync(ptype, s_pt, sizeof(int) * n, cudaMemcpyDeviceToHost, io));
+    if (usrmark) CK(cudaMemcpyAsync(usrmark, s_um, sizeof(int) * n, cudaMemcpyDeviceToHost, io));
+    if (posR) CK(cudaMemcpyAsync(posR, s_pos, sizeof(dbl4) * n, cudaMemcpyDeviceToHost, io));
+    for (int f = 0; f < 7; f++)
+      if (fields[f].host)
+        CK(cudaMemcpyAsync(fields[f].host, where[f], sizeof(double) * 3 * fields[f].levels * (size_t)n,
+                           cudaMemcpyDeviceToHost, io));
+  }
+  if (contacts) k_snap_copy<<<h->num_sms * 2, kThreads, 0, io>>>(h->sn_dev, h->sn_host_dptr);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(h->ev_snap_done, io));
+  h->snap_busy = true;
+  h->snap_done = false;
+  return 0;
+}
+
+int snapshot_end(sdem_h* h, int* n_out) {
+  if (!h->snap_busy) return set_err(h, SDEM_E_ARG, "sdem_snapshot_end: no snapshot in flight");
+  CK(cudaEventSynchronize(h->ev_snap_done));
+  h->snap_busy = false;
+  h->snap_done = true;
+  if (n_out) *n_out = *h->sn_n_host;
+  return 0;
+}
+
+// Contact records of the finished snapshot, in the restart writer's listing:
+// a local pair under both particles (bucket + Head_Cp), a pair with a periodic
+// image under its local particle, then each particle's wall records.
+int snapshot_records(sdem_h* h, std::vector<CRec>& out) {
+  if (!h->snap_done || !h->snap_contacts) return set_err(h, SDEM_E_ARG, "no finished snapshot with contacts");
   out.clear();
-  int n = 0;
-  CK(cudaMemcpy(&n, h->scal + S_N, sizeof n, cudaMemcpyDeviceToHost));
-  std::vector<int> gid(std::max(n, 1));
-  CK(cudaMemcpy(gid.data(), h->gid, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  const SnapContacts& v = h->sn_host;
+  const int n = v.scal[0];
   const sdem_cfg& c = h->cfg;
   std::vector<int> idx_of((size_t)c.max_gid + 1, -1);
-  for (int i = 0; i < n; i++) idx_of[gid[i]] = i;
-  // the buffers last written are "prev" now (cur flipped after each step)
-  int lw = 1 - h->cur;
-  size_t G = (size_t)c.max_gid + 1;
-  if (h->stepped) {
-    int C = 0;
-    CK(cudaMemcpy(&C, h->row_off + h->n_host + h->gcap, sizeof C, cudaMemcpyDeviceToHost));
-    std::vector<int> og(std::max(C, 1)), pg(std::max(C, 1));
-    std::vector<dbl4> hs(std::max(C, 1));
-    if (C > 0) {
-      CK(cudaMemcpy(og.data(), h->c_ogid, sizeof(int) * C, cudaMemcpyDeviceToHost));
-      CK(cudaMemcpy(pg.data(), h->c_pgid[lw], sizeof(int) * C, cudaMemcpyDeviceToHost));
-      CK(cudaMemcpy(hs.data(), h->c_hist[lw], sizeof(dbl4) * C, cudaMemcpyDeviceToHost));
-    }
-    // a local pair is listed under both particles (bucket + Head_Cp), a pair
-    // with a periodic image under its local particle only
+  for (int i = 0; i < n; i++) idx_of[v.gid[i]] = i;
+  if (h->snap_stepped) {
+    const int C = v.scal[1];
     for (int i = 0; i < C; i++) {
-      const bool img = (og[i] & kImgFlag) != 0;
-      const int o = og[i] & ~kImgFlag;
-      int a = idx_of[o], b = img ? -1 : idx_of[pg[i]];
+      const bool img = (v.og[i] & kImgFlag) != 0;
+      const int o = v.og[i] & ~kImgFlag;
+      const int a = idx_of[o], b = img ? -1 : idx_of[v.pg[i]];
       CRec r;
-      r.t[0] = hs[i].x; r.t[1] = hs[i].y; r.t[2] = hs[i].z; r.vr = hs[i].w;
-      if (a >= 0) { r.owner = a; r.partner = pg[i]; out.push_back(r); }
+      r.t[0] = v.hs[i].x; r.t[1] = v.hs[i].y; r.t[2] = v.hs[i].z; r.vr = v.hs[i].w;
+      if (a >= 0) { r.owner = a; r.partner = v.pg[i]; out.push_back(r); }
       if (b >= 0) { r.owner = b; r.partner = o; out.push_back(r); }
     }
   } else {
-    // not stepped since upload: report the uploaded history
-    for (const auto& u : h->h_up) {
-      int a = idx_of[u.owner], b = u.both ? idx_of[u.partner] : -1;
+    // not stepped since upload: the uploaded history
+    for (const auto& u : h->sn_up) {
+      const int a = idx_of[u.owner], b = u.both ? idx_of[u.partner] : -1;
       CRec r;
       r.t[0] = u.hist.x; r.t[1] = u.hist.y; r.t[2] = u.hist.z; r.vr = u.hist.w;
       if (a >= 0) { r.owner = a; r.partner = u.partner; out.push_back(r); }
       if (b >= 0) { r.owner = b; r.partner = u.owner; out.push_back(r); }
     }
   }
-  std::vector<int> whc(G), whw(G * kKw);
-  std::vector<dbl4> whh(G * kKw);
-  CK(cudaMemcpy(whc.data(), h->wh_cnt[lw], sizeof(int) * G, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(whw.data(), h->wh_wall[lw], sizeof(int) * G * kKw, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(whh.data(), h->wh_hist[lw], sizeof(dbl4) * G * kKw, cudaMemcpyDeviceToHost));
   for (int i = 0; i < n; i++) {
-    int g = gid[i];
-    for (int j = 0; j < whc[g] && j < kKw; j++) {
-      int wi = whw[(size_t)g * kKw + j];
+    for (int j = 0; j < v.wcnt[i] && j < kKw; j++) {
+      const int wi = v.wwall[(size_t)i * kKw + j];
       if (wi < 0 || wi >= h->nw) continue;
       CRec r;
       r.owner = i;
       r.partner = h->h_wall_id[wi];
-      dbl4 v = whh[(size_t)g * kKw + j];
-      r.t[0] = v.x; r.t[1] = v.y; r.t[2] = v.z; r.vr = v.w;
+      const dbl4 w = v.whist[(size_t)i * kKw + j];
+      r.t[0] = w.x; r.t[1] = w.y; r.t[2] = w.z; r.vr = w.w;
       out.push_back(r);
     }
   }
@@ -2365,14 +2563,21 @@ int gather_contacts(sdem_h* h, std::vector<CRec>& out) {
   });
   return 0;
 }
-}  // namespace
 
-int sdem_download_contacts(sdem_h* h, int cap, int* nc, int* owner_idx, int* partner_id, double* tandelta,
-                           double* velrel) {
-  if (!h || !nc) return SDEM_E_ARG;
-  std::vector<CRec> recs;
-  int rc = gather_contacts(h, recs);
+int gather_contacts(sdem_h* h, std::vector<CRec>& out) {
+  int rc = sync_and_check(h);
   if (rc) return rc;
+  rc = snapshot_begin(h, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, true);
+  if (rc) return rc;
+  rc = snapshot_end(h, nullptr);
+  if (rc) return rc;
+  return snapshot_records(h, out);
+}
+
+int emit_records(sdem_h* h, const std::vector<CRec>& recs, int cap, int* nc, int* owner_idx, int* partner_id,
+                 double* tandelta, double* velrel) {
+  (void)h;
   *nc = (int)recs.size();
   if ((int)recs.size() > cap || !owner_idx || !partner_id || !tandelta || !velrel) return 0;
   for (size_t i = 0; i < recs.size(); i++) {
@@ -2384,6 +2589,38 @@ int sdem_download_contacts(sdem_h* h, int cap, int* nc, int* owner_idx, int* par
     velrel[i] = recs[i].vr;
   }
   return 0;
+}
+}  // namespace
+
+int sdem_download_contacts(sdem_h* h, int cap, int* nc, int* owner_idx, int* partner_id, double* tandelta,
+                           double* velrel) {
+  if (!h || !nc) return SDEM_E_ARG;
+  std::vector<CRec> recs;
+  int rc = gather_contacts(h, recs);
+  if (rc) return rc;
+  return emit_records(h, recs, cap, nc, owner_idx, partner_id, tandelta, velrel);
+}
+
+int sdem_snapshot_begin(sdem_h* h, int* id, int* ptype, int* usrmark, double* posR, double* linVel, double* linAcc,
+                        double* theta, double* rotVel, double* rotAcc, double* F, double* T, int want_contacts) {
+  if (!h) return SDEM_E_ARG;
+  if (!h->have_types) return set_err(h, SDEM_E_ARG, "sdem_snapshot_begin: call sdem_set_types first");
+  return snapshot_begin(h, id, ptype, usrmark, posR, linVel, linAcc, theta, rotVel, rotAcc, F, T, want_contacts != 0);
+}
+
+int sdem_snapshot_end(sdem_h* h, int* n_out) {
+  if (!h) return SDEM_E_ARG;
+  // waits for the download only: steps enqueued after the snapshot keep running
+  return snapshot_end(h, n_out);
+}
+
+int sdem_snapshot_contacts(sdem_h* h, int cap, int* nc, int* owner_idx, int* partner_id, double* tandelta,
+                           double* velrel) {
+  if (!h || !nc) return SDEM_E_ARG;
+  std::vector<CRec> recs;
+  int rc = snapshot_records(h, recs);
+  if (rc) return rc;
+  return emit_records(h, recs, cap, nc, owner_idx, partner_id, tandelta, velrel);
 }
 
 int sdem_check_restart_limit(sdem_h* h) {
@@ -2593,6 +2830,15 @@ void sdem_destroy(sdem_h* h) {
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
   if (h->stage) cudaFree(h->stage);
+  if (h->stream_io) cudaStreamSynchronize(h->stream_io);
+  if (h->sn_state) cudaFree(h->sn_state);
+  if (h->sn_ints) cudaFree(h->sn_ints);
+  if (h->sn_cdev) cudaFree(h->sn_cdev);
+  if (h->sn_chost) cudaFreeHost(h->sn_chost);
+  if (h->sn_n_host) cudaFreeHost(h->sn_n_host);
+  if (h->ev_snap) cudaEventDestroy(h->ev_snap);
+  if (h->ev_snap_done) cudaEventDestroy(h->ev_snap_done);
+  if (h->stream_io) cudaStreamDestroy(h->stream_io);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
