@@ -118,6 +118,7 @@ typedef struct sdem_cfg {
   double dom_min[3], dom_max[3];/* SimDomain_min/max (the whole domain on one rank)  */
   double cs_ratio;              /* Prtcl_cs_ratio                                    */
   double wall_neighbor_ratio;   /* Wall_neighbor_ratio                               */
+  int    n_fixed_capacity;      /* numPrtclFix: most fixed spheres (0 = none)        */
 } sdem_cfg;
 
 typedef struct sdem_h sdem_h;
@@ -201,6 +202,16 @@ int sdem_check_restart_limit(sdem_h* h);
 /* Contact force and torque of the last step (GPrtcl_cntctForce, GPrtcl_torque),
  * 3 doubles per particle each; either may be NULL. */
 int sdem_download_forces(sdem_h* h, double* F, double* T);
+
+/* Fixed spheres (PIO_ReadFixedCoord, Prtcl_IOAndVisu.f90:164-291; FineSearch1
+ * and ContactForce_PPFix, Prtcl_NBS_Munjiza.f90:478-498,
+ * Prtcl_CL_and_CF.f90:200-222,803-827): nfix <= n_fixed_capacity spheres,
+ * centres pos (3 doubles each), types 1..nT (radius from the type) and ids
+ * above max_gid and below base_wall_id (the reference numbers them file
+ * position + numPrtcl).  Spheres outside [dom_min, dom_max) are dropped, as the
+ * reader does on one rank.  Call after sdem_set_types; not with periodic
+ * directions (SDEM_E_UNSUPPORTED). */
+int sdem_set_fixed(sdem_h* h, int nfix, const int* id, const int* ptype, const double* pos);
 
 /* Counters of the last step, SDEM_CNT_SIZE ints (see SDEM_CNT_*). */
 int sdem_counters(sdem_h* h, int* out);

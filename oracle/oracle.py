@@ -42,6 +42,7 @@ def load() -> C.CDLL:
     lib.orc_create.restype = P
     lib.orc_set_types.argtypes = [P, C.c_int, dp, dp, dp, dp, C.c_int, dp]
     lib.orc_set_walls.argtypes = [P, C.c_int, dp, ip]
+    lib.orc_set_fixed.argtypes = [P, C.c_int, ip, ip, dp]
     lib.orc_upload_particles.argtypes = [P, C.c_int, ip, ip, ip, dp, dp, dp, dp, dp, dp]
     lib.orc_upload_contacts.argtypes = [P, C.c_int, ip, ip, dp, dp]
     lib.orc_step.argtypes = [P, C.c_int]
@@ -64,7 +65,7 @@ def load() -> C.CDLL:
     lib.orc_grid.restype = None
     lib.orc_set_iter.argtypes = [P, C.c_int]
     lib.orc_set_iter.restype = None
-    for name in ("orc_set_types", "orc_set_walls", "orc_upload_particles", "orc_upload_contacts", "orc_step",
+    for name in ("orc_set_types", "orc_set_walls", "orc_set_fixed", "orc_upload_particles", "orc_upload_contacts", "orc_step",
                  "orc_nlocal", "orc_download_particles", "orc_download_forces", "orc_download_contacts",
                  "orc_counters"):
         getattr(lib, name).restype = C.c_int
@@ -88,6 +89,12 @@ class OracleSystem:
         w, f = case.walls.arrays()
         self._check(self.lib.orc_set_walls(self.h, case.walls.n, dptr(w) if case.walls.n else None,
                                            iptr(f) if case.walls.n else None))
+        if case.fixed is not None and case.fixed.n:
+            fx = case.fixed
+            self._fix = (np.ascontiguousarray(fx.id, dtype=np.int32), np.ascontiguousarray(fx.ptype, dtype=np.int32),
+                         np.ascontiguousarray(fx.pos, dtype=np.float64))
+            self._check(self.lib.orc_set_fixed(self.h, fx.n, iptr(self._fix[0]), iptr(self._fix[1]),
+                                               dptr(self._fix[2])))
         self.upload(case.particles)
         if case.contacts is not None:
             self.upload_contacts(*case.contacts)

@@ -101,6 +101,11 @@ typedef struct orc {
   double cell_len, xst_cs, yst_cs, zst_cs;
   int nx, ny, nz, mbox;
   int *bx, *by, *bz, *NextX, *NextY, *NextZ, *HeadY, *HeadX, *HeadX0;
+  /* fixed particles (GPFix_*, PIO_ReadFixedCoord, Prtcl_IOAndVisu.f90:164-291),
+   * 1-based; in the search they take indices 1..nFixed, before the locals */
+  int nFixed;
+  int *FixId, *FixType;
+  r4* FixPosR;
   /* periodic ghosts (GhostP_*, Prtcl_Variables.f90:69-73), 1-based */
   int nGhost, mGhost;
   int *GhostP_id, *GhostP_pType;
@@ -326,6 +331,37 @@ int orc_set_types(orc* h, int nT, const double* radius, const double* mass,
   h->DeltaXmax1 = maxR * h->cfg.wall_neighbor_ratio;
   h->DeltaXmax2 = maxR * (h->cfg.wall_neighbor_ratio + 1.0);
   h->have_types = 1;
+  return 0;
+}
+
+static void grow_nbs(orc* h);
+
+/* PIO_ReadFixedCoord (Prtcl_IOAndVisu.f90:164-291) on one rank: the fixed
+ * spheres inside [dom_min, dom_max) are kept in file order; ids as given (the
+ * reader numbers them file position + numPrtcl, :249); the radius comes from
+ * the type (:222). */
+int orc_set_fixed(orc* h, int nfix, const int* id, const int* ptype, const double* pos) {
+  if (!h->have_types) return fail(h, SDEM_E_ARG, "orc_set_fixed: call orc_set_types first");
+  if (h->cfg.periodic[0] || h->cfg.periodic[1] || h->cfg.periodic[2])
+    return fail(h, SDEM_E_UNSUPPORTED, "orc_set_fixed: the fixed spheres' periodic images are not restated");
+  free(h->FixId); free(h->FixType); free(h->FixPosR);
+  h->FixId = (int*)xcalloc((size_t)nfix + 1, sizeof(int));
+  h->FixType = (int*)xcalloc((size_t)nfix + 1, sizeof(int));
+  h->FixPosR = (r4*)xcalloc((size_t)nfix + 1, sizeof(r4));
+  int k = 0;
+  for (int i = 0; i < nfix; i++) {
+    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    if (ptype[i] < 1 || ptype[i] > h->nT) return fail(h, SDEM_E_ARG, "orc_set_fixed: type outside 1..nT");
+    if (!(x >= h->cfg.dom_min[0] && x < h->cfg.dom_max[0] && y >= h->cfg.dom_min[1] && y < h->cfg.dom_max[1] &&
+          z >= h->cfg.dom_min[2] && z < h->cfg.dom_max[2]))
+      continue;
+    k++;
+    h->FixId[k] = id[i];
+    h->FixType[k] = ptype[i];
+    h->FixPosR[k] = (r4){x, y, z, h->Radius[ptype[i] - 1]};
+  }
+  h->nFixed = k;
+  if (h->nFixed + h->nlocal + h->nGhost >= h->mbox) grow_nbs(h);
   return 0;
 }
 
@@ -801,7 +837,7 @@ static void comm_for_cntct(orc* h) {
     }
   }
   h->nGhost = ng;
-  if (h->nlocal + ng > h->mbox) grow_nbs(h);
+  if (h->nFixed + h->nlocal + ng >= h->mbox) grow_nbs(h);
 }
 
 /* ContactForce_PPG, Prtcl_CL_and_CF.f90:761-798: force on the local particle only */
@@ -881,10 +917,60 @@ static void fine_search2(orc* h, int pid1, int pid2) {
   else add_contact_pp(h, pid2, pid1, ovrlp);
 }
 
-/* NBSM_clcBoxIndex, :163-212 (no fixed or ghost particles) */
+/* ContactForce_PPFix, Prtcl_CL_and_CF.f90:803-827: the moving particle is i,
+ * the fixed one j (zero velocities); force and torque on i only (the
+ * ContactForce_PPFix_W branch of Prtcl_ContactForce_inc.f90:83-86). */
+static void contact_force_ppfix(orc* h, int pid, int f, int ind, double ovrlp) {
+  const double* P = bp_pp(h, h->pType[pid], h->FixType[f]);
+  r4 Posi = h->PosR[pid], Posj = h->FixPosR[f];
+  double ri = Posi.w, rj = Posj.w;
+  r3 Norm_v = nv_of(r3sub(r4xyz(Posj), r4xyz(Posi)));
+  r3 S, M, Mr;
+  contact_force(h, P, LV(h, 1, pid), zero_r3, RV(h, 1, pid), zero_r3, ri, rj, Norm_v, ovrlp, ind, &S, &M, &Mr);
+  h->F[pid] = r3add(h->F[pid], S);
+  h->T[pid] = r3add(r3add(h->T[pid], r3scale(M, ri)), Mr);
+}
+
+/* CL_AddContactPPFix, Prtcl_CL_and_CF.f90:200-222 */
+static void add_contact_ppfix(orc* h, int id1, int f, double ovrlp) {
+  int item1, item2;
+  find_insert(h, id1, h->FixId[f], &item1, &item2);
+  if (item1 > 0) {
+    h->CntctStatus[item2] = item1;
+    h->numCntcts[2]++;
+    contact_force_ppfix(h, id1, f, item2, ovrlp);
+  } else if (item1 == -1) {
+    fail(h, SDEM_E_BAD_ID, "CL_AddContactPPFix: The inserted item's id is greater than allowed value");
+  } else {
+    fail(h, SDEM_E_CL_FULL, "CL_AddContactPPFix: The container is full and there is no space for new item");
+  }
+}
+
+/* NBSM_FineSearch1, Prtcl_NBS_Munjiza.f90:478-498 (pid1 a local, f a fixed particle) */
+static void fine_search1(orc* h, int pid1, int f) {
+  double dx, dy, dz, dr, d2sum, dr2, ovrlp;
+  dr = h->PosR[pid1].w + h->FixPosR[f].w;
+  dr2 = dr * dr;
+  dx = h->PosR[pid1].x - h->FixPosR[f].x;
+  d2sum = dx * dx;
+  if (d2sum > dr2) return;
+  dy = h->PosR[pid1].y - h->FixPosR[f].y;
+  d2sum = dy * dy + d2sum;
+  if (d2sum > dr2) return;
+  dz = h->PosR[pid1].z - h->FixPosR[f].z;
+  d2sum = dz * dz + d2sum;
+  if (d2sum > dr2) return;
+  ovrlp = dr - sqrt(d2sum);
+  add_contact_ppfix(h, pid1, f, ovrlp);
+}
+
+/* NBSM_clcBoxIndex, :163-212, and the fixed particles' indices of Init_NBSM
+ * (:104-109).  Search index s: 1..nFixed fixed, then the locals, then the
+ * ghosts (nFixedAndlocal = nFixed + nlocal, :127-129). */
 static int clc_box_index(orc* h) {
-  for (int i = 1; i <= h->nlocal + h->nGhost; i++) {
-    r4 P = (i <= h->nlocal) ? h->PosR[i] : h->GhostP_PosR[i - h->nlocal];
+  const int nf = h->nFixed, nfl = h->nFixed + h->nlocal;
+  for (int i = 1; i <= nfl + h->nGhost; i++) {
+    r4 P = (i <= nf) ? h->FixPosR[i] : (i <= nfl) ? h->PosR[i - nf] : h->GhostP_PosR[i - nfl];
     double rpdx = P.x - h->xst_cs;
     double rpdy = P.y - h->yst_cs;
     double rpdz = P.z - h->zst_cs;
@@ -902,7 +988,7 @@ static int clc_box_index(orc* h) {
 
 static void build_y_list(orc* h) { /* :217-229 */
   for (int i = 1; i <= h->ny; i++) h->HeadY[i] = -1;
-  for (int i = 1; i <= h->nlocal + h->nGhost; i++) {
+  for (int i = 1; i <= h->nFixed + h->nlocal + h->nGhost; i++) {
     int iy = h->by[i];
     h->NextY[i] = h->HeadY[iy];
     h->HeadY[iy] = i;
@@ -944,14 +1030,24 @@ static void build_z_list0(orc* h, int ix, int m) { /* :277-296 */
   }
 }
 
-/* NBSM_LoopNBSMask, :302-473: moving particles and their ghost images (the
- * ghost branch :358-405 and the ELSE branch :406-469; no fixed particles) */
+/* NBSM_LoopNBSMask, :302-473.  Search indices: s <= nf fixed, s > nfl ghost,
+ * else local (local pid = s - nf, ghost index for fine_search3 = s - nf).
+ * A fixed or ghost target pairs with local particles only (FineSearch1/3 with
+ * the local first); a local target with everything (:406-469). */
 static void loop_nbs_mask(orc* h, int iz) {
-  const int nl = h->nlocal;
+  const int nf = h->nFixed, nfl = h->nFixed + h->nlocal;
   int m = HZ(h, 1, iz);
   while (m != -1) {
-    if (m > nl) {
-#define GHOST_VISIT(start) do { int n_ = (start); while (n_ != -1) { if (n_ <= nl) { fine_search3(h, n_, m); h->num_Cnsv++; } n_ = h->NextZ[n_]; } } while (0)
+    if (m <= nf) {
+#define FIXED_VISIT(start) do { int n_ = (start); while (n_ != -1) { if (n_ <= nfl && n_ > nf) { fine_search1(h, n_ - nf, m); h->num_Cnsv++; } n_ = h->NextZ[n_]; } } while (0)
+      FIXED_VISIT(h->NextZ[m]);
+      FIXED_VISIT(HZ(h, 1, iz - 1));
+      for (int i = -1; i <= 1; i++) FIXED_VISIT(HZ(h, 0, iz + i));
+      for (int lx = 0; lx <= 2; lx++)
+        for (int i = -1; i <= 1; i++) FIXED_VISIT(HZ0(h, lx, iz + i));
+#undef FIXED_VISIT
+    } else if (m > nfl) {
+#define GHOST_VISIT(start) do { int n_ = (start); while (n_ != -1) { if (n_ <= nfl && n_ > nf) { fine_search3(h, n_ - nf, m - nf); h->num_Cnsv++; } n_ = h->NextZ[n_]; } } while (0)
       GHOST_VISIT(h->NextZ[m]);
       GHOST_VISIT(HZ(h, 1, iz - 1));
       for (int i = -1; i <= 1; i++) GHOST_VISIT(HZ(h, 0, iz + i));
@@ -959,7 +1055,7 @@ static void loop_nbs_mask(orc* h, int iz) {
         for (int i = -1; i <= 1; i++) GHOST_VISIT(HZ0(h, lx, iz + i));
 #undef GHOST_VISIT
     } else {
-#define LOCAL_VISIT(start) do { int n_ = (start); while (n_ != -1) { if (n_ > nl) fine_search3(h, m, n_); else fine_search2(h, m, n_); h->num_Cnsv++; n_ = h->NextZ[n_]; } } while (0)
+#define LOCAL_VISIT(start) do { int n_ = (start); while (n_ != -1) { if (n_ <= nf) fine_search1(h, m - nf, n_); else if (n_ > nfl) fine_search3(h, m - nf, n_ - nf); else fine_search2(h, m - nf, n_ - nf); h->num_Cnsv++; n_ = h->NextZ[n_]; } } while (0)
       LOCAL_VISIT(h->NextZ[m]);
       LOCAL_VISIT(HZ(h, 1, iz - 1));
       for (int i = -1; i <= 1; i++) LOCAL_VISIT(HZ(h, 0, iz + i));
@@ -974,7 +1070,7 @@ static void loop_nbs_mask(orc* h, int iz) {
 /* NBSM_clcBoxIndex regrow (:172-189): room for locals + ghosts */
 static void grow_nbs(orc* h) {
   int sizen = (int)(1.2 * (double)h->mbox);
-  int need = h->nlocal + h->nGhost + 1;
+  int need = h->nFixed + h->nlocal + h->nGhost + 1;
   if (sizen < need) sizen = need;
   free(h->bx); free(h->by); free(h->bz); free(h->NextX); free(h->NextY); free(h->NextZ);
   h->bx = (int*)xcalloc(sizen + 1, sizeof(int));
@@ -1408,6 +1504,7 @@ void orc_grid(orc* h, double* cell_len, double* origin, int* dims) {
 
 void orc_destroy(orc* h) {
   if (!h) return;
+  free(h->FixId); free(h->FixType); free(h->FixPosR);
   free(h->id); free(h->pType); free(h->usrMark); free(h->PosR);
   free(h->linVel); free(h->linAcc); free(h->rotVel); free(h->rotAcc);
   free(h->theta); free(h->F); free(h->T);

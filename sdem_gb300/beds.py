@@ -74,6 +74,20 @@ class Particles:
 
 
 @dataclass
+class FixedSpheres:
+    """Fixed spheres (GPFix_id, GPFix_pType, GPFix_PosR; PIO_ReadFixedCoord,
+    Prtcl_IOAndVisu.f90:164-291).  The reference numbers them file position +
+    numPrtcl, above every moving id; the radius comes from the type."""
+    id: np.ndarray      # int32 (n,)
+    ptype: np.ndarray   # int32 (n,), 1-based
+    pos: np.ndarray     # (n, 3)
+
+    @property
+    def n(self) -> int:
+        return len(self.id)
+
+
+@dataclass
 class Case:
     name: str
     opts: Options
@@ -82,6 +96,7 @@ class Case:
     particles: Particles
     contacts: Optional[tuple] = None   # (owner_idx, partner_id, tandelta (nc,3), velrel) or None
     note: str = ""
+    fixed: Optional[FixedSpheres] = None
 
     @property
     def max_gid(self) -> int:
@@ -463,6 +478,126 @@ def periodic_lattice_case(n: int, seed: int, periodic=(1, 1, 1), nn: float = 1.0
     walls = box_walls(tuple(wlo), tuple(whi), base_wall_id=opts.base_wall_id,
                       skip_axes=[k for k in range(3) if periodic[k]])
     return Case(f"periodic_{n}_{seed}_{''.join(str(int(v)) for v in periodic)}", opts, case.tables, walls, p)
+
+
+def hopper_case(n: int, seed: int, width: float = 20.0e-3, outlet: float = 6.0e-3, angle_deg: float = 60.0,
+                d_small: float = 0.5e-3, d_large: float = 1.5e-3, frac_large: float = 0.3, e_n: float = 0.7,
+                mu: float = 0.5, E: float = 5.0e7, dt: float = 5.0e-7, vfall: float = 0.5, pi: int = 2,
+                pri: int = 2) -> Case:
+    """A small hopper of the bidisperse kind: Hertz spheres of diameters
+    d_small and d_large (by count (1 - frac_large) : frac_large) in a square
+    funnel of four finite inclined planes (angle_deg from the horizontal) whose
+    lower edges frame a square outlet, with four finite vertical planes
+    holding a column above it.  Below the outlet the domain ends at y = 0, so
+    spheres that fall through leave it and are deleted (one rank,
+    Comm_For_Exchange).  The spheres start on a jittered cubic lattice (pitch
+    0.97 d_large, so neighbouring large spheres and the walls already touch)
+    filling the outlet throat and the funnel from the bottom up, moving down
+    at up to vfall m/s; the ones in the throat fall fast (40-80 m/s) so that
+    a few steps already delete some."""
+    rng = np.random.default_rng(seed)
+    diam = np.array([d_small, d_large])
+    coefs = (mu, mu, 0.1, e_n, e_n)
+    tables = props.build_tables(props.CFT_NLIN, list(diam), [2500.0] * 2, [E] * 2, [0.3] * 2, coefs, [E], [0.3],
+                                coefs)
+    W, a = width, outlet
+    c = 0.5 * W
+    run = 0.5 * (W - a)
+    drop = run * math.tan(math.radians(angle_deg))
+    y_o = 4.0e-3                       # outlet level; the throat below it is open down to y = 0
+    y_t = y_o + drop                   # top of the funnel
+    y_top = y_t + 0.75 * W             # top of the column
+    centre = np.array([c, 0.5 * (y_o + y_t), c])
+    walls = WallSet()
+    kw = dict(infinite=False, base_wall_id=10000000)
+
+    def add(quad):
+        q = [np.array(p, dtype=float) for p in quad]
+        nrm = np.cross(q[1] - q[0], q[2] - q[0])
+        if np.dot(nrm, centre - q[0]) < 0:     # normals point into the hopper
+            q = q[::-1]
+        walls.add(*(tuple(p) for p in q), **kw)
+
+    lo, hi = c - 0.5 * a, c + 0.5 * a
+    # inclined sides (z = 0, z = W, x = 0, x = W edges at the top)
+    add([(0, y_t, 0), (W, y_t, 0), (hi, y_o, lo), (lo, y_o, lo)])
+    add([(0, y_t, W), (W, y_t, W), (hi, y_o, hi), (lo, y_o, hi)])
+    add([(0, y_t, 0), (0, y_t, W), (lo, y_o, hi), (lo, y_o, lo)])
+    add([(W, y_t, 0), (W, y_t, W), (hi, y_o, hi), (hi, y_o, lo)])
+    # vertical column
+    add([(0, y_t, 0), (W, y_t, 0), (W, y_top, 0), (0, y_top, 0)])
+    add([(0, y_t, W), (W, y_t, W), (W, y_top, W), (0, y_top, W)])
+    add([(0, y_t, 0), (0, y_t, W), (0, y_top, W), (0, y_top, 0)])
+    add([(W, y_t, 0), (W, y_t, W), (W, y_top, W), (W, y_top, 0)])
+    ptype = np.where(rng.uniform(size=4 * n) < frac_large, 2, 1).astype(np.int32)
+    pitch = 0.97 * d_large
+    g = np.arange(0.5 * pitch, max(W, y_top) + pitch, pitch)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    pts = pts + rng.uniform(-0.02 * pitch, 0.02 * pitch, size=pts.shape)
+    rmax = 0.5 * d_large
+    inside = np.ones(len(pts), bool)
+    for w in walls.walls:
+        nrm, dd = w[12:15], w[15]
+        inside &= (pts @ nrm + dd) >= 0.95 * rmax
+    throat = ((np.abs(pts[:, 0] - c) < 0.5 * a - 1.1 * rmax) & (np.abs(pts[:, 2] - c) < 0.5 * a - 1.1 * rmax)
+              & (pts[:, 1] > 0.6 * rmax) & (pts[:, 1] < y_o))
+    ok = (inside & (pts[:, 1] >= y_o) & (pts[:, 1] < y_top - rmax)) | throat
+    pts = pts[ok]
+    pts = pts[np.argsort(pts[:, 1], kind="stable")][:n]
+    if len(pts) < n:
+        raise ValueError("hopper_case: the hopper holds fewer lattice sites than n")
+    ptype = ptype[:n]
+    vel = np.zeros((n, 3))
+    vel[:, 1] = -rng.uniform(0.0, vfall, size=n)
+    in_throat = pts[:, 1] < y_o
+    vel[in_throat, 1] = -rng.uniform(40.0, 80.0, size=int(in_throat.sum()))
+    vel[:, 0] = rng.uniform(-0.05, 0.05, size=n)
+    vel[:, 2] = rng.uniform(-0.05, 0.05, size=n)
+    opts = Options(dt=dt, minpoint=(-1.0e-3, 0.0, -1.0e-3), maxpoint=(W + 1.0e-3, y_top + 1.0e-3, W + 1.0e-3),
+                   cf_type=props.CFT_NLIN, pi_method=pi, pri_method=pri)
+    parts = new_particles(pts, ptype, tables.radius, vel, opts.tsize, opts.rsize)
+    return Case(f"hopper_{n}_{seed}", opts, tables, walls, parts)
+
+
+def fixed_floor_case(n: int, seed: int, **kw) -> Case:
+    """lattice_cloud_case whose floor wall is replaced by a rough floor of
+    fixed spheres (one under every sphere of the lowest layer, overlapping it
+    by 2%), plus a few fixed spheres in place of moving ones inside the
+    cloud: moving-fixed pairs are found both from fixed and from moving
+    targets."""
+    case = lattice_cloud_case(n, seed, **kw)
+    rng = np.random.default_rng(seed + 1000)
+    p = case.particles
+    ft = 1                                              # the fixed spheres' type
+    rf = float(case.tables.radius[ft - 1])
+    lo = p.posR[:, :3].min(axis=0)
+    hi = p.posR[:, :3].max(axis=0)
+    low = np.nonzero(p.posR[:, 1] < p.posR[:, 1].min() + 0.5 * float(case.tables.radius.min()))[0]
+    # one fixed sphere under every sphere of the lowest layer, 2% into it
+    floor = p.posR[low, :3].copy()
+    floor[:, 1] -= 0.98 * (p.posR[low, 3] + rf)
+    floor[:, [0, 2]] += rng.uniform(-0.1 * rf, 0.1 * rf, size=(len(floor), 2))
+    y_floor = float(floor[:, 1].min())
+    # a few inside the cloud, in place of moving spheres
+    k = max(1, n // 50)
+    pick = rng.choice(np.setdiff1d(np.arange(n), low), size=k, replace=False)
+    inner = p.posR[np.sort(pick), :3].copy()
+    keep = np.setdiff1d(np.arange(n), pick)
+    parts = p.take(keep)
+    parts.id[:] = np.arange(1, len(keep) + 1, dtype=np.int32)
+    pos = np.concatenate([floor, inner])
+    nmax = int(parts.id.max())
+    fixed = FixedSpheres(id=np.arange(nmax + 1, nmax + 1 + len(pos), dtype=np.int32),
+                         ptype=np.full(len(pos), ft, np.int32), pos=pos)
+    walls = WallSet()
+    for w, f in zip(case.walls.walls[1:], case.walls.flags[1:]):   # no floor wall
+        walls.walls.append(w)
+        walls.flags.append(f)
+    lo_dom = list(case.opts.minpoint)
+    lo_dom[1] = min(lo_dom[1], y_floor - 2.0 * rf)
+    opts = replace(case.opts, minpoint=tuple(lo_dom))
+    return Case(f"fixedfloor_{n}_{seed}", opts, case.tables, walls, parts, fixed=fixed)
 
 
 def scaled(case: Case, **opt_changes) -> Case:

@@ -28,7 +28,8 @@ EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls
             "sdem_download_particles", "sdem_download_contacts", "sdem_check_restart_limit",
             "sdem_download_forces", "sdem_counters", "sdem_counter_sums", "sdem_launch_count", "sdem_profile_begin",
             "sdem_profile_end", "sdem_profile_phase_name", "sdem_count_contacts_noalloc", "sdem_selftest_fp64",
-            "sdem_snapshot_begin", "sdem_snapshot_end", "sdem_snapshot_contacts", "sdem_last_error", "sdem_destroy")
+            "sdem_snapshot_begin", "sdem_snapshot_end", "sdem_snapshot_contacts", "sdem_set_fixed", "sdem_last_error",
+            "sdem_destroy")
 
 
 def selftest_fp64(n: int, seed: int = 1) -> int:
@@ -51,7 +52,7 @@ class SdemCfg(C.Structure):
         ("wall_max_update_iter", C.c_int), ("periodic", C.c_int * 3), ("quirk_ab2_rot", C.c_int),
         ("max_contacts_per_particle", C.c_int), ("dt", C.c_double), ("gravity", C.c_double * 3),
         ("dom_min", C.c_double * 3), ("dom_max", C.c_double * 3), ("cs_ratio", C.c_double),
-        ("wall_neighbor_ratio", C.c_double),
+        ("wall_neighbor_ratio", C.c_double), ("n_fixed_capacity", C.c_int),
     ]
 
 
@@ -83,6 +84,7 @@ def cfg_from_case(case: Case, n_capacity: Optional[int] = None, max_gid: Optiona
     c.dt = o.dt
     c.cs_ratio = o.cs_ratio
     c.wall_neighbor_ratio = o.wall_neighbor_ratio
+    c.n_fixed_capacity = int(case.fixed.n) if case.fixed is not None else 0
     return c
 
 
@@ -106,6 +108,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_create.argtypes = [C.POINTER(SdemCfg), C.POINTER(P)]
     lib.sdem_set_types.argtypes = [P, C.c_int, dp, dp, dp, dp, C.c_int, dp]
     lib.sdem_set_walls.argtypes = [P, C.c_int, dp, ip]
+    lib.sdem_set_fixed.argtypes = [P, C.c_int, ip, ip, dp]
     lib.sdem_upload_particles.argtypes = [P, C.c_int, ip, ip, ip, dp, dp, dp, dp, dp, dp]
     lib.sdem_upload_contacts.argtypes = [P, C.c_int, ip, ip, dp, dp]
     lib.sdem_step.argtypes = [P, C.c_int]
@@ -187,9 +190,18 @@ class DEMSystem:
         w, f = case.walls.arrays()
         self._check(self.lib.sdem_set_walls(self.h, case.walls.n, dptr(w) if case.walls.n else None,
                                             iptr(f) if case.walls.n else None))
+        if case.fixed is not None and case.fixed.n:
+            self.set_fixed(case.fixed)
         self.upload(case.particles)
         if case.contacts is not None:
             self.upload_contacts(*case.contacts)
+
+    def set_fixed(self, fx) -> None:
+        """Fixed spheres (beds.FixedSpheres: ids above max_gid, types, centres)."""
+        self._fix = (np.ascontiguousarray(fx.id, dtype=np.int32), np.ascontiguousarray(fx.ptype, dtype=np.int32),
+                     np.ascontiguousarray(fx.pos, dtype=np.float64))
+        self._check(self.lib.sdem_set_fixed(self.h, len(self._fix[0]), iptr(self._fix[0]), iptr(self._fix[1]),
+                                            dptr(self._fix[2])))
 
     def _check(self, rc: int) -> None:
         if rc:

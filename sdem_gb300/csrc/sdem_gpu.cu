@@ -85,6 +85,10 @@ struct Dev {
   // periodic images: ghosts live at indices [n, n + ng) of the search arrays
   // (gid, ptype, posr, vel0, rv0 and the binning/row arrays, stride nall)
   int nall, nall_launch, gcap;
+  // fixed spheres: appended to the search arrays after the images every step
+  int nfix;
+  const int *fix_gid, *fix_ptype;
+  const dbl4* fix_posr;
   int* ng;
   int* nt;   // n + ng: particles the search sees
   int per[3];
@@ -386,6 +390,22 @@ __global__ void k_ghost_count(Dev d) {
   *d.nt = *d.n + ng;
 }
 
+// Fixed spheres join the search after the images (zero velocities); in the
+// within-cell order they rank below every moving sphere and image (the
+// reference gives them search indices 1..nFixed, Prtcl_NBS_Munjiza.f90:86).
+__global__ void k_fixed_append(Dev d) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int base = *d.n + *d.ng;
+  if (f == 0) *d.nt = base + d.nfix;
+  if (f >= d.nfix) return;
+  const int g = base + f;
+  d.posr[g] = d.fix_posr[f];
+  d.gid[g] = d.fix_gid[f];
+  d.ptype[g] = d.fix_ptype[f];
+  d.vel0[g] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+  d.rv0[g] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+}
+
 // ---------------------------------------------------------------------------
 // Binning: NBSM_clcBoxIndex (Prtcl_NBS_Munjiza.f90:193-198) + counting sort.
 // Linear cell key orders cells as the reference's sweep visits them:
@@ -429,8 +449,13 @@ __global__ void k_cellorder(Dev d) {
   int key = d.cell_of[p];
   if (key < 0) return;
   int a = d.cell_start[key], b = d.cell_start[key + 1];
+  // reference search index order: fixed spheres (appended after the moving
+  // spheres and images here) come first there, so they rank lowest
+  const int moving = d.fix_gid ? *d.n + *d.ng : 0x7FFFFFFF;
+  auto ref_key = [&](int q) { return q >= moving ? q - moving : q + d.nfix; };
+  const int kp = ref_key(p);
   int rank = 0;
-  for (int t = a; t < b; t++) rank += (d.tmp_sorted[t] > p);
+  for (int t = a; t < b; t++) rank += (ref_key(d.tmp_sorted[t]) > kp);
   d.sorted[a + rank] = p;
   d.sortpos[p] = a + rank;
   dbl4 P = d.posr[p];
@@ -687,7 +712,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     if (blockIdx.x == 0 && threadIdx.x == 0) raise(d, SDEM_E_CL_FULL, C);
     return;
   }
-  unsigned long long nimg = 0;
+  unsigned long long nimg = 0, nfx = 0;
+  const int first_fixed = nloc + *d.ng;   // search index of the first fixed sphere
   for (int c = c0 + blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
     const int s = d.c_row[c];
     const int slot = c - d.row_off[s];
@@ -744,10 +770,17 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     const int os = atomicAdd(&d.own_cnt[owner], 1);
     if (os < d.Ko) d.own_c[(size_t)owner * d.Ko + os] = c;
     else raise(d, SDEM_E_CL_FULL, owner);
-    nimg += img ? 1ull : 0ull;
+    // one-sided pairs: with an image (AddContactPPG) or a fixed sphere (AddContactPPFix)
+    const bool fx = img && oth >= first_fixed;
+    nimg += (img && !fx) ? 1ull : 0ull;
+    nfx += fx ? 1ull : 0ull;
   }
-  for (int o = 16; o > 0; o >>= 1) nimg += __shfl_down_sync(0xffffffffu, nimg, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    nimg += __shfl_down_sync(0xffffffffu, nimg, o);
+    nfx += __shfl_down_sync(0xffffffffu, nfx, o);
+  }
   if ((threadIdx.x & 31) == 0 && nimg) atomicAdd(&d.counters[5], nimg);
+  if ((threadIdx.x & 31) == 0 && nfx) atomicAdd(&d.counters[8], nfx);
 }
 
 // ---------------------------------------------------------------------------
@@ -1247,21 +1280,22 @@ __global__ void k_pack3(double* __restrict__ dst, const dbl4* __restrict__ src, 
 
 __global__ void k_step_end(Dev d, int* counters_out) {
   const int C = d.row_off[d.nall_launch];
-  counters_out[SDEM_CNT_PP] = C - (int)d.counters[5];
+  counters_out[SDEM_CNT_PP] = C - (int)d.counters[5] - (int)d.counters[8];
   counters_out[SDEM_CNT_PPG] = (int)d.counters[5];
-  counters_out[SDEM_CNT_PPFIX] = 0;
+  counters_out[SDEM_CNT_PPFIX] = (int)d.counters[8];
   counters_out[SDEM_CNT_PW] = (int)d.counters[1];
   counters_out[SDEM_CNT_CNSV] = (int)d.counters[0];
   counters_out[SDEM_CNT_NLOCAL] = *d.n;
   *d.iter += 1;
   counters_out[SDEM_CNT_ITER] = *d.iter;
   counters_out[SDEM_CNT_NEXTWALL] = *d.next_update;
-  d.counters[2] += (unsigned long long)(C - (int)d.counters[5]);
+  d.counters[2] += (unsigned long long)(C - (int)d.counters[5] - (int)d.counters[8]);
   d.counters[3] += d.counters[1];
   d.counters[4] += 1ull;
   d.counters[0] = 0;
   d.counters[1] = 0;
   d.counters[5] = 0;
+  d.counters[8] = 0;
   *d.out_cnt = 0;
   *d.wl_cnt = 0;
 }
@@ -1425,6 +1459,9 @@ struct sdem_h {
   int ccap = 0;
   int *c_ogid = nullptr, *c_pgid[2] = {}, *own_cnt[2] = {}, *own_c[2] = {}, *c_row = nullptr;
   int nall = 0, gcap = 0;
+  int fcap = 0, nfix = 0;
+  int *fix_gid = nullptr, *fix_ptype = nullptr;
+  dbl4* fix_posr = nullptr;
   int *gflag = nullptr, *goff = nullptr;
   // particle-particle records as uploaded (reported until the first step):
   // owner id, partner id, listed under the partner too
@@ -1444,7 +1481,9 @@ struct sdem_h {
   int cur = 0;  // buffer written by the next step
   // device scalars
   int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
-  unsigned long long* ull = nullptr;  // counters[5] (see Dev::counters), unused, red[2]
+  // device counters: [0] candidates, [1] wall contacts, [2..4] sums since
+  // upload, [5] image pairs, [6..7] max |v|, |a| reductions, [8] fixed pairs
+  unsigned long long* ull = nullptr;
   int *out_list = nullptr, *moves = nullptr, *map_pos = nullptr, *map_id = nullptr;
   int* h_counters = nullptr;  // pinned
   double* stage = nullptr;    // device staging of host-layout 3-vectors (upload, download)
@@ -1538,7 +1577,11 @@ Dev make_dev(sdem_h* h) {
   d.n = h->scal + S_N;
   d.nall = h->nall;
   d.gcap = h->gcap;
-  d.nall_launch = h->n_host + h->gcap;
+  d.nall_launch = h->n_host + h->gcap + h->nfix;
+  d.nfix = h->nfix;
+  d.fix_gid = h->fix_gid;
+  d.fix_ptype = h->fix_ptype;
+  d.fix_posr = h->fix_posr;
   d.ng = h->scal + S_NG;
   d.nt = h->scal + S_NT;
   for (int k = 0; k < 3; k++) d.per[k] = c.periodic[k];
@@ -1692,7 +1735,7 @@ int enqueue_step(sdem_h* h) {
   k_wall_refresh_end<<<1, 1, 0, st>>>(d);
   L += 2;
   mark(PH_BIN);
-  const int na = n + h->gcap;   // search arrays: locals and their periodic images
+  const int na = n + h->gcap + h->nfix;   // search arrays: locals, periodic images, fixed spheres
   k_ghost_begin<<<1, 1, 0, st>>>(d);
   L += 1;
   if (h->gcap > 0) {
@@ -1707,6 +1750,10 @@ int enqueue_step(sdem_h* h) {
       k_ghost_count<<<1, 1, 0, st>>>(d);
       L += 6;
     }
+  }
+  if (h->nfix > 0) {
+    k_fixed_append<<<grid_for(h->nfix), kThreads, 0, st>>>(d);
+    L += 1;
   }
   cudaMemsetAsync(h->cell_cnt, 0, sizeof(int) * (size_t)h->ncell, st);
   cudaMemsetAsync(h->in_cnt, 0, sizeof(int) * (size_t)std::max(n, 1), st);
@@ -1886,12 +1933,21 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   for (int k = 0; k < kChunks; k++) CK(cudaEventCreateWithFlags(&h->ev_chunk[k], cudaEventDisableTiming));
   int N = c.n_capacity;
+  if (c.n_fixed_capacity < 0) return bad("n_fixed_capacity must be >= 0");
+  if (c.n_fixed_capacity > 0 && nper > 0) {
+    h->err = "fixed spheres with periodic directions are not implemented on the GPU";
+    *out = h;
+    return SDEM_E_UNSUPPORTED;
+  }
+  h->fcap = c.n_fixed_capacity;
   // Periodic images need room beside the particles in the search arrays.  A
   // periodic side longer than two search cells gives every point at most one
   // image per direction (the bands at both faces are disjoint), so the
   // points after the y, x and z passes number at most 2^(directions) per particle.
   h->gcap = (int)(((long long)N << nper) - N);
-  const int NA = N + h->gcap;
+  if ((long long)N + h->gcap + h->fcap >= (1LL << 26))
+    return bad("particles + periodic images + fixed spheres must stay below 2^26");
+  const int NA = N + h->gcap + h->fcap;   // + fixed spheres after the images
   h->nall = NA;
   int rc = 0;
   rc |= dalloc(h, &h->gid, NA);
@@ -1905,6 +1961,11 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   if (h->gcap > 0) {
     rc |= dalloc(h, &h->gflag, (size_t)NA);
     rc |= dalloc(h, &h->goff, (size_t)NA + 1);
+  }
+  if (h->fcap > 0) {
+    rc |= dalloc(h, &h->fix_gid, (size_t)h->fcap);
+    rc |= dalloc(h, &h->fix_ptype, (size_t)h->fcap);
+    rc |= dalloc(h, &h->fix_posr, (size_t)h->fcap);
   }
   rc |= dalloc(h, &h->theta, N);
   rc |= dalloc(h, &h->F, N);
@@ -1950,7 +2011,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
     rc |= dalloc(h, &h->wh_hist[b], G * kKw);
   }
   rc |= dalloc(h, &h->scal, S_SIZE);
-  rc |= dalloc(h, &h->ull, 8);
+  rc |= dalloc(h, &h->ull, 10);
   rc |= dalloc(h, &h->out_list, kOutCap);
   rc |= dalloc(h, &h->moves, 1 + 2 * 5 * kOutCap + 5 * kOutCap);
   rc |= dalloc(h, &h->map_pos, 5 * kOutCap);
@@ -2061,6 +2122,39 @@ int sdem_set_walls(sdem_h* h, int nw, const double* wall, const int* flags) {
   return 0;
 }
 
+int sdem_set_fixed(sdem_h* h, int nfix, const int* id, const int* ptype, const double* pos) {
+  if (!h) return SDEM_E_ARG;
+  const sdem_cfg& c = h->cfg;
+  if (!h->have_types) return set_err(h, SDEM_E_ARG, "sdem_set_fixed: call sdem_set_types first");
+  if (nfix < 0 || (nfix > 0 && (!id || !ptype || !pos))) return set_err(h, SDEM_E_ARG, "sdem_set_fixed: bad arguments");
+  if (nfix > h->fcap) return set_err(h, SDEM_E_CAPACITY, "sdem_set_fixed: more fixed spheres than n_fixed_capacity");
+  std::vector<int> g, t;
+  std::vector<dbl4> p;
+  for (int i = 0; i < nfix; i++) {
+    if (ptype[i] < 1 || ptype[i] > h->nT) return set_err(h, SDEM_E_ARG, "sdem_set_fixed: type outside 1..nT");
+    if (id[i] <= c.max_gid || id[i] >= c.base_wall_id)
+      return set_err(h, SDEM_E_BAD_ID, "sdem_set_fixed: fixed ids must lie above max_gid and below base_wall_id");
+    const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    // PIO_ReadFixedCoord keeps the spheres of this rank's subdomain (:222)
+    if (!(x >= c.dom_min[0] && x < c.dom_max[0] && y >= c.dom_min[1] && y < c.dom_max[1] && z >= c.dom_min[2] &&
+          z < c.dom_max[2]))
+      continue;
+    g.push_back(id[i]);
+    t.push_back(ptype[i]);
+    p.push_back(make_dbl4(x, y, z, h->h_radius[ptype[i] - 1]));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  if (!g.empty()) {
+    CK(cudaMemcpyAsync(h->fix_gid, g.data(), sizeof(int) * g.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->fix_ptype, t.data(), sizeof(int) * t.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->fix_posr, p.data(), sizeof(dbl4) * p.size(), cudaMemcpyHostToDevice, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  h->nfix = (int)g.size();
+  drop_graph(h);   // the step graph bakes in the search length
+  return 0;
+}
+
 int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, const int* usrmark, const double* posR,
                           const double* linVel, const double* linAcc, const double* theta, const double* rotVel,
                           const double* rotAcc) {
@@ -2120,7 +2214,7 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   sc[S_N] = n;
   sc[S_NT] = n;
   CK(cudaMemcpyAsync(h->scal, sc, sizeof sc, cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(h->ull, 0, sizeof(unsigned long long) * 8, st));
+  CK(cudaMemsetAsync(h->ull, 0, sizeof(unsigned long long) * 10, st));
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
   h->n_host = n;
@@ -2479,7 +2573,7 @@ int snapshot_begin(sdem_h* h, int* id, int* ptype, int* usrmark, double* posR, d
     const int use_rows = h->stepped ? 1 : 0;
     k_snap_contacts<<<h->num_sms * 4, kThreads, 0, st>>>(d, h->c_pgid[lw], h->c_hist[lw], h->wh_cnt[lw],
                                                          h->wh_wall[lw], h->wh_hist[lw], h->sn_dev,
-                                                         use_rows ? h->n_host + h->gcap : -1);
+                                                         use_rows ? h->n_host + h->gcap + h->nfix : -1);
     h->sn_up = h->h_up;
   }
   CK(cudaGetLastError());

@@ -38,6 +38,12 @@ CASES = {
     "periodic_y": lambda: beds.periodic_lattice_case(800, 32, (0, 1, 0)),
     "periodic_xz": lambda: beds.periodic_lattice_case(800, 33, (1, 0, 1)),
     "periodic_x_lsd": lambda: beds.periodic_lattice_case(800, 34, (1, 0, 0), cf_type=props.CFT_LSD, ntypes=3),
+    # a small hopper: bidisperse 1:3 spheres, eight finite walls (inclined and
+    # vertical quads, their edges and corners), an outlet that deletes
+    "hopper": lambda: beds.hopper_case(1500, 51),
+    # fixed spheres (FineSearch1, ContactForce_PPFix): a rough floor and a few inside
+    "fixed_floor": lambda: beds.fixed_floor_case(800, 61),
+    "fixed_floor_lsd_fe": lambda: beds.fixed_floor_case(800, 62, cf_type=props.CFT_LSD, ntypes=3, pi=1, pri=1),
 }
 
 
@@ -75,7 +81,8 @@ def test_one_step_from_identical_inputs(gpu_lib, name):
     compare_step(g, o, case, name)
 
 
-@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "hertz_finite_walls", "periodic_xyz", "periodic_xz"])
+@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "hertz_finite_walls", "periodic_xyz", "periodic_xz",
+                                  "hopper", "fixed_floor"])
 def test_twenty_steps_resynchronised(gpu_lib, name):
     """A chain of single steps, each from the oracle's state and contact list
     (restart-file style), so chaos cannot hide or create a mismatch."""
@@ -83,7 +90,7 @@ def test_twenty_steps_resynchronised(gpu_lib, name):
     o = OracleSystem(case)
     for k in range(20):
         st = o.state()
-        c = beds.Case(case.name, case.opts, case.tables, case.walls, st, contacts=o.contacts())
+        c = beds.Case(case.name, case.opts, case.tables, case.walls, st, contacts=o.contacts(), fixed=case.fixed)
         g = DEMSystem(c)
         g.step(1)
         o.step(1)
@@ -91,7 +98,7 @@ def test_twenty_steps_resynchronised(gpu_lib, name):
         g.close()
 
 
-@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "periodic_xyz"])
+@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "periodic_xyz", "fixed_floor"])
 def test_free_run_trajectory(gpu_lib, name):
     """50 free-running steps: contact sets stay identical and the state within
     a loose bound (differences start at ~1 ulp per step)."""
@@ -182,6 +189,39 @@ def test_row_capacity_error(gpu_lib):
     assert e.value.code == 3
 
 
+def test_hopper_outflow_matches_oracle(gpu_lib):
+    """60 free-running steps of the hopper: the outlet deletes spheres in the
+    reference's swap-with-last order, wall and pair contact sets stay equal."""
+    case = CASES["hopper"]()
+    g, o = DEMSystem(case), OracleSystem(case)
+    for k in range(60):
+        g.step(1)
+        o.step(1)
+        np.testing.assert_array_equal(g.state().id, o.state().id)
+        assert g.counters() == o.counters(), f"hopper step {k}"
+        kg = keyed_contacts(g, case.opts.base_wall_id)
+        ko = keyed_contacts(o, case.opts.base_wall_id)
+        assert_same_contact_sets(kg, ko, f"hopper step {k}")
+    assert g.counters()["nlocal"] < case.particles.n
+    assert g.counters()["pw"] > 20
+    np.testing.assert_allclose(g.state().posR, o.state().posR, rtol=1e-11, atol=1e-15)
+
+
+def test_fixed_sphere_arguments(gpu_lib):
+    case = CASES["fixed_floor"]()
+    g = DEMSystem(case)
+    fx = case.fixed
+    with pytest.raises(SdemError) as e:      # ids must lie above the moving ids
+        g.set_fixed(beds.FixedSpheres(id=np.array([1], np.int32), ptype=fx.ptype[:1], pos=fx.pos[:1]))
+    assert e.value.code == 4
+    per = CASES["periodic_y"]()
+    c = beds.Case(per.name, per.opts, per.tables, per.walls, per.particles, fixed=beds.FixedSpheres(
+        id=np.array([10**6], np.int32), ptype=np.array([1], np.int32), pos=per.particles.posR[:1, :3] + 1e-3))
+    with pytest.raises(SdemError) as e:      # no fixed spheres with periodic directions
+        DEMSystem(c)
+    assert e.value.code == 10
+
+
 def test_unsupported_options_are_refused(gpu_lib):
     case = beds.scaled(cloud(seed=24, n=20), cs_method=2)
     with pytest.raises(SdemError) as e:
@@ -216,7 +256,7 @@ def test_periodic_history_roundtrip(gpu_lib):
     case = beds.periodic_lattice_case(800, 36, (1, 0, 1))
     o = OracleSystem(case)
     o.step(2)
-    c = beds.Case(case.name, case.opts, case.tables, case.walls, o.state(), contacts=o.contacts())
+    c = beds.Case(case.name, case.opts, case.tables, case.walls, o.state(), contacts=o.contacts(), fixed=case.fixed)
     g = DEMSystem(c)
     kg0 = keyed_contacts(g, case.opts.base_wall_id)
     ko0 = keyed_contacts(o, case.opts.base_wall_id)

@@ -61,7 +61,7 @@ def test_snapshot_before_any_step_reports_uploaded_history(gpu_lib):
     case = beds.lattice_cloud_case(600, seed=43)
     o = OracleSystem(case)
     o.step(3)
-    c = beds.Case(case.name, case.opts, case.tables, case.walls, o.state(), contacts=o.contacts())
+    c = beds.Case(case.name, case.opts, case.tables, case.walls, o.state(), contacts=o.contacts(), fixed=case.fixed)
     g = DEMSystem(c)
     out = empty_like(g)
     g.snapshot_begin(out, contacts=True)

@@ -145,3 +145,31 @@ def test_coulomb_sliding_on_floor():
     fn = abs(F[0, 1])
     assert s.counters()["pw"] == 1
     assert ft == pytest.approx(mu * fn, rel=1e-9)
+
+
+def test_rebound_on_fixed_sphere():
+    # a sphere dropped head-on onto a fixed sphere of its own type (no gravity).
+    # The pair's damping comes from the two-particle table (effective mass m/2),
+    # while the fixed sphere acts as an infinite mass, so the rebound ratio is
+    # a little above e_n (damping ratio smaller by sqrt(2))
+    e = 0.8
+    t = props.build_tables(2, [1e-3], [2500.0], [5e7], [0.3], (0.3, 0.3, 0.0, e, e), [5e7], [0.3],
+                           (0.3, 0.3, 0.0, e, e))
+    o = beds.Options(dt=2e-8, minpoint=(0, 0, 0), maxpoint=(0.01, 0.01, 0.01), gravity=(0.0, 0.0, 0.0), cf_type=2,
+                     pi_method=2, pri_method=1)
+    p = beds.new_particles(np.array([[0.005, 0.006001, 0.005]]), np.array([1]), t.radius,
+                           np.array([[0.0, -0.2, 0.0]]), 2, 1)
+    fx = beds.FixedSpheres(id=np.array([2], np.int32), ptype=np.array([1], np.int32),
+                           pos=np.array([[0.005, 0.005, 0.005]]))
+    s = OracleSystem(beds.Case("f", o, t, WallSet(), p, fixed=fx))
+    touched = False
+    for _ in range(2000):
+        s.step(100)
+        c = s.counters()["ppfix"]
+        touched = touched or c > 0
+        if touched and c == 0:
+            break
+    assert touched
+    v = s.state().linVel[0, 0]
+    assert e < v[1] / 0.2 < e + 0.1, v
+    assert abs(v[0]) < 1e-12 and abs(v[2]) < 1e-12
