@@ -47,6 +47,7 @@ extern "C" {
 
 /* ---- enums: values are the reference's (Prtcl_Parameters.f90:13-24) ---- */
 #define SDEM_CSM_NBS_MUNJIZA   1
+#define SDEM_CSM_HRCHL         2   /* hierarchical NBS Munjiza (Prtcl_Hrchl_Munjiza.f90) */
 #define SDEM_CFT_LSD           1
 #define SDEM_CFT_NLIN          2   /* Hertz-Mindlin */
 #define SDEM_CTM_CONSTANT      1
@@ -95,7 +96,8 @@ extern "C" {
 #define SDEM_CNT_NLOCAL    5  /* particles in the domain after the step                   */
 #define SDEM_CNT_ITER      6  /* iterNumber after the last step                           */
 #define SDEM_CNT_NEXTWALL  7  /* Next_iter_update of the near-wall list                   */
-#define SDEM_CNT_SIZE      8
+#define SDEM_CNT_CNSV_CROSS 8 /* lvl_num_cnsv_cntct: cross-level candidates (CS_Method 2)  */
+#define SDEM_CNT_SIZE      9
 
 /* Configuration: the &DEMOptions fields the hot path reads
  * (Prtcl_Parameters.f90:45-95), plus the GPU's own capacities. */
@@ -106,7 +108,7 @@ typedef struct sdem_cfg {
   int    cf_type;               /* SDEM_CFT_*                                        */
   int    ct_model;              /* SDEM_CTM_*                                        */
   int    pi_method, pri_method; /* SDEM_PIM_*                                        */
-  int    cs_method;             /* SDEM_CSM_NBS_MUNJIZA                              */
+  int    cs_method;             /* SDEM_CSM_NBS_MUNJIZA or SDEM_CSM_HRCHL            */
   int    cntct_list_size;       /* CntctList_Size (contact records = size * mlocal)  */
   int    base_wall_id;          /* Base_wall_id                                      */
   int    wall_max_update_iter;  /* Wall_max_update_iter                              */
@@ -119,6 +121,7 @@ typedef struct sdem_cfg {
   double cs_ratio;              /* Prtcl_cs_ratio                                    */
   double wall_neighbor_ratio;   /* Wall_neighbor_ratio                               */
   int    n_fixed_capacity;      /* numPrtclFix: most fixed spheres (0 = none)        */
+  int    cs_num_levels;         /* CS_numlvls of the hierarchical search (0: from the diameter ratio) */
 } sdem_cfg;
 
 typedef struct sdem_h sdem_h;

@@ -153,7 +153,7 @@ class OracleSystem:
         return o[:m], q[:m], t[:m], v[:m]
 
     def counters(self) -> dict:
-        out = np.zeros(8, np.int32)
+        out = np.zeros(9, np.int32)
         self._check(self.lib.orc_counters(self.h, iptr(out)))
         return dict(zip(CNT_NAMES, (int(x) for x in out)))
 

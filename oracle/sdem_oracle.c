@@ -76,6 +76,17 @@ typedef struct {
   int bothSide, isInfinite, wall_id, wall_Type;
 } wall_t;
 
+/* one level of the hierarchical search (type lvl_Munjiza,
+ * Prtcl_Hrchl_Munjiza.f90:24-47); list heads keep the reference's bounds */
+struct hlvl {
+  int lvl, lvl_multiple, nx, ny, nz;
+  double cell_len;
+  int *HeadY, *HeadX0, *HeadX, *HeadX2;   /* (0:ny+1), (0:nx+1) */
+  int curr_xList_ind, curr_xList2_ind;
+  int *HeadZ0, *HeadZ, *HeadZ2;           /* (0:2, 0:nz+1) as [m*(nz+2) + iz] */
+  int curr_zList0_ind[3], curr_zList_ind[3], curr_zList2_ind[3];
+};
+
 typedef struct orc {
   sdem_cfg cfg;
   int err;
@@ -101,6 +112,11 @@ typedef struct orc {
   double cell_len, xst_cs, yst_cs, zst_cs;
   int nx, ny, nz, mbox;
   int *bx, *by, *bz, *NextX, *NextY, *NextZ, *HeadY, *HeadX, *HeadX0;
+  /* hierarchical NBS (CS_Method=2, Prtcl_Hrchl_Munjiza.f90): levels 1-based */
+  int num_lvls;
+  struct hlvl* lvls;
+  int* type_level;          /* CS_Hrchl_level of each type (0-based type index) */
+  long long lvl_num_cnsv;   /* lvl_num_cnsv_cntct: cross-level candidates */
   /* fixed particles (GPFix_*, PIO_ReadFixedCoord, Prtcl_IOAndVisu.f90:164-291),
    * 1-based; in the search they take indices 1..nFixed, before the locals */
   int nFixed;
@@ -307,6 +323,8 @@ static void init_nbsm(orc* h) {
   for (int i = 0; i <= mb; i++) h->NextX[i] = h->NextY[i] = h->NextZ[i] = -1;
 }
 
+static void init_hrchl(orc* h);
+
 int orc_set_types(orc* h, int nT, const double* radius, const double* mass,
                   const double* inertia, const double* bnry_pp, int nWT,
                   const double* bnry_pw) {
@@ -325,6 +343,7 @@ int orc_set_types(orc* h, int nT, const double* radius, const double* mass,
   memcpy(h->bpp, bnry_pp, (size_t)nT * nT * SDEM_BP_SIZE * sizeof(double));
   memcpy(h->bpw, bnry_pw, (size_t)nT * nWT * SDEM_BP_SIZE * sizeof(double));
   init_nbsm(h);
+  if (h->cfg.cs_method == SDEM_CSM_HRCHL) init_hrchl(h);
   /* InitContactSearchPW, Prtcl_ContactSearchPW.f90:74-75 */
   double maxR = radius[0];
   for (int t = 1; t < nT; t++) if (radius[t] > maxR) maxR = radius[t];
@@ -344,6 +363,8 @@ int orc_set_fixed(orc* h, int nfix, const int* id, const int* ptype, const doubl
   if (!h->have_types) return fail(h, SDEM_E_ARG, "orc_set_fixed: call orc_set_types first");
   if (h->cfg.periodic[0] || h->cfg.periodic[1] || h->cfg.periodic[2])
     return fail(h, SDEM_E_UNSUPPORTED, "orc_set_fixed: the fixed spheres' periodic images are not restated");
+  if (h->cfg.cs_method == SDEM_CSM_HRCHL)
+    return fail(h, SDEM_E_UNSUPPORTED, "orc_set_fixed: the hierarchical search has no fixed-sphere branch");
   free(h->FixId); free(h->FixType); free(h->FixPosR);
   h->FixId = (int*)xcalloc((size_t)nfix + 1, sizeof(int));
   h->FixType = (int*)xcalloc((size_t)nfix + 1, sizeof(int));
@@ -1112,6 +1133,336 @@ static int nbsm_contact_search(orc* h) {
   return h->err;
 }
 
+/* ---- hierarchical NBS (CS_Method = 2), Prtcl_Hrchl_Munjiza.f90 ------------
+ * A line-by-line restatement, list quirks included: BuildXList2 records its
+ * row in curr_xList_ind (:453), so curr_xList2_ind stays -1 and the
+ * "already built" test of BuildXList2 never holds.  Search indices: locals
+ * 1..nlocal, ghosts after them (no fixed particles in this search). */
+#define HLZ(L, arr, m, iz) ((L)->arr[(m) * ((L)->nz + 2) + (iz)])
+
+static void hlvl_free(struct hlvl* L) {
+  free(L->HeadY); free(L->HeadX0); free(L->HeadX); free(L->HeadX2);
+  free(L->HeadZ0); free(L->HeadZ); free(L->HeadZ2);
+}
+
+/* Init_Munjiza_Hrchl, :78-218.  Every type of the table counts as populated
+ * (nPrtcl_in_Bin > 0): a level without particles has empty lists and finds
+ * nothing, so dropping it or keeping it gives the same contacts. */
+static void init_hrchl(orc* h) {
+  for (int k = 1; k <= h->num_lvls; k++) hlvl_free(&h->lvls[k]);
+  free(h->lvls); free(h->type_level);
+  double maxD = 0.0, minD = 0.0;
+  for (int t = 0; t < h->nT; t++) {
+    double d = 2.0 * h->Radius[t];
+    if (t == 0 || d > maxD) maxD = d;
+    if (t == 0 || d < minD) minD = d;
+  }
+  int dmax_min = (int)(maxD / minD);
+  int numLevels;
+  if (h->cfg.cs_num_levels > 0) numLevels = h->cfg.cs_num_levels;
+  else if (dmax_min <= 1) numLevels = 1;
+  else if (dmax_min <= 3) numLevels = 2;
+  else if (dmax_min <= 7) numLevels = 3;
+  else if (dmax_min <= 15) numLevels = 4;
+  else if (dmax_min <= 31) numLevels = 5;
+  else numLevels = 6;
+  h->type_level = (int*)xcalloc(h->nT, sizeof(int));
+  h->lvls = (struct hlvl*)xcalloc((size_t)numLevels + 1, sizeof(struct hlvl));
+  double cell_len = h->cfg.cs_ratio * maxD;
+  double xst = h->cfg.dom_min[0] - cell_len * 1.05, yst = h->cfg.dom_min[1] - cell_len * 1.05;
+  double zst = h->cfg.dom_min[2] - cell_len * 1.05;
+  double xed = h->cfg.dom_max[0] + cell_len * 1.05, yed = h->cfg.dom_max[1] + cell_len * 1.05;
+  double zed = h->cfg.dom_max[2] + cell_len * 1.05;
+  h->xst_cs = xst; h->yst_cs = yst; h->zst_cs = zst;
+  int nx = (int)((xed - xst) / cell_len) + 1, ny = (int)((yed - yst) / cell_len) + 1;
+  int nz = (int)((zed - zst) / cell_len) + 1;
+  int id_level = 0;
+  double maxD_lvl = maxD;
+  for (int idh = 1; idh <= numLevels; idh++) {
+    double minD_lvl = maxD_lvl / 2.0;
+    if (idh == numLevels) minD_lvl = 0.0;
+    int populated = 0;
+    for (int t = 0; t < h->nT; t++) {
+      double d = 2.0 * h->Radius[t];
+      if (d > minD_lvl && (idh == 1 || d <= maxD_lvl)) populated = 1;
+    }
+    if (populated) {
+      id_level++;
+      for (int t = 0; t < h->nT; t++) {
+        double d = 2.0 * h->Radius[t];
+        if (d > minD_lvl && (idh == 1 || d <= maxD_lvl)) h->type_level[t] = id_level;
+      }
+      struct hlvl* L = &h->lvls[id_level];
+      L->lvl = id_level;
+      L->lvl_multiple = idh;
+      L->nx = nx; L->ny = ny; L->nz = nz;
+      L->cell_len = cell_len;
+      L->HeadY = (int*)xcalloc((size_t)ny + 2, sizeof(int));
+      L->HeadX0 = (int*)xcalloc((size_t)nx + 2, sizeof(int));
+      L->HeadX = (int*)xcalloc((size_t)nx + 2, sizeof(int));
+      L->HeadX2 = (int*)xcalloc((size_t)nx + 2, sizeof(int));
+      L->HeadZ0 = (int*)xcalloc((size_t)3 * (nz + 2), sizeof(int));
+      L->HeadZ = (int*)xcalloc((size_t)3 * (nz + 2), sizeof(int));
+      L->HeadZ2 = (int*)xcalloc((size_t)3 * (nz + 2), sizeof(int));
+      for (int i = 0; i < ny + 2; i++) L->HeadY[i] = -1;
+      for (int i = 0; i < nx + 2; i++) L->HeadX0[i] = L->HeadX[i] = L->HeadX2[i] = -1;
+      for (int i = 0; i < 3 * (nz + 2); i++) L->HeadZ0[i] = L->HeadZ[i] = L->HeadZ2[i] = -1;
+      L->curr_xList_ind = -1;
+      L->curr_xList2_ind = -1;
+      for (int m = 0; m < 3; m++) L->curr_zList0_ind[m] = L->curr_zList_ind[m] = L->curr_zList2_ind[m] = -1;
+    }
+    nx *= 2; ny *= 2; nz *= 2;
+    maxD_lvl = minD_lvl;
+    cell_len = cell_len / 2.0;
+  }
+  h->num_lvls = id_level;
+}
+
+/* NBSMH_clcBoxIndex_and_BuildYList, :247-336 */
+static int hbox_and_ylist(orc* h) {
+  int n12 = h->nlocal + h->nGhost;
+  if (n12 >= h->mbox) grow_nbs(h);
+  for (int k = 1; k <= h->num_lvls; k++) {
+    struct hlvl* L = &h->lvls[k];
+    for (int i = 0; i < L->ny + 2; i++) L->HeadY[i] = -1;
+  }
+  for (int i = 1; i <= n12; i++) {
+    r4 P;
+    int t;
+    if (i <= h->nlocal) { P = h->PosR[i]; t = h->pType[i]; }
+    else { P = h->GhostP_PosR[i - h->nlocal]; t = h->GhostP_pType[i - h->nlocal]; }
+    double rpdx = P.x - h->xst_cs, rpdy = P.y - h->yst_cs, rpdz = P.z - h->zst_cs;
+    struct hlvl* L = &h->lvls[h->type_level[t - 1]];
+    double cl = L->cell_len;
+    h->bx[i] = (int)floor(rpdx / cl) + 1;
+    int iy = (int)floor(rpdy / cl) + 1;
+    h->by[i] = iy;
+    h->bz[i] = (int)floor(rpdz / cl) + 1;
+    if (h->bx[i] < 1 || h->bx[i] > L->nx || iy < 1 || iy > L->ny || h->bz[i] < 1 || h->bz[i] > L->nz)
+      return fail(h, SDEM_E_GRID, "NBSMH_clcBoxIndex: particle outside the search grid");
+    h->NextY[i] = L->HeadY[iy];
+    L->HeadY[iy] = i;
+  }
+  return 0;
+}
+
+static void hbuild_xlist(orc* h, struct hlvl* L, int iy) { /* :341-361 */
+  if (iy == L->curr_xList_ind) return;
+  for (int i = 0; i < L->nx + 2; i++) L->HeadX[i] = -1;
+  L->curr_xList_ind = iy;
+  int n = L->HeadY[iy];
+  while (n != -1) {
+    int ix = h->bx[n];
+    h->NextX[n] = L->HeadX[ix];
+    L->HeadX[ix] = n;
+    n = h->NextY[n];
+  }
+}
+
+static void hbuild_xlist2(orc* h, struct hlvl* L, int iy) { /* :366-386 */
+  if (iy == L->curr_xList2_ind) return;
+  for (int i = 0; i < L->nx + 2; i++) L->HeadX2[i] = -1;
+  L->curr_xList_ind = iy;   /* the reference records the row here (:380) */
+  int n = L->HeadY[iy];
+  while (n != -1) {
+    int ix = h->bx[n];
+    h->NextX[n] = L->HeadX2[ix];
+    L->HeadX2[ix] = n;
+    n = h->NextY[n];
+  }
+}
+
+/* BuildZList0 / BuildZList / BuildZList2 (:391-475): column ix+m-1 of the
+ * row below / this row / the row above */
+static void hbuild_zl(orc* h, struct hlvl* L, int* head_x, int* head_z, int* curr, int ix, int m, int lcheck) {
+  if (lcheck && ix == curr[m]) return;
+  for (int iz = 0; iz < L->nz + 2; iz++) head_z[m * (L->nz + 2) + iz] = -1;
+  curr[m] = ix;
+  int n = head_x[ix + m - 1];
+  while (n != -1) {
+    int iz = h->bz[n];
+    h->NextZ[n] = head_z[m * (L->nz + 2) + iz];
+    head_z[m * (L->nz + 2) + iz] = n;
+    n = h->NextX[n];
+  }
+}
+
+/* NBSMH_FineSearch, :709-753 (pid1 the partner, pid2 the target) */
+static void hfine_search(orc* h, int pid1, int pid2) {
+  const int nl = h->nlocal;
+  double dx, dy, dz, dr, d2sum, dr2, ovrlp;
+  if (pid1 > nl || pid2 > nl) {
+    const int gid = pid1 > nl ? pid1 - nl : pid2 - nl;
+    const int loc = pid1 > nl ? pid2 : pid1;
+    r4 A = pid1 > nl ? h->GhostP_PosR[gid] : h->PosR[pid1];
+    r4 B = pid1 > nl ? h->PosR[pid2] : h->GhostP_PosR[gid];
+    dr = A.w + B.w;
+    dr2 = dr * dr;
+    dx = A.x - B.x;
+    d2sum = dx * dx;
+    if (d2sum > dr2) return;
+    dy = A.y - B.y;
+    d2sum = dy * dy + d2sum;
+    if (d2sum > dr2) return;
+    dz = A.z - B.z;
+    d2sum = dz * dz + d2sum;
+    if (d2sum > dr2) return;
+    ovrlp = dr - sqrt(d2sum);
+    add_contact_ppg(h, loc, gid, ovrlp);
+    return;
+  }
+  dr = h->PosR[pid1].w + h->PosR[pid2].w;
+  dr2 = dr * dr;
+  dx = h->PosR[pid1].x - h->PosR[pid2].x;
+  d2sum = dx * dx;
+  if (d2sum > dr2) return;
+  dy = h->PosR[pid1].y - h->PosR[pid2].y;
+  d2sum = dy * dy + d2sum;
+  if (d2sum > dr2) return;
+  dz = h->PosR[pid1].z - h->PosR[pid2].z;
+  d2sum = dz * dz + d2sum;
+  if (d2sum > dr2) return;
+  ovrlp = dr - sqrt(d2sum);
+  if (h->id[pid1] < h->id[pid2]) add_contact_pp(h, pid1, pid2, ovrlp);
+  else add_contact_pp(h, pid2, pid1, ovrlp);
+}
+
+/* NBSMH_LoopNBSMask, :601-704 */
+static void hloop_nbs_mask(orc* h, struct hlvl* L, int iz) {
+  const int nl = h->nlocal;
+  int m = HLZ(L, HeadZ, 1, iz);
+  while (m != -1) {
+    const int ghost = m > nl;
+#define HVISIT(start) do { int n_ = (start); while (n_ != -1) { if (!ghost || n_ <= nl) { hfine_search(h, n_, m); h->num_Cnsv++; } n_ = h->NextZ[n_]; } } while (0)
+    HVISIT(h->NextZ[m]);
+    HVISIT(HLZ(L, HeadZ, 1, iz - 1));
+    for (int i = -1; i <= 1; i++) HVISIT(HLZ(L, HeadZ, 0, iz + i));
+    for (int lx = 0; lx <= 2; lx++)
+      for (int i = -1; i <= 1; i++) HVISIT(HLZ(L, HeadZ0, lx, iz + i));
+#undef HVISIT
+    m = h->NextZ[m];
+  }
+}
+
+/* NBSMH_Loop_CrossMask, :762-863: 27 cells of the coarser level (row below,
+ * this row, row above; columns crs_ix-1..+1; cells crs_iz-1..+1) */
+static void hloop_cross(orc* h, struct hlvl* L, int iz, int crs_iz, struct hlvl* X) {
+  const int nl = h->nlocal;
+  int m = HLZ(L, HeadZ, 1, iz);
+  while (m != -1) {
+    const int ghost = m > nl;
+#define XVISIT(start) do { int n_ = (start); while (n_ != -1) { if (!ghost || n_ <= nl) { hfine_search(h, n_, m); h->lvl_num_cnsv++; } n_ = h->NextZ[n_]; } } while (0)
+    for (int lx = 0; lx <= 2; lx++)
+      for (int l = -1; l <= 1; l++) XVISIT(HLZ(X, HeadZ0, lx, crs_iz + l));
+    for (int lx = 0; lx <= 2; lx++)
+      for (int l = -1; l <= 1; l++) XVISIT(HLZ(X, HeadZ, lx, crs_iz + l));
+    for (int lx = 0; lx <= 2; lx++)
+      for (int l = -1; l <= 1; l++) XVISIT(HLZ(X, HeadZ2, lx, crs_iz + l));
+#undef XVISIT
+    m = h->NextZ[m];
+  }
+}
+
+static void hcopy(int* dst, const int* src, int n) { memcpy(dst, src, sizeof(int) * (size_t)n); }
+
+/* OneLevelBroadSearch, :480-596 */
+static void one_level(orc* h, struct hlvl* B) {
+  const int zs = B->nz + 2;
+  for (int i = 0; i < B->nx + 2; i++) B->HeadX0[i] = -1;
+  for (int iy = 1; iy <= B->ny; iy++) {
+    hbuild_xlist(h, B, iy);
+    for (int idh = B->lvl - 1; idh >= 1; idh--) {
+      struct hlvl* X = &h->lvls[idh];
+      int coe = 1 << (B->lvl_multiple - X->lvl_multiple);
+      int crs_y = (iy - 1) / coe + 1;
+      if (crs_y == 1) {
+        for (int i = 0; i < X->nx + 2; i++) X->HeadX0[i] = -1;
+        hbuild_xlist(h, X, 1);
+      }
+      hbuild_xlist2(h, X, crs_y + 1);
+    }
+    if (B->HeadY[iy] != -1) {
+      for (int iz = 0; iz < zs; iz++) { HLZ(B, HeadZ, 0, iz) = -1; HLZ(B, HeadZ0, 0, iz) = -1; }
+      hbuild_zl(h, B, B->HeadX0, B->HeadZ0, B->curr_zList0_ind, 1, 1, 0);
+      for (int ix = 1; ix <= B->nx; ix++) {
+        hbuild_zl(h, B, B->HeadX, B->HeadZ, B->curr_zList_ind, ix, 1, 0);
+        hbuild_zl(h, B, B->HeadX0, B->HeadZ0, B->curr_zList0_ind, ix, 2, 0);
+        for (int idh = B->lvl - 1; idh >= 1; idh--) {
+          struct hlvl* X = &h->lvls[idh];
+          int coe = 1 << (B->lvl_multiple - X->lvl_multiple);
+          int crs_x = (ix - 1) / coe + 1;
+          const int xzs = X->nz + 2;
+          if (crs_x == 1) {
+            for (int iz = 0; iz < xzs; iz++) { HLZ(X, HeadZ0, 0, iz) = -1; HLZ(X, HeadZ, 0, iz) = -1; HLZ(X, HeadZ2, 0, iz) = -1; }
+            hbuild_zl(h, X, X->HeadX0, X->HeadZ0, X->curr_zList0_ind, crs_x, 1, 1);
+            hbuild_zl(h, X, X->HeadX, X->HeadZ, X->curr_zList_ind, crs_x, 1, 1);
+            hbuild_zl(h, X, X->HeadX2, X->HeadZ2, X->curr_zList2_ind, crs_x, 1, 1);
+          }
+          hbuild_zl(h, X, X->HeadX0, X->HeadZ0, X->curr_zList0_ind, crs_x, 2, 1);
+          hbuild_zl(h, X, X->HeadX, X->HeadZ, X->curr_zList_ind, crs_x, 2, 1);
+          hbuild_zl(h, X, X->HeadX2, X->HeadZ2, X->curr_zList2_ind, crs_x, 2, 1);
+        }
+        if (B->HeadX[ix] != -1) {
+          for (int iz = 1; iz <= B->nz; iz++) {
+            hloop_nbs_mask(h, B, iz);
+            for (int idh = B->lvl - 1; idh >= 1; idh--) {
+              struct hlvl* X = &h->lvls[idh];
+              int coe = 1 << (B->lvl_multiple - X->lvl_multiple);
+              hloop_cross(h, B, iz, (iz - 1) / coe + 1, X);
+            }
+          }
+        }
+        hcopy(&HLZ(B, HeadZ, 0, 0), &HLZ(B, HeadZ, 1, 0), zs);
+        hcopy(&HLZ(B, HeadZ0, 0, 0), &HLZ(B, HeadZ0, 1, 0), zs);
+        hcopy(&HLZ(B, HeadZ0, 1, 0), &HLZ(B, HeadZ0, 2, 0), zs);
+        for (int idh = B->lvl - 1; idh >= 1; idh--) {
+          struct hlvl* X = &h->lvls[idh];
+          int coe = 1 << (B->lvl_multiple - X->lvl_multiple);
+          if (ix % coe == 0) {
+            const int xzs = X->nz + 2;
+            hcopy(&HLZ(X, HeadZ0, 0, 0), &HLZ(X, HeadZ0, 1, 0), xzs);
+            hcopy(&HLZ(X, HeadZ0, 1, 0), &HLZ(X, HeadZ0, 2, 0), xzs);
+            X->curr_zList0_ind[0] = X->curr_zList0_ind[1];
+            X->curr_zList0_ind[1] = X->curr_zList0_ind[2];
+            hcopy(&HLZ(X, HeadZ, 0, 0), &HLZ(X, HeadZ, 1, 0), xzs);
+            hcopy(&HLZ(X, HeadZ, 1, 0), &HLZ(X, HeadZ, 2, 0), xzs);
+            X->curr_zList_ind[0] = X->curr_zList_ind[1];
+            X->curr_zList_ind[1] = X->curr_zList_ind[2];
+            hcopy(&HLZ(X, HeadZ2, 0, 0), &HLZ(X, HeadZ2, 1, 0), xzs);
+            hcopy(&HLZ(X, HeadZ2, 1, 0), &HLZ(X, HeadZ2, 2, 0), xzs);
+            X->curr_zList2_ind[0] = X->curr_zList2_ind[1];
+            X->curr_zList2_ind[1] = X->curr_zList2_ind[2];
+          }
+        }
+        if (h->err) return;
+      }
+    }
+    hcopy(B->HeadX0, B->HeadX, B->nx + 2);
+    for (int idh = B->lvl - 1; idh >= 1; idh--) {
+      struct hlvl* X = &h->lvls[idh];
+      int coe = 1 << (B->lvl_multiple - X->lvl_multiple);
+      if (iy % coe == 0) {
+        hcopy(X->HeadX0, X->HeadX, X->nx + 2);
+        hcopy(X->HeadX, X->HeadX2, X->nx + 2);
+        X->curr_xList_ind = X->curr_xList2_ind;
+      }
+    }
+  }
+}
+
+/* NBSMH_ContactSearch, :227-242 */
+static int nbsmh_contact_search(orc* h) {
+  h->num_Cnsv = 0;
+  h->lvl_num_cnsv = 0;
+  if (h->nlocal == 0) return 0;
+  if (hbox_and_ylist(h)) return h->err;
+  for (int idh = h->num_lvls; idh >= 1; idh--) {
+    one_level(h, &h->lvls[idh]);
+    if (h->err) return h->err;
+  }
+  return 0;
+}
+
 /* ---- plane walls (Prtcl_Geometry.f90) ---------------------------------- */
 static int pw_is_in_plane(r3 p1, r3 p2, r3 p3, r3 p4, r3 cp) { /* :185-221 */
   r3 p1p = r3sub(p1, cp), p2p = r3sub(p2, cp), p3p = r3sub(p3, cp), p4p = r3sub(p4, cp);
@@ -1398,7 +1749,7 @@ int orc_step(orc* h, int nsteps) {
     for (int i = 1; i <= h->nlocal; i++) { h->F[i] = zero_r3; h->T[i] = zero_r3; }
     cl_pre_iteration(h);
     comm_for_cntct(h);
-    if (nbsm_contact_search(h)) return h->err;
+    if ((h->cfg.cs_method == SDEM_CSM_HRCHL ? nbsmh_contact_search(h) : nbsm_contact_search(h))) return h->err;
     find_contacts_pw(h);
     if (h->err) return h->err;
     clc_acceleration(h);
@@ -1492,6 +1843,7 @@ int orc_counters(orc* h, int* out) {
   out[SDEM_CNT_NLOCAL] = h->nlocal;
   out[SDEM_CNT_ITER] = h->iterNumber;
   out[SDEM_CNT_NEXTWALL] = h->Next_iter_update;
+  out[SDEM_CNT_CNSV_CROSS] = (int)h->lvl_num_cnsv;
   return 0;
 }
 
@@ -1505,6 +1857,8 @@ void orc_grid(orc* h, double* cell_len, double* origin, int* dims) {
 void orc_destroy(orc* h) {
   if (!h) return;
   free(h->FixId); free(h->FixType); free(h->FixPosR);
+  for (int k = 1; k <= h->num_lvls; k++) hlvl_free(&h->lvls[k]);
+  free(h->lvls); free(h->type_level);
   free(h->id); free(h->pType); free(h->usrMark); free(h->PosR);
   free(h->linVel); free(h->linAcc); free(h->rotVel); free(h->rotAcc);
   free(h->theta); free(h->F); free(h->T);

@@ -28,6 +28,7 @@ class Options:
     periodic: Tuple[int, int, int] = (0, 0, 0)
     cs_ratio: float = 1.0
     cs_method: int = 1
+    cs_num_levels: int = 0
     cf_type: int = props.CFT_LSD
     ct_model: int = 1
     pi_method: int = 1

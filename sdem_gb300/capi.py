@@ -21,7 +21,7 @@ SDEM_OK = 0
 ERRORS = {1: "SDEM_E_ARG", 2: "SDEM_E_CUDA", 3: "SDEM_E_CL_FULL", 4: "SDEM_E_BAD_ID", 5: "SDEM_E_NCV20",
           6: "SDEM_E_GRID", 7: "SDEM_E_TIMEOUT", 8: "SDEM_E_CAPACITY", 9: "SDEM_E_NOMEM",
           10: "SDEM_E_UNSUPPORTED"}
-CNT_NAMES = ("pp", "ppg", "ppfix", "pw", "cnsv", "nlocal", "iter", "next_wall_update")
+CNT_NAMES = ("pp", "ppg", "ppfix", "pw", "cnsv", "nlocal", "iter", "next_wall_update", "cnsv_cross")
 
 EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls", "sdem_upload_particles",
             "sdem_upload_contacts", "sdem_step", "sdem_step_async", "sdem_get_stream",
@@ -52,7 +52,7 @@ class SdemCfg(C.Structure):
         ("wall_max_update_iter", C.c_int), ("periodic", C.c_int * 3), ("quirk_ab2_rot", C.c_int),
         ("max_contacts_per_particle", C.c_int), ("dt", C.c_double), ("gravity", C.c_double * 3),
         ("dom_min", C.c_double * 3), ("dom_max", C.c_double * 3), ("cs_ratio", C.c_double),
-        ("wall_neighbor_ratio", C.c_double), ("n_fixed_capacity", C.c_int),
+        ("wall_neighbor_ratio", C.c_double), ("n_fixed_capacity", C.c_int), ("cs_num_levels", C.c_int),
     ]
 
 
@@ -85,6 +85,7 @@ def cfg_from_case(case: Case, n_capacity: Optional[int] = None, max_gid: Optiona
     c.cs_ratio = o.cs_ratio
     c.wall_neighbor_ratio = o.wall_neighbor_ratio
     c.n_fixed_capacity = int(case.fixed.n) if case.fixed is not None else 0
+    c.cs_num_levels = int(getattr(o, "cs_num_levels", 0))
     return c
 
 
@@ -346,7 +347,7 @@ class DEMSystem:
         self._check(self.lib.sdem_check_restart_limit(self.h))
 
     def counters(self) -> dict:
-        out = np.zeros(8, np.int32)
+        out = np.zeros(9, np.int32)
         self._check(self.lib.sdem_counters(self.h, iptr(out)))
         return dict(zip(CNT_NAMES, (int(x) for x in out)))
 

@@ -68,6 +68,17 @@ constexpr int kOutCap = 4096;     // out-of-domain deletions per step
 constexpr int kScanTile = 4096;   // elements per scan block (1024 threads x 4)
 constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact records
 constexpr int kChunks = 2;        // search/force pipeline chunks per step
+constexpr int kMaxLevels = 6;     // hierarchical search levels (Init_Munjiza_Hrchl caps at 6)
+
+// One level of the hierarchical search: a grid of cells 2^(mult-1) times
+// finer than the base grid; its cells sit at [base, base + nx*ny*nz) of the
+// concatenated cell arrays (the finest level first, the order of the search).
+struct LevelGrid {
+  int nx, ny, nz, mult;
+  long long base;
+  double cell;
+  float cellf;
+};
 constexpr int kImgFlag = 1 << 30; // c_ogid bit: a pair with a periodic image (ids < 2^30)
 
 // Phases of one step, for the optional per-phase timing (sdem_profile_*).
@@ -85,6 +96,10 @@ struct Dev {
   // periodic images: ghosts live at indices [n, n + ng) of the search arrays
   // (gid, ptype, posr, vel0, rv0 and the binning/row arrays, stride nall)
   int nall, nall_launch, gcap;
+  // hierarchical search (CS_Method 2): levels, 0 = coarsest
+  int hier, nlvl;
+  LevelGrid lv[kMaxLevels];
+  const int* type_lvl;   // level of each type
   // fixed spheres: appended to the search arrays after the images every step
   int nfix;
   const int *fix_gid, *fix_ptype;
@@ -414,18 +429,29 @@ __global__ void k_bin(Dev d) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= *d.nt) return;
   const dbl4 P = d.posr[p];
+  // the grid of the particle's level (hierarchical search: by type,
+  // NBSMH_clcBoxIndex_and_BuildYList, Prtcl_Hrchl_Munjiza.f90:247-336)
+  double cell = d.cell;
+  int nx = d.nx, ny = d.ny, nz = d.nz;
+  long long base = 0;
+  if (d.hier) {
+    const LevelGrid& G = d.lv[d.type_lvl[d.ptype[p] - 1]];
+    cell = G.cell;
+    nx = G.nx; ny = G.ny; nz = G.nz;
+    base = G.base;
+  }
   // floor((x - x0) / cell_len), the quotient IEEE-rounded; division and
   // floor on the integer pipes.  The reference's index is this + 1.
-  const fpi::Divisor dc = fpi::divisor(d.cell);
-  const int fx = fpi::floor_in_range(fpi::div_by(P.x - d.x0, dc), d.nx);
-  const int fy = fpi::floor_in_range(fpi::div_by(P.y - d.y0, dc), d.ny);
-  const int fz = fpi::floor_in_range(fpi::div_by(P.z - d.z0, dc), d.nz);
+  const fpi::Divisor dc = fpi::divisor(cell);
+  const int fx = fpi::floor_in_range(fpi::div_by(P.x - d.x0, dc), nx);
+  const int fy = fpi::floor_in_range(fpi::div_by(P.y - d.y0, dc), ny);
+  const int fz = fpi::floor_in_range(fpi::div_by(P.z - d.z0, dc), nz);
   if (fx < 0 || fy < 0 || fz < 0) {
     raise(d, SDEM_E_GRID, p);
     d.cell_of[p] = -1;
     return;
   }
-  long long key = ((long long)fy * d.nx + (long long)fx) * d.nz + (long long)fz;
+  long long key = base + ((long long)fy * nx + (long long)fx) * nz + (long long)fz;
   d.cell_of[p] = (int)key;
   d.tmp_rank[p] = atomicAdd(&d.cell_cnt[key], 1);
 }
@@ -461,10 +487,18 @@ __global__ void k_cellorder(Dev d) {
   dbl4 P = d.posr[p];
   // single-precision copy relative to the particle's own cell corner: all
   // values are below one cell, so their rounding error is ~cell*2^-24
-  const int cz = key % d.nz, cr = key / d.nz;
-  const int cx = cr % d.nx, cy = cr / d.nx;
-  d.spos[a + rank] = make_float4((float)(P.x - (d.x0 + (double)cx * d.cell)), (float)(P.y - (d.y0 + (double)cy * d.cell)),
-                                 (float)(P.z - (d.z0 + (double)cz * d.cell)), (float)P.w);
+  int lk = key, lnx = d.nx, lnz = d.nz;
+  double lcell = d.cell;
+  if (d.hier) {
+    const LevelGrid& G = d.lv[d.type_lvl[d.ptype[p] - 1]];
+    lk = (int)(key - G.base);
+    lnx = G.nx; lnz = G.nz;
+    lcell = G.cell;
+  }
+  const int cz = lk % lnz, cr = lk / lnz;
+  const int cx = cr % lnx, cy = cr / lnx;
+  d.spos[a + rank] = make_float4((float)(P.x - (d.x0 + (double)cx * lcell)), (float)(P.y - (d.y0 + (double)cy * lcell)),
+                                 (float)(P.z - (d.z0 + (double)cz * lcell)), (float)P.w);
 }
 
 // ---------------------------------------------------------------------------
@@ -476,7 +510,7 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_e
   int s = s_begin + blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = *d.nt;
   const int nloc = *d.n;
-  unsigned long long cand = 0;
+  unsigned long long cand = 0, cand_x = 0;
   if (s < s_end) {
     if (s >= nt) {
       d.row_cnt[s] = 0;
@@ -485,11 +519,23 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_e
       // a periodic image as target pairs with local particles only
       // (LoopNBSMask, Prtcl_NBS_Munjiza.f90:358-405 -> FineSearch3(n, m))
       const bool m_img = m >= nloc;
-      const int key = d.cell_of[m];
-      const int iz = key % d.nz;
-      const int rest = key / d.nz;
-      const int ix = rest % d.nx;
-      const int iy = rest / d.nx;
+      // the target's grid: the base grid, or its level's (hierarchical search)
+      int lvl = 0, nx = d.nx, nz = d.nz;
+      long long lbase = 0;
+      float cellf = d.cellf;
+      if (d.hier) {
+        lvl = d.type_lvl[d.ptype[m] - 1];
+        const LevelGrid& G = d.lv[lvl];
+        nx = G.nx;
+        nz = G.nz;
+        lbase = G.base;
+        cellf = G.cellf;
+      }
+      const int key = (int)(d.cell_of[m] - lbase);
+      const int iz = key % nz;
+      const int rest = key / nz;
+      const int ix = rest % nx;
+      const int iy = rest / nx;
       const float4 Pf = d.spos[s];
       const dbl4 Pm = d.posr[m];
       const float margin = d.pf_margin;
@@ -501,10 +547,10 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_e
       // only candidates inside the band run the FP64 test here.  FP64 work left
       // in this divergent loop would occupy the FP64 pipe with one or two lanes.
       // (ox, oy, oz): target cell corner minus candidate cell corner (0 or one cell)
-      auto test = [&](int t, float ox, float oy, float oz) {
+      auto test = [&](int t, float ox, float oy, float oz, unsigned long long& ctr) {
         if (m_img) {
           if (d.sorted[t] >= nloc) return;   // image-image pairs are not searched
-          cand++;
+          ctr++;
         }
         const float4 Qf = d.spos[t];
         const float fx = (Pf.x - Qf.x) + ox, fy = (Pf.y - Qf.y) + oy, fz = (Pf.z - Qf.z) + oz;
@@ -545,8 +591,7 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_e
       // reference's order.  The three cells iz-1..iz+1 of one (ix, iy) column
       // are consecutive in the sort, so a column is one range with two inner
       // boundaries; cells outside the grid are empty ranges.
-      const int nx = d.nx, nz = d.nz;
-      const int* __restrict__ cs = d.cell_start;
+      const int* __restrict__ cs = d.cell_start + lbase;
       const int tail_end = cs[key + 1];
       const int own_lo = iz > 0 ? cs[key - 1] : 0, own_hi = iz > 0 ? cs[key] : 0;   // cell (ix, iy, iz-1)
       int cb[4][4];
@@ -565,26 +610,62 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_e
         }
       }
       // same cell, particles after the target in list order
-      for (int t = s + 1; t < tail_end; t++) test(t, 0.f, 0.f, 0.f);
+      for (int t = s + 1; t < tail_end; t++) test(t, 0.f, 0.f, 0.f, cand);
       // (ix, iy, iz-1)
-      for (int t = own_lo; t < own_hi; t++) test(t, 0.f, 0.f, d.cellf);
+      for (int t = own_lo; t < own_hi; t++) test(t, 0.f, 0.f, cellf, cand);
       if (!m_img) cand += (unsigned long long)((tail_end - s - 1) + (own_hi - own_lo));
       // columns (ix-1, iy), then (ix-1..ix+1, iy-1), cells iz-1, iz, iz+1
 #pragma unroll
       for (int c = 0; c < 4; c++) {
-        const float ox = (float)(ix - ccx[c]) * d.cellf, oy = (float)(iy - ccy[c]) * d.cellf;
+        const float ox = (float)(ix - ccx[c]) * cellf, oy = (float)(iy - ccy[c]) * cellf;
         int t = cb[c][0];
-        for (; t < cb[c][1]; t++) test(t, ox, oy, d.cellf);
-        for (; t < cb[c][2]; t++) test(t, ox, oy, 0.f);
-        for (; t < cb[c][3]; t++) test(t, ox, oy, -d.cellf);
+        for (; t < cb[c][1]; t++) test(t, ox, oy, cellf, cand);
+        for (; t < cb[c][2]; t++) test(t, ox, oy, 0.f, cand);
+        for (; t < cb[c][3]; t++) test(t, ox, oy, -cellf, cand);
         if (!m_img) cand += (unsigned long long)(cb[c][3] - cb[c][0]);
+      }
+      // Hierarchical search: then the 27 cells around the target's cell in
+      // every coarser level, next coarser first (NBSMH_Loop_CrossMask,
+      // Prtcl_Hrchl_Munjiza.f90:762-863): the row below, the same row, the
+      // row above; columns crs_ix-1..+1; cells crs_iz-1..+1.  Offsets between
+      // cell corners are whole target cells (coarse cells are coe fine ones).
+      if (d.hier) {
+        const int mk = d.lv[lvl].mult;
+        for (int j = lvl - 1; j >= 0; j--) {
+          const LevelGrid& X = d.lv[j];
+          const int coe = 1 << (mk - X.mult);
+          const int cx0 = ix / coe, cy0 = iy / coe, cz0 = iz / coe;
+          const int* __restrict__ csx = d.cell_start + X.base;
+          for (int r = -1; r <= 1; r++) {
+            const int cy = cy0 + r;
+            if (cy < 0 || cy >= X.ny) continue;
+            for (int lx = -1; lx <= 1; lx++) {
+              const int cx = cx0 + lx;
+              if (cx < 0 || cx >= X.nx) continue;
+              const long long kc = ((long long)cy * X.nx + cx) * X.nz;
+              const float ox = (float)(ix - cx * coe) * cellf, oy = (float)(iy - cy * coe) * cellf;
+              for (int l = -1; l <= 1; l++) {
+                const int cz = cz0 + l;
+                if (cz < 0 || cz >= X.nz) continue;
+                const int a = csx[kc + cz], b = csx[kc + cz + 1];
+                const float oz = (float)(iz - cz * coe) * cellf;
+                for (int t = a; t < b; t++) test(t, ox, oy, oz, cand_x);
+                if (!m_img) cand_x += (unsigned long long)(b - a);
+              }
+            }
+          }
+        }
       }
       d.row_cnt[s] = cnt < K ? cnt : K;
 
     }
   }
-  for (int o = 16; o > 0; o >>= 1) cand += __shfl_down_sync(0xffffffffu, cand, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    cand += __shfl_down_sync(0xffffffffu, cand, o);
+    cand_x += __shfl_down_sync(0xffffffffu, cand_x, o);
+  }
   if ((threadIdx.x & 31) == 0 && cand) atomicAdd(&d.counters[0], cand);
+  if ((threadIdx.x & 31) == 0 && cand_x) atomicAdd(&d.counters[9], cand_x);
 }
 
 // Wall contacts of each particle: FindContactsPW (Prtcl_ContactSearchPW.f90:308-317)
@@ -1289,6 +1370,7 @@ __global__ void k_step_end(Dev d, int* counters_out) {
   *d.iter += 1;
   counters_out[SDEM_CNT_ITER] = *d.iter;
   counters_out[SDEM_CNT_NEXTWALL] = *d.next_update;
+  counters_out[SDEM_CNT_CNSV_CROSS] = (int)d.counters[9];
   d.counters[2] += (unsigned long long)(C - (int)d.counters[5] - (int)d.counters[8]);
   d.counters[3] += d.counters[1];
   d.counters[4] += 1ull;
@@ -1296,6 +1378,7 @@ __global__ void k_step_end(Dev d, int* counters_out) {
   d.counters[1] = 0;
   d.counters[5] = 0;
   d.counters[8] = 0;
+  d.counters[9] = 0;
   *d.out_cnt = 0;
   *d.wl_cnt = 0;
 }
@@ -1460,6 +1543,10 @@ struct sdem_h {
   int *c_ogid = nullptr, *c_pgid[2] = {}, *own_cnt[2] = {}, *own_c[2] = {}, *c_row = nullptr;
   int nall = 0, gcap = 0;
   int fcap = 0, nfix = 0;
+  bool hier = false;
+  int nlvl = 0;
+  LevelGrid lv[kMaxLevels] = {};
+  int* type_lvl = nullptr;
   int *fix_gid = nullptr, *fix_ptype = nullptr;
   dbl4* fix_posr = nullptr;
   int *gflag = nullptr, *goff = nullptr;
@@ -1482,7 +1569,8 @@ struct sdem_h {
   // device scalars
   int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
   // device counters: [0] candidates, [1] wall contacts, [2..4] sums since
-  // upload, [5] image pairs, [6..7] max |v|, |a| reductions, [8] fixed pairs
+  // upload, [5] image pairs, [6..7] max |v|, |a| reductions, [8] fixed pairs,
+  // [9] cross-level candidates
   unsigned long long* ull = nullptr;
   int *out_list = nullptr, *moves = nullptr, *map_pos = nullptr, *map_id = nullptr;
   int* h_counters = nullptr;  // pinned
@@ -1566,8 +1654,8 @@ int ensure_stage(sdem_h* h, size_t count) {
   return 0;
 }
 
-enum { S_N = 0, S_STATUS = 1, S_ITER = 3, S_NEXT = 4, S_OUTCNT = 5, S_WLCNT = 6, S_NG = 7, S_COUNTERS = 8,
-       S_NT = 16, S_SIZE = 24 };
+enum { S_N = 0, S_STATUS = 1, S_ITER = 3, S_NEXT = 4, S_OUTCNT = 5, S_WLCNT = 6, S_NG = 7, S_COUNTERS = 8,  // counters: 8..16
+       S_NT = 20, S_SIZE = 24 };
 
 Dev make_dev(sdem_h* h) {
   Dev d{};
@@ -1579,6 +1667,10 @@ Dev make_dev(sdem_h* h) {
   d.gcap = h->gcap;
   d.nall_launch = h->n_host + h->gcap + h->nfix;
   d.nfix = h->nfix;
+  d.hier = h->hier ? 1 : 0;
+  d.nlvl = h->nlvl;
+  for (int k = 0; k < kMaxLevels; k++) d.lv[k] = h->lv[k];
+  d.type_lvl = h->type_lvl;
   d.fix_gid = h->fix_gid;
   d.fix_ptype = h->fix_ptype;
   d.fix_posr = h->fix_posr;
@@ -1906,11 +1998,15 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   if (c.tsize < c.pi_method || c.rsize < c.pri_method) return bad("tsize >= PI_Method and rsize >= PRI_Method required");
   if (c.cf_type != SDEM_CFT_LSD && c.cf_type != SDEM_CFT_NLIN) return bad("cf_type must be 1 (LSD) or 2 (Hertz)");
   if (c.ct_model != SDEM_CTM_CONSTANT && c.ct_model != SDEM_CTM_VARIABLE) return bad("ct_model must be 1 or 2");
-  if (c.cs_method != SDEM_CSM_NBS_MUNJIZA) {
-    h->err = "only CS_Method=1 (NBS Munjiza) is implemented on the GPU";
+  if (c.cs_method != SDEM_CSM_NBS_MUNJIZA && c.cs_method != SDEM_CSM_HRCHL) return bad("cs_method must be 1 or 2");
+  if (c.cs_method == SDEM_CSM_HRCHL && c.n_fixed_capacity > 0) {
+    // NBSMH_LoopNBSMask has no fixed-particle branch (Prtcl_Hrchl_Munjiza.f90:601-704)
+    h->err = "fixed spheres with the hierarchical search (CS_Method=2) are not supported";
     *out = h;
     return SDEM_E_UNSUPPORTED;
   }
+  if (c.cs_num_levels < 0 || c.cs_num_levels > kMaxLevels) return bad("cs_num_levels must be 0..6");
+  h->hier = c.cs_method == SDEM_CSM_HRCHL;
   if (c.max_gid >= kImgFlag) return bad("max_gid must be < 2^30");
   if (!(c.cs_ratio >= 1.0)) return bad("Prtcl_cs_ratio must be >= 1 for the one-level NBS search");
   const int nper = (c.periodic[0] != 0) + (c.periodic[1] != 0) + (c.periodic[2] != 0);
@@ -2061,6 +2157,58 @@ int sdem_set_types(sdem_h* h, int nT, const double* radius, const double* mass, 
   h->ny = (int)((yed - h->y0) / h->cell) + 1;
   h->nz = (int)((zed - h->z0) / h->cell) + 1;
   h->ncell = (long long)h->nx * h->ny * h->nz;
+  if (h->hier) {
+    // Init_Munjiza_Hrchl (Prtcl_Hrchl_Munjiza.f90:78-218): levels halve the
+    // diameter bracket and the cell; every type of the table counts as
+    // populated (an empty level finds nothing either way).  Levels here are
+    // ordered coarsest first; the cell arrays hold the finest level first.
+    double maxD = 0.0, minD = 0.0;
+    for (int t = 0; t < nT; t++) {
+      const double dd = 2.0 * radius[t];
+      if (t == 0 || dd > maxD) maxD = dd;
+      if (t == 0 || dd < minD) minD = dd;
+    }
+    const int dmax_min = (int)(maxD / minD);
+    int numLevels = c.cs_num_levels > 0 ? c.cs_num_levels
+                  : dmax_min <= 1 ? 1 : dmax_min <= 3 ? 2 : dmax_min <= 7 ? 3 : dmax_min <= 15 ? 4
+                  : dmax_min <= 31 ? 5 : 6;
+    std::vector<int> tl(nT, 0);
+    h->nlvl = 0;
+    double maxD_lvl = maxD, cl = h->cell;
+    int nx = h->nx, ny = h->ny, nz = h->nz;
+    for (int idh = 1; idh <= numLevels; idh++) {
+      double minD_lvl = maxD_lvl / 2.0;
+      if (idh == numLevels) minD_lvl = 0.0;
+      bool populated = false;
+      for (int t = 0; t < nT; t++) {
+        const double dd = 2.0 * radius[t];
+        if (dd > minD_lvl && (idh == 1 || dd <= maxD_lvl)) {
+          populated = true;
+          tl[t] = h->nlvl;
+        }
+      }
+      if (populated) {
+        LevelGrid& G = h->lv[h->nlvl++];
+        G.nx = nx; G.ny = ny; G.nz = nz;
+        G.mult = idh;
+        G.cell = cl;
+        G.cellf = (float)cl;
+      }
+      nx *= 2; ny *= 2; nz *= 2;
+      maxD_lvl = minD_lvl;
+      cl = cl / 2.0;
+    }
+    long long off = 0;
+    for (int k = h->nlvl - 1; k >= 0; k--) {
+      h->lv[k].base = off;
+      off += (long long)h->lv[k].nx * h->lv[k].ny * h->lv[k].nz;
+    }
+    h->ncell = off;
+    rc |= dalloc(h, &h->type_lvl, (size_t)nT);
+    if (rc) return SDEM_E_NOMEM;
+    CK(cudaMemcpyAsync(h->type_lvl, tl.data(), sizeof(int) * nT, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
   {
     double mn = std::min(c.dom_max[0] - c.dom_min[0], std::min(c.dom_max[1] - c.dom_min[1], c.dom_max[2] - c.dom_min[2]));
     if (1.02 * h->cell > mn) return set_err(h, SDEM_E_ARG, "PC_InitComm: so big Diameter (domain narrower than 1.02 cells)");

@@ -44,6 +44,12 @@ CASES = {
     # fixed spheres (FineSearch1, ContactForce_PPFix): a rough floor and a few inside
     "fixed_floor": lambda: beds.fixed_floor_case(800, 61),
     "fixed_floor_lsd_fe": lambda: beds.fixed_floor_case(800, 62, cf_type=props.CFT_LSD, ntypes=3, pi=1, pri=1),
+    # hierarchical search (CS_Method 2): two levels (the 1:3 hopper), three levels
+    # (diameters 0.3-1.2 mm), two levels with periodic images
+    "hrchl_hopper": lambda: beds.scaled(beds.hopper_case(1500, 52), cs_method=2),
+    "hrchl_poly3": lambda: beds.scaled(cloud(seed=71, ntypes=9, d_lo=0.3e-3, d_hi=1.2e-3, nn=0.9e-3), cs_method=2),
+    "hrchl_periodic": lambda: beds.scaled(beds.periodic_lattice_case(800, 72, (1, 0, 1), d_lo=0.4e-3, d_hi=1.2e-3,
+                                                                     ntypes=5), cs_method=2),
 }
 
 
@@ -82,7 +88,7 @@ def test_one_step_from_identical_inputs(gpu_lib, name):
 
 
 @pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "hertz_finite_walls", "periodic_xyz", "periodic_xz",
-                                  "hopper", "fixed_floor"])
+                                  "hopper", "fixed_floor", "hrchl_hopper", "hrchl_poly3"])
 def test_twenty_steps_resynchronised(gpu_lib, name):
     """A chain of single steps, each from the oracle's state and contact list
     (restart-file style), so chaos cannot hide or create a mismatch."""
@@ -98,7 +104,8 @@ def test_twenty_steps_resynchronised(gpu_lib, name):
         g.close()
 
 
-@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "periodic_xyz", "fixed_floor"])
+@pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "periodic_xyz", "fixed_floor", "hrchl_poly3",
+                                  "hrchl_periodic"])
 def test_free_run_trajectory(gpu_lib, name):
     """50 free-running steps: contact sets stay identical and the state within
     a loose bound (differences start at ~1 ulp per step)."""
@@ -223,7 +230,7 @@ def test_fixed_sphere_arguments(gpu_lib):
 
 
 def test_unsupported_options_are_refused(gpu_lib):
-    case = beds.scaled(cloud(seed=24, n=20), cs_method=2)
+    case = beds.scaled(CASES["fixed_floor"](), cs_method=2)   # no fixed spheres in the hierarchical search
     with pytest.raises(SdemError) as e:
         DEMSystem(case)
     assert e.value.code == 10
