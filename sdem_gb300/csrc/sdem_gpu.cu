@@ -506,6 +506,7 @@ __global__ void k_cellorder(Dev d) {
 // position s).  Visit order per target: the tail of its own cell, then
 // (ix,iy,iz-1), (ix-1,iy,iz-1..iz+1), then row iy-1: columns ix-1..ix+1,
 // cells iz-1..iz+1 -- the order of Prtcl_NBS_Munjiza.f90:409-468.
+template <bool kHier>
 __global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_end) {
   int s = s_begin + blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = *d.nt;
@@ -523,7 +524,7 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_e
       int lvl = 0, nx = d.nx, nz = d.nz;
       long long lbase = 0;
       float cellf = d.cellf;
-      if (d.hier) {
+      if (kHier) {
         lvl = d.type_lvl[d.ptype[m] - 1];
         const LevelGrid& G = d.lv[lvl];
         nx = G.nx;
@@ -629,7 +630,7 @@ __global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_e
       // Prtcl_Hrchl_Munjiza.f90:762-863): the row below, the same row, the
       // row above; columns crs_ix-1..+1; cells crs_iz-1..+1.  Offsets between
       // cell corners are whole target cells (coarse cells are coe fine ones).
-      if (d.hier) {
+      if (kHier) {
         const int mk = d.lv[lvl].mult;
         for (int j = lvl - 1; j >= 0; j--) {
           const LevelGrid& X = d.lv[j];
@@ -785,7 +786,9 @@ __global__ void k_row_fill(Dev d, int s_begin, int s_end) {
 
 // ---------------------------------------------------------------------------
 // One thread per contact: Find_insert's history lookup + ContactForce_PP.
-// Contacts of the rows [s_begin, s_end).
+// Contacts of the rows [s_begin, s_end).  kOneSided: the search holds periodic
+// images or fixed spheres (pairs whose force goes to one sphere only).
+template <bool kOneSided>
 __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s_end) {
   const int nloc = *d.n;
   const int c0 = d.row_off[s_begin], C = d.row_off[s_end];
@@ -804,7 +807,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     // particle-particle (AddContactPP) or local-image (AddContactPPG) pair; the
     // lower id is particle i of the force law either way
     // (Prtcl_NBS_Munjiza.f90:525-529, Prtcl_CL_and_CF.f90:773-797)
-    const bool img = (m >= nloc) || (q >= nloc);
+    const bool img = kOneSided && ((m >= nloc) || (q >= nloc));
     const int loc = (m >= nloc) ? q : m;     // the local particle of an image pair
     const int oth = (loc == m) ? q : m;
     bool m_lo = gm < gq;
@@ -852,16 +855,20 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     if (os < d.Ko) d.own_c[(size_t)owner * d.Ko + os] = c;
     else raise(d, SDEM_E_CL_FULL, owner);
     // one-sided pairs: with an image (AddContactPPG) or a fixed sphere (AddContactPPFix)
-    const bool fx = img && oth >= first_fixed;
-    nimg += (img && !fx) ? 1ull : 0ull;
-    nfx += fx ? 1ull : 0ull;
+    if (kOneSided) {
+      const bool fx = img && oth >= first_fixed;
+      nimg += (img && !fx) ? 1ull : 0ull;
+      nfx += fx ? 1ull : 0ull;
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    nimg += __shfl_down_sync(0xffffffffu, nimg, o);
-    nfx += __shfl_down_sync(0xffffffffu, nfx, o);
+  if (kOneSided) {
+    for (int o = 16; o > 0; o >>= 1) {
+      nimg += __shfl_down_sync(0xffffffffu, nimg, o);
+      nfx += __shfl_down_sync(0xffffffffu, nfx, o);
+    }
+    if ((threadIdx.x & 31) == 0 && nimg) atomicAdd(&d.counters[5], nimg);
+    if ((threadIdx.x & 31) == 0 && nfx) atomicAdd(&d.counters[8], nfx);
   }
-  if ((threadIdx.x & 31) == 0 && nimg) atomicAdd(&d.counters[5], nimg);
-  if ((threadIdx.x & 31) == 0 && nfx) atomicAdd(&d.counters[8], nfx);
 }
 
 // ---------------------------------------------------------------------------
@@ -1871,7 +1878,8 @@ int enqueue_step(sdem_h* h) {
   }
   for (int k = 0; k < nchunk; k++) {
     const int a = cut(k), b = cut(k + 1);
-    k_search<<<grid_for(std::max(b - a, 1)), kThreads, 0, s2>>>(d, a, b);
+    if (h->hier) k_search<true><<<grid_for(std::max(b - a, 1)), kThreads, 0, s2>>>(d, a, b);
+    else k_search<false><<<grid_for(std::max(b - a, 1)), kThreads, 0, s2>>>(d, a, b);
     if (s2 != st) cudaEventRecord(h->ev_chunk[k], s2);
   }
   k_wall_detect<<<grid_for(n), kThreads, 0, s2>>>(d);
@@ -1881,7 +1889,8 @@ int enqueue_step(sdem_h* h) {
     mark(PH_ROW_FILL);
     k_row_fill<<<grid_for(na), kThreads, 0, st>>>(d, 0, na);
     mark(PH_FORCE);
-    k_force<<<h->num_sms * 8, kThreads, 0, st>>>(d, 0, na);
+    if (h->gcap > 0 || h->nfix > 0) k_force<true><<<h->num_sms * 8, kThreads, 0, st>>>(d, 0, na);
+    else k_force<false><<<h->num_sms * 8, kThreads, 0, st>>>(d, 0, na);
     mark(PH_WALL_FORCE);
     k_wall_force<<<std::max(1, h->num_sms * 2), kThreads, 0, st>>>(d);
   } else {
@@ -1892,7 +1901,8 @@ int enqueue_step(sdem_h* h) {
       cudaStreamWaitEvent(st, h->ev_chunk[k], 0);
       scan(h, h->row_cnt + a, b - a, h->row_off + a, k ? h->row_off + a : nullptr);
       k_row_fill<<<grid_for(std::max(b - a, 1)), kThreads, 0, st>>>(d, a, b);
-      k_force<<<h->num_sms * 3, kThreads, 0, st>>>(d, a, b);
+      if (h->gcap > 0 || h->nfix > 0) k_force<true><<<h->num_sms * 3, kThreads, 0, st>>>(d, a, b);
+      else k_force<false><<<h->num_sms * 3, kThreads, 0, st>>>(d, a, b);
     }
     cudaStreamWaitEvent(st, h->ev_join, 0);
   }
