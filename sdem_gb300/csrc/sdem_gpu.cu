@@ -1342,6 +1342,20 @@ __global__ void k_snap_copy(SnapContacts src, SnapContacts dst) {
   }
 }
 
+// Upload checks on the device: ids in 1..max_gid and unique (a flag per id),
+// types in 1..nT.  status[0] = first error, status[1] = its particle index.
+__global__ void k_check_upload(const int* __restrict__ id, const int* __restrict__ ptype, int n, int max_gid, int nT,
+                               int* __restrict__ flag, int* __restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int g = id[i];
+  int code = 0;
+  if (g < 1 || g > max_gid) code = SDEM_E_BAD_ID;
+  else if (atomicExch(&flag[g], 1) != 0) code = SDEM_E_BAD_ID + 100;   // duplicate
+  else if (ptype[i] < 1 || ptype[i] > nT) code = SDEM_E_ARG;
+  if (code && atomicCAS(status, 0, code) == 0) status[1] = i;
+}
+
 // Host layout <-> device layout of the per-particle 3-vectors: the ABI's
 // [(i*levels + k)*3 + c] doubles against one 32-byte record per particle and
 // level.  A null source writes zeros.
@@ -1537,7 +1551,6 @@ struct sdem_h {
   size_t scan_tmp_n = 0;
   // particles
   int n_host = 0;  // count at upload (upper bound of the device count)
-  std::vector<int> h_gid;
   int *gid = nullptr, *ptype = nullptr, *usrmark = nullptr;
   dbl4 *posr = nullptr, *vel[3] = {}, *acc[3] = {}, *theta = nullptr, *rv[3] = {}, *ra[3] = {};
   dbl4 *F = nullptr, *T = nullptr;
@@ -2327,14 +2340,6 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   if (!h->have_types) return set_err(h, SDEM_E_ARG, "sdem_upload_particles: call sdem_set_types first");
   if (n < 0 || n > c.n_capacity) return set_err(h, SDEM_E_CAPACITY, "sdem_upload_particles: n exceeds n_capacity");
   if (n > 0 && (!id || !ptype || !posR || !linVel)) return set_err(h, SDEM_E_ARG, "sdem_upload_particles: null arrays");
-  std::vector<char> seen((size_t)c.max_gid + 1, 0);
-  for (int i = 0; i < n; i++) {
-    if (id[i] < 1 || id[i] > c.max_gid) return set_err(h, SDEM_E_BAD_ID, "particle id outside 1..max_gid");
-    if (seen[id[i]]) return set_err(h, SDEM_E_BAD_ID, "duplicate particle id");
-    seen[id[i]] = 1;
-    if (ptype[i] < 1 || ptype[i] > h->nT) return set_err(h, SDEM_E_ARG, "particle type outside 1..nT");
-  }
-  h->h_gid.assign(id, id + n);
   // Stream-ordered copies: a step still in flight finishes before the state
   // is replaced, and the call returns after the last copy has landed.
   cudaStream_t st = h->stream;
@@ -2342,6 +2347,28 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   if (n > 0) {
     CK(cudaMemcpyAsync(h->gid, id, sizeof(int) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(h->ptype, ptype, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    // ids and types are checked on the device (the owner table of buffer 0,
+    // cleared again below, holds the per-id flags)
+    int* scal = h->scal;
+    CK(cudaMemsetAsync(h->own_cnt[0], 0, sizeof(int) * ((size_t)c.max_gid + 1), st));
+    CK(cudaMemsetAsync(scal + S_STATUS, 0, 2 * sizeof(int), st));
+    k_check_upload<<<grid_for(n), kThreads, 0, st>>>(h->gid, h->ptype, n, c.max_gid, h->nT, h->own_cnt[0],
+                                                     scal + S_STATUS);
+    int chk[2] = {0, 0};
+    CK(cudaMemcpyAsync(chk, scal + S_STATUS, sizeof chk, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (chk[0] != 0) {
+      h->n_host = 0;   // the handle holds no valid particle set now
+      h->stepped = false;
+      drop_graph(h);
+      int z[2] = {0, 0};
+      CK(cudaMemcpyAsync(scal + S_STATUS, z, sizeof z, cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+      const std::string at = " (particle index " + std::to_string(chk[1]) + ")";
+      if (chk[0] == SDEM_E_BAD_ID) return set_err(h, SDEM_E_BAD_ID, "particle id outside 1..max_gid" + at);
+      if (chk[0] == SDEM_E_BAD_ID + 100) return set_err(h, SDEM_E_BAD_ID, "duplicate particle id" + at);
+      return set_err(h, SDEM_E_ARG, "particle type outside 1..nT" + at);
+    }
     if (usrmark) CK(cudaMemcpyAsync(h->usrmark, usrmark, sizeof(int) * n, cudaMemcpyHostToDevice, st));
     else CK(cudaMemsetAsync(h->usrmark, 0, sizeof(int) * n, st));
     // (x, y, z, r) per particle is also the device record
@@ -2402,8 +2429,10 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
   int pv = 1 - h->cur;
   std::vector<std::vector<std::pair<int, dbl4>>> wl(n);
   std::vector<sdem_h::UpRec> pp;
+  std::vector<int> hg(std::max(n, 1));
+  if (n > 0) CK(cudaMemcpy(hg.data(), h->gid, sizeof(int) * n, cudaMemcpyDeviceToHost));
   std::unordered_map<int, int> idx_of;
-  for (int i = 0; i < n; i++) idx_of[h->h_gid[i]] = i;
+  for (int i = 0; i < n; i++) idx_of[hg[i]] = i;
   std::vector<double> posr(4 * (size_t)std::max(n, 1));
   if (n > 0) {
     std::vector<dbl4> pb(n);
@@ -2415,7 +2444,7 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
   for (int i = 0; i < nc; i++) {
     int o = owner_idx[i];
     if (o < 0 || o >= n) return set_err(h, SDEM_E_ARG, "sdem_upload_contacts: owner index out of range");
-    int go = h->h_gid[o], pid = partner_id[i];
+    int go = hg[o], pid = partner_id[i];
     dbl4 hist = make_dbl4(tandelta[3 * i], tandelta[3 * i + 1], tandelta[3 * i + 2], velrel[i]);
     if (pid > c.base_wall_id) {
       int wi = -1;
@@ -2476,7 +2505,7 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
   std::vector<int> whc(G, 0), whw(G * kKw, 0);
   std::vector<dbl4> whh(G * kKw);
   for (int o = 0; o < n; o++) {
-    int g = h->h_gid[o];
+    int g = hg[o];
     int k = 0;
     for (auto& e : wl[o]) {
       if (k >= kKw) return set_err(h, SDEM_E_CL_FULL, "sdem_upload_contacts: more than 4 wall contacts on one particle");

@@ -188,6 +188,26 @@ def test_grid_error(gpu_lib):
     assert e.value.code == 6
 
 
+def test_upload_checks_ids_and_types(gpu_lib):
+    case = cloud(seed=25, n=200)
+    g = DEMSystem(case)
+    for field, value, code in (("id", None, 4), ("id", 10**6, 4), ("ptype", 99, 1)):
+        p = case.particles.copy()
+        if field == "id" and value is None:
+            p.id[7] = p.id[3]                      # duplicate id
+        elif field == "id":
+            p.id[7] = value                        # above max_gid
+        else:
+            p.ptype[7] = value
+        with pytest.raises(SdemError) as e:
+            g.upload(p)
+        assert e.value.code == code, (field, value)
+        assert "index 7" in str(e.value)
+    g.upload(case.particles)                       # a valid set is accepted again
+    g.step(1)
+    assert g.counters()["nlocal"] == case.particles.n
+
+
 def test_row_capacity_error(gpu_lib):
     case = beds.scaled(cloud(seed=23), max_contacts_per_particle=1)
     g = DEMSystem(case)
