@@ -1380,7 +1380,11 @@ __global__ void k_pack3(double* __restrict__ dst, const dbl4* __restrict__ src, 
   v[2] = a.z;
 }
 
-__global__ void k_step_end(Dev d, int* counters_out) {
+// Ends a step: the counters of the step (CL and search logs), running sums,
+// per-step resets, and a copy of the device scalars (status, particle count,
+// counters) into mapped host memory, so that the host reads them after a
+// stream synchronisation without another copy.
+__global__ void k_step_end(Dev d, int* counters_out, const int* scal, int* mirror, int nscal) {
   const int C = d.row_off[d.nall_launch];
   counters_out[SDEM_CNT_PP] = C - (int)d.counters[5] - (int)d.counters[8];
   counters_out[SDEM_CNT_PPG] = (int)d.counters[5];
@@ -1402,6 +1406,8 @@ __global__ void k_step_end(Dev d, int* counters_out) {
   d.counters[9] = 0;
   *d.out_cnt = 0;
   *d.wl_cnt = 0;
+  if (mirror)
+    for (int k = 0; k < nscal; k++) mirror[k] = scal[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -1594,6 +1600,11 @@ struct sdem_h {
   unsigned long long* ull = nullptr;
   int *out_list = nullptr, *moves = nullptr, *map_pos = nullptr, *map_id = nullptr;
   int* h_counters = nullptr;  // pinned
+  // mapped host copy of the device scalars, written by every step's last
+  // kernel; valid while no host write to the scalars came after the last step
+  int* h_mirror = nullptr;
+  int* d_mirror = nullptr;
+  bool mirror_ok = false;
   double* stage = nullptr;    // device staging of host-layout 3-vectors (upload, download)
   size_t stage_n = 0;
   // asynchronous output: a frozen copy of the state and contacts on the device,
@@ -1929,7 +1940,8 @@ int enqueue_step(sdem_h* h) {
   k_delete<<<1, 1, 0, st>>>(d);
   k_apply_moves<<<16, kThreads, 0, st>>>(d);
   mark(PH_END);
-  k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS);
+  k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS, h->scal, h->d_mirror, S_SIZE);
+  h->mirror_ok = true;
   mark(kPhases);
   // bin, scan, scatter, cellorder, wall detect, wall force, degree scatter,
   // gather, integrate, delete (2), step end; per chunk search, scan (3),
@@ -1956,7 +1968,8 @@ void drop_graph(sdem_h* h) {
 int sync_and_check(sdem_h* h) {
   CK(cudaStreamSynchronize(h->stream));
   int s[S_SIZE];
-  CK(cudaMemcpy(s, h->scal, sizeof s, cudaMemcpyDeviceToHost));
+  if (h->mirror_ok) std::memcpy(s, h->h_mirror, sizeof s);
+  else CK(cudaMemcpy(s, h->scal, sizeof s, cudaMemcpyDeviceToHost));
   std::memcpy(h->h_counters, s + S_COUNTERS, sizeof(int) * SDEM_CNT_SIZE);
   if (s[S_STATUS] != 0) {
     int code = s[S_STATUS], detail = s[S_STATUS + 1];
@@ -1972,6 +1985,7 @@ int sync_and_check(sdem_h* h) {
     int z[2] = {0, 0};
     cudaMemcpyAsync(h->scal + S_STATUS, z, sizeof z, cudaMemcpyHostToDevice, h->stream);
     cudaStreamSynchronize(h->stream);
+    h->mirror_ok = false;
     return set_err(h, code, msg);
   }
   return 0;
@@ -2144,6 +2158,8 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->scan_tmp, 65536);
   if (rc) return SDEM_E_NOMEM;
   CK(cudaMallocHost(&h->h_counters, sizeof(int) * SDEM_CNT_SIZE));
+  CK(cudaHostAlloc((void**)&h->h_mirror, sizeof(int) * S_SIZE, cudaHostAllocMapped));
+  CK(cudaHostGetDevicePointer((void**)&h->d_mirror, h->h_mirror, 0));
   std::memset(h->h_counters, 0, sizeof(int) * SDEM_CNT_SIZE);
   CK(cudaStreamSynchronize(h->stream));
   return 0;
@@ -2295,6 +2311,7 @@ int sdem_set_walls(sdem_h* h, int nw, const double* wall, const int* flags) {
   // the near-wall list is rebuilt at the next step
   int zero = 0;
   CK(cudaMemcpyAsync(h->scal + S_NEXT, &zero, sizeof zero, cudaMemcpyHostToDevice, h->stream));
+  h->mirror_ok = false;
   CK(cudaStreamSynchronize(h->stream));
   return 0;
 }
@@ -2344,6 +2361,7 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   // is replaced, and the call returns after the last copy has landed.
   cudaStream_t st = h->stream;
   CK(cudaStreamSynchronize(st));
+  h->mirror_ok = false;   // the device scalars are rewritten below
   if (n > 0) {
     CK(cudaMemcpyAsync(h->gid, id, sizeof(int) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(h->ptype, ptype, sizeof(int) * n, cudaMemcpyHostToDevice, st));
@@ -3153,6 +3171,7 @@ void sdem_destroy(sdem_h* h) {
   for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
+  if (h->h_mirror) cudaFreeHost(h->h_mirror);
   if (h->stage) cudaFree(h->stage);
   if (h->stream_io) cudaStreamSynchronize(h->stream_io);
   if (h->sn_state) cudaFree(h->sn_state);
