@@ -295,7 +295,7 @@ def our_arm(args):
         t0 = time.perf_counter()
         sys2.upload(st)
         for _ in range(Ke):
-            sys2.step(1)
+            sys2.step_async(1)      # the counters read below waits for the step
             sys2.counters()
         out = sys2.state(out=out_buf)
         torch.cuda.synchronize()
@@ -307,7 +307,7 @@ def our_arm(args):
                                                    "rotVel", "rotAcc")) + Ke * 32
         e2e = {"value": n_all * Ke / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / Ke),
                "d2h_bytes_per_step": int(d2h / Ke), "steps": Ke,
-               "note": "upload of the state from pinned host memory, K x (sdem_step(h,1) + sdem_counters), "
+               "note": "upload of the state from pinned host memory, K x (sdem_step_async(h,1) + sdem_counters), "
                        "download of the state into pinned host memory"}
         sys2.close()
 
