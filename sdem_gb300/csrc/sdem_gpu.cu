@@ -3,8 +3,9 @@
 // -O3 -fmad=false (see sdem_gb300/build.py).
 //
 // One step (the body of DEMS_iterate, Prtcl_DEMSystem.f90:214-247) is:
-//   k_wall_refresh/k_wall_refresh_end  UpdateNearPrtclsPW (Prtcl_ContactSearchPW.f90:159-235),
-//                                      device-predicated on iter >= Next_iter_update
+//   k_step_begin                       UpdateNearPrtclsPW (Prtcl_ContactSearchPW.f90:159-235),
+//                                      device-predicated on iter >= Next_iter_update; the
+//                                      step's image and gather-order counters reset
 //   k_ghost_*                          PC_Comm_For_Cntct on one rank (periodic directions only):
 //                                      images of the particles near periodic faces, in the
 //                                      reference's pass order, as ordered stream compactions
@@ -34,8 +35,8 @@
 //   k_integrate                        clc_Acceleration (Prtcl_DEMSystem.f90:166-181), Prtcl_Integrate
 //                                      (Prtcl_Integration.f90:15-88) and the periodic wrap, in index
 //                                      order
-//   k_delete, k_apply_moves            one-rank out-of-domain delete (Prtcl_Comm.f90:1569-1840)
-//   k_step_end                         iterNumber += 1, counters
+//   k_finish                           one-rank out-of-domain delete (Prtcl_Comm.f90:1569-1840),
+//                                      iterNumber += 1, counters
 // RemvReleased/PreIteration have no kernel: the history of step n+1 is exactly
 // the contact records written at step n (double-buffered, keyed by particle id).
 #include <cuda_runtime.h>
@@ -178,6 +179,7 @@ struct Dev {
   int* iter;
   int* next_update;
   int* out_cnt;
+  int* ticket;   // last-block ticket of k_step_begin
   int* out_list;
   int* moves;      // [0] count, then (dst, src) pairs
   int* map_pos;    // deletion scratch
@@ -268,54 +270,68 @@ __global__ void k_scan_apply(const int* __restrict__ in, long long n, const int*
 // ---------------------------------------------------------------------------
 // UpdateNearPrtclsPW (Prtcl_ContactSearchPW.f90:159-235): near-wall bit mask per
 // particle (walls whose AABB +- DeltaXmax2 holds the particle), max |v|, max |a|.
-__global__ void k_wall_refresh(Dev d) {
-  if (*d.iter < *d.next_update) return;
-  int n = *d.n;
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  double vmax = 0.0, amax = 0.0;
-  if (p < n) {
-    dbl4 P = d.posr[p];
-    unsigned long long mask = 0ull;
-    for (int k = 0; k < d.nw; k++) {
-      const double* r = d.walls + k * SDEM_W_SIZE;
-      double pminx = r[SDEM_W_MIN] - d.dx2, pminy = r[SDEM_W_MIN + 1] - d.dx2, pminz = r[SDEM_W_MIN + 2] - d.dx2;
-      double pmaxx = r[SDEM_W_MAX] + d.dx2, pmaxy = r[SDEM_W_MAX + 1] + d.dx2, pmaxz = r[SDEM_W_MAX + 2] + d.dx2;
-      if (P.x >= pminx && P.x <= pmaxx && P.y >= pminy && P.y <= pmaxy && P.z >= pminz && P.z <= pmaxz)
-        mask |= (1ull << k);
+// The start of a step: UpdateNearPrtclsPW when iter >= Next_iter_update (the
+// near-wall mask of every particle and the max |v|, |a| reductions; the last
+// block to finish computes the next refresh iteration), and the step's image
+// and gather-order counters reset (by that last block as well).
+__global__ void k_step_begin(Dev d) {
+  const bool refresh = *d.iter >= *d.next_update;
+  if (refresh) {
+    int n = *d.n;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    double vmax = 0.0, amax = 0.0;
+    if (p < n) {
+      dbl4 P = d.posr[p];
+      unsigned long long mask = 0ull;
+      for (int k = 0; k < d.nw; k++) {
+        const double* r = d.walls + k * SDEM_W_SIZE;
+        double pminx = r[SDEM_W_MIN] - d.dx2, pminy = r[SDEM_W_MIN + 1] - d.dx2, pminz = r[SDEM_W_MIN + 2] - d.dx2;
+        double pmaxx = r[SDEM_W_MAX] + d.dx2, pmaxy = r[SDEM_W_MAX + 1] + d.dx2, pmaxz = r[SDEM_W_MAX + 2] + d.dx2;
+        if (P.x >= pminx && P.x <= pmaxx && P.y >= pminy && P.y <= pmaxy && P.z >= pminz && P.z <= pmaxz)
+          mask |= (1ull << k);
+      }
+      d.near_mask[p] = mask;
+      vmax = sdem::norm3(sdem::xyz(d.vel0[p]));
+      amax = sdem::norm3(sdem::xyz(d.acc0[p]));
     }
-    d.near_mask[p] = mask;
-    vmax = sdem::norm3(sdem::xyz(d.vel0[p]));
-    amax = sdem::norm3(sdem::xyz(d.acc0[p]));
+    // non-negative doubles order like their bit patterns
+    for (int o = 16; o > 0; o >>= 1) {
+      vmax = fmax(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+      amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&d.red[0], (unsigned long long)__double_as_longlong(vmax));
+      atomicMax(&d.red[1], (unsigned long long)__double_as_longlong(amax));
+      __threadfence();
+    }
   }
-  // non-negative doubles order like their bit patterns
-  for (int o = 16; o > 0; o >>= 1) {
-    vmax = fmax(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
-    amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, o));
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(d.ticket, 1) == (int)gridDim.x - 1;
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  *d.ticket = 0;
+  if (refresh) {
+    const int it = *d.iter;
+    // read and clear the reductions at L2, where the other blocks' atomics went
+    double max_v = __longlong_as_double((long long)atomicExch(&d.red[0], 0ull));
+    double max_a = __longlong_as_double((long long)atomicExch(&d.red[1], 0ull));
+    max_v = max_v + d.max_wall_vel;
+    max_v = (max_v > 0.3) ? max_v : 0.3;
+    max_v = max_v * 1.5;
+    double gn = sdem::norm3(sdem::mk3(d.g.x, d.g.y, d.g.z));
+    max_a = (max_a > gn) ? max_a : gn;
+    max_a = max_a * 1.5;
+    double t = (sqrt(max_v * max_v + 2.0 * max_a * d.dx1) - max_v) / max_a;
+    int numIter = (int)(t / d.law.dt);
+    numIter = numIter > 1 ? numIter : 1;
+    numIter = numIter < d.wall_max_update_iter ? numIter : d.wall_max_update_iter;
+    *d.next_update = it + numIter;
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&d.red[0], (unsigned long long)__double_as_longlong(vmax));
-    atomicMax(&d.red[1], (unsigned long long)__double_as_longlong(amax));
-  }
-}
-
-__global__ void k_wall_refresh_end(Dev d) {
-  int it = *d.iter;
-  if (it < *d.next_update) return;
-  double max_v = __longlong_as_double((long long)d.red[0]);
-  double max_a = __longlong_as_double((long long)d.red[1]);
-  d.red[0] = 0ull;
-  d.red[1] = 0ull;
-  max_v = max_v + d.max_wall_vel;
-  max_v = (max_v > 0.3) ? max_v : 0.3;
-  max_v = max_v * 1.5;
-  double gn = sdem::norm3(sdem::mk3(d.g.x, d.g.y, d.g.z));
-  max_a = (max_a > gn) ? max_a : gn;
-  max_a = max_a * 1.5;
-  double t = (sqrt(max_v * max_v + 2.0 * max_a * d.dx1) - max_v) / max_a;
-  int numIter = (int)(t / d.law.dt);
-  numIter = numIter > 1 ? numIter : 1;
-  numIter = numIter < d.wall_max_update_iter ? numIter : d.wall_max_update_iter;
-  *d.next_update = it + numIter;
+  *d.ng = 0;
+  *d.nt = *d.n;
+  for (int b = 0; b < kDegBuckets; b++) d.deg_cnt[b] = 0;   // gather-order buckets of this step
 }
 
 // ---------------------------------------------------------------------------
@@ -338,12 +354,6 @@ __device__ __forceinline__ int ghost_count(const Dev& d, int pass, const dbl4& P
     case GP_ZP: return P.z >= d.dmax.z - L ? 1 : 0;
     default: return (P.z <= d.dmin.z + L && P.z >= d.dmin.z) ? 1 : 0;
   }
-}
-
-__global__ void k_ghost_begin(Dev d) {
-  *d.ng = 0;
-  *d.nt = *d.n;
-  for (int b = 0; b < kDegBuckets; b++) d.deg_cnt[b] = 0;   // gather-order buckets of this step
 }
 
 __global__ void k_ghost_flag(Dev d, int pass) {
@@ -1086,7 +1096,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
 
   // Comm_For_Exchange, y pencil, one rank (Prtcl_Comm.f90:1569-1840): a periodic
   // direction wraps the position (passes y, +x, -x, +z, -z); the others delete
-  // what left [min, max), in k_delete.
+  // what left [min, max), in the delete passes (k_finish).
   if (d.per[0] || d.per[1] || d.per[2]) {
     dbl4 Q = d.posr[p];
     if (d.per[1]) {
@@ -1129,7 +1139,7 @@ __device__ __forceinline__ bool out_pass(const Dev& d, int id, int pass) {
   }
 }
 
-__global__ void k_delete(Dev d) {
+__device__ void delete_serial(const Dev& d) {
   int U = *d.out_cnt;
   d.moves[0] = 0;
   if (U == 0) return;
@@ -1199,9 +1209,9 @@ __global__ void k_delete(Dev d) {
 // GL_copy + CL_copy + CSPW_copy for each move (force and torque are not part of
 // GL_copy and stay where they are).  Sources lie beyond the new count and
 // destinations below it, so the copies are independent.
-__global__ void k_apply_moves(Dev d) {
+__device__ void apply_moves(const Dev& d, int first, int stride) {
   int mv = d.moves[0];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < mv; i += gridDim.x * blockDim.x) {
+  for (int i = first; i < mv; i += stride) {
     int dst = d.moves[1 + 2 * i], src = d.moves[2 + 2 * i];
     d.gid[dst] = d.gid[src];
     d.ptype[dst] = d.ptype[src];
@@ -1384,7 +1394,7 @@ __global__ void k_pack3(double* __restrict__ dst, const dbl4* __restrict__ src, 
 // per-step resets, and a copy of the device scalars (status, particle count,
 // counters) into mapped host memory, so that the host reads them after a
 // stream synchronisation without another copy.
-__global__ void k_step_end(Dev d, int* counters_out, const int* scal, int* mirror, int nscal) {
+__device__ void step_end_serial(const Dev& d, int* counters_out, const int* scal, int* mirror, int nscal) {
   const int C = d.row_off[d.nall_launch];
   counters_out[SDEM_CNT_PP] = C - (int)d.counters[5] - (int)d.counters[8];
   counters_out[SDEM_CNT_PPG] = (int)d.counters[5];
@@ -1408,6 +1418,16 @@ __global__ void k_step_end(Dev d, int* counters_out, const int* scal, int* mirro
   *d.wl_cnt = 0;
   if (mirror)
     for (int k = 0; k < nscal; k++) mirror[k] = scal[k];
+}
+
+// The end of a step in one block: the serial delete passes (thread 0), the
+// moves they imply (all threads), then the counters (thread 0).
+__global__ void k_finish(Dev d, int* counters_out, const int* scal, int* mirror, int nscal) {
+  if (threadIdx.x == 0) delete_serial(d);
+  __syncthreads();
+  apply_moves(d, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (threadIdx.x == 0) step_end_serial(d, counters_out, scal, mirror, nscal);
 }
 
 // ---------------------------------------------------------------------------
@@ -1688,7 +1708,7 @@ int ensure_stage(sdem_h* h, size_t count) {
 }
 
 enum { S_N = 0, S_STATUS = 1, S_ITER = 3, S_NEXT = 4, S_OUTCNT = 5, S_WLCNT = 6, S_NG = 7, S_COUNTERS = 8,  // counters: 8..16
-       S_NT = 20, S_SIZE = 24 };
+       S_NT = 20, S_TICKET = 21, S_SIZE = 24 };
 
 Dev make_dev(sdem_h* h) {
   Dev d{};
@@ -1709,6 +1729,7 @@ Dev make_dev(sdem_h* h) {
   d.fix_posr = h->fix_posr;
   d.ng = h->scal + S_NG;
   d.nt = h->scal + S_NT;
+  d.ticket = h->scal + S_TICKET;
   for (int k = 0; k < 3; k++) d.per[k] = c.periodic[k];
   d.Lbox = make_double3(c.dom_max[0] - c.dom_min[0], c.dom_max[1] - c.dom_min[1], c.dom_max[2] - c.dom_min[2]);
   d.lencs = h->cell;
@@ -1856,13 +1877,10 @@ int enqueue_step(sdem_h* h) {
   long long L = 0;
   mark(PH_WALL);
   // the refresh schedule (Next_iter_update) advances with or without walls
-  k_wall_refresh<<<grid_for(n), kThreads, 0, st>>>(d);
-  k_wall_refresh_end<<<1, 1, 0, st>>>(d);
-  L += 2;
+  k_step_begin<<<grid_for(n), kThreads, 0, st>>>(d);
+  L += 1;
   mark(PH_BIN);
   const int na = n + h->gcap + h->nfix;   // search arrays: locals, periodic images, fixed spheres
-  k_ghost_begin<<<1, 1, 0, st>>>(d);
-  L += 1;
   if (h->gcap > 0) {
     const int per[3] = {h->cfg.periodic[0], h->cfg.periodic[1], h->cfg.periodic[2]};
     const int passes[5] = {GP_Y, GP_XP, GP_XM, GP_ZP, GP_ZM};
@@ -1937,16 +1955,13 @@ int enqueue_step(sdem_h* h) {
   k_gather<true><<<grid_for(n), kThreads, 0, st>>>(d);
   k_integrate<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_DELETE);
-  k_delete<<<1, 1, 0, st>>>(d);
-  k_apply_moves<<<16, kThreads, 0, st>>>(d);
+  k_finish<<<1, kThreads, 0, st>>>(d, h->scal + S_COUNTERS, h->scal, h->d_mirror, S_SIZE);
   mark(PH_END);
-  k_step_end<<<1, 1, 0, st>>>(d, h->scal + S_COUNTERS, h->scal, h->d_mirror, S_SIZE);
   h->mirror_ok = true;
   mark(kPhases);
   // bin, scan, scatter, cellorder, wall detect, wall force, degree scatter,
-  // gather, integrate, delete (2), step end; per chunk search, scan (3),
-  // row fill, force
-  L += 1 + 3 + 1 + 1 + 1 + 1 + 3 + 2 + 1 + 6 * nchunk;
+  // gather, integrate, finish; per chunk search, scan (3), row fill, force
+  L += 1 + 3 + 1 + 1 + 1 + 1 + 3 + 1 + 6 * nchunk;
   h->launches += L;
   if (ev) h->prof_steps++;
   h->cur = 1 - h->cur;
