@@ -15,7 +15,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc", "sdem_gpu.cu")
-DEPS = [SRC, os.path.join(HERE, "csrc", "dem_device.cuh"), os.path.join(ROOT, "include", "sdem_gpu.h")]
+DEPS = [SRC, os.path.join(HERE, "csrc", "dem_device.cuh"), os.path.join(HERE, "csrc", "fp64_int.cuh"),
+        os.path.join(ROOT, "include", "sdem_gpu.h")]
 LIB = os.path.join(HERE, "libsdem_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -68,7 +68,10 @@ constexpr int kMaxWalls = 64;     // near-wall mask is 64 bits
 constexpr int kOutCap = 4096;     // out-of-domain deletions per step
 constexpr int kScanTile = 4096;   // elements per scan block (1024 threads x 4)
 constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact records
-constexpr int kChunks = 2;        // search/force pipeline chunks per step
+#ifndef SDEM_PIPELINE_CHUNKS
+#define SDEM_PIPELINE_CHUNKS 2
+#endif
+constexpr int kChunks = SDEM_PIPELINE_CHUNKS;   // search/force pipeline chunks per step
 constexpr int kMaxLevels = 6;     // hierarchical search levels (Init_Munjiza_Hrchl caps at 6)
 
 // One level of the hierarchical search: a grid of cells 2^(mult-1) times
@@ -516,8 +519,10 @@ __global__ void k_cellorder(Dev d) {
 // position s).  Visit order per target: the tail of its own cell, then
 // (ix,iy,iz-1), (ix-1,iy,iz-1..iz+1), then row iy-1: columns ix-1..ix+1,
 // cells iz-1..iz+1 -- the order of Prtcl_NBS_Munjiza.f90:409-468.
+// Six blocks per SM (40 registers): the walk is latency bound, and the extra
+// resident warps measured faster than the unconstrained 60-register build.
 template <bool kHier>
-__global__ void __launch_bounds__(kThreads) k_search(Dev d, int s_begin, int s_end) {
+__global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int s_end) {
   int s = s_begin + blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = *d.nt;
   const int nloc = *d.n;
