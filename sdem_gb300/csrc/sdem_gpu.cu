@@ -418,6 +418,20 @@ __global__ void k_ghost_count(Dev d) {
   *d.nt = *d.n + ng;
 }
 
+// The fourth word of a velocity record carries the particle's id and type
+// (low and high 32 bits), so that the force kernel learns both from the
+// velocity load it needs anyway instead of two more scattered loads.
+__device__ __forceinline__ double id_tag(int gid, int ptype) {
+  return __hiloint2double(ptype, gid);
+}
+__device__ __forceinline__ int tag_gid(double w) { return __double2loint(w); }
+__device__ __forceinline__ int tag_type(double w) { return __double2hiint(w); }
+
+__global__ void k_tag_vel(dbl4* __restrict__ vel0, const int* __restrict__ gid, const int* __restrict__ ptype, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) vel0[i].w = id_tag(gid[i], ptype[i]);
+}
+
 // Fixed spheres join the search after the images (zero velocities); in the
 // within-cell order they rank below every moving sphere and image (the
 // reference gives them search indices 1..nFixed, Prtcl_NBS_Munjiza.f90:86).
@@ -430,7 +444,7 @@ __global__ void k_fixed_append(Dev d) {
   d.posr[g] = d.fix_posr[f];
   d.gid[g] = d.fix_gid[f];
   d.ptype[g] = d.fix_ptype[f];
-  d.vel0[g] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+  d.vel0[g] = make_dbl4(0.0, 0.0, 0.0, id_tag(d.fix_gid[f], d.fix_ptype[f]));
   d.rv0[g] = make_dbl4(0.0, 0.0, 0.0, 0.0);
 }
 
@@ -818,26 +832,28 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     const int slot = c - d.row_off[s];
     int m = d.sorted[s];
     int q = d.row_partner[(size_t)slot * d.nall + s];
-    int gm = d.gid[m], gq = d.gid[q];
+    // both particles' state records; the velocity records carry id and type
+    const dbl4 Pm = d.posr[m], Pq = d.posr[q];
+    const dbl4 Vm = d.vel0[m], Vq = d.vel0[q], Wm = d.rv0[m], Wq = d.rv0[q];
+    const int gm = tag_gid(Vm.w), gq = tag_gid(Vq.w);
     // particle-particle (AddContactPP) or local-image (AddContactPPG) pair; the
     // lower id is particle i of the force law either way
     // (Prtcl_NBS_Munjiza.f90:525-529, Prtcl_CL_and_CF.f90:773-797)
     const bool img = kOneSided && ((m >= nloc) || (q >= nloc));
-    const int loc = (m >= nloc) ? q : m;     // the local particle of an image pair
-    const int oth = (loc == m) ? q : m;
-    bool m_lo = gm < gq;
-    int pid = m_lo ? m : q, pjd = m_lo ? q : m;
+    const bool m_loc = m < nloc;              // the local particle of an image pair is m
+    const int oth = m_loc ? q : m;
+    const bool m_lo = gm < gq;
     // Find_insert's bucket: the lower id's for PP, the local particle's for PPG
-    const int owner = img ? d.gid[loc] : (m_lo ? gm : gq);
-    const int partner = img ? d.gid[oth] : (m_lo ? gq : gm);
-    // particle state first: these loads do not depend on the history lookup
-    // below, so their latency overlaps its chain of dependent loads
-    const dbl4 Pi = d.posr[pid], Pj = d.posr[pjd];
-    const dbl4 Vi = d.vel0[pid], Vj = d.vel0[pjd], Wi = d.rv0[pid], Wj = d.rv0[pjd];
+    const int owner = img ? (m_loc ? gm : gq) : (m_lo ? gm : gq);
+    const int partner = img ? (m_loc ? gq : gm) : (m_lo ? gq : gm);
+    const dbl4 Pi = m_lo ? Pm : Pq, Pj = m_lo ? Pq : Pm;
+    const dbl4 Vi = m_lo ? Vm : Vq, Vj = m_lo ? Vq : Vm;
+    const dbl4 Wi = m_lo ? Wm : Wq, Wj = m_lo ? Wq : Wm;
     // Prtcl_BnryProp(pType(lower id), pType(higher id)) for PP (:743),
     // (pType(local), pType(image)) for PPG (:772)
-    const int ta = img ? d.ptype[loc] : d.ptype[pid];
-    const int tb = img ? d.ptype[oth] : d.ptype[pjd];
+    const int tm = tag_type(Vm.w), tq = tag_type(Vq.w);
+    const int ta = img ? (m_loc ? tm : tq) : (m_lo ? tm : tq);
+    const int tb = img ? (m_loc ? tq : tm) : (m_lo ? tq : tm);
     dbl4 hist = make_dbl4(0.0, 0.0, 0.0, -2.0);
     {
       const int k = d.own_cnt_prev[owner];
@@ -1064,7 +1080,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
     d.acc1[p] = sdem::d4(a1, 0.0);
     d.acc0[p] = sdem::d4(a1, 0.0);
   }
-  d.vel0[p] = sdem::d4(lv1_new, 0.0);
+  d.vel0[p] = sdem::d4(lv1_new, v1.w);   // keeps the id/type word
   d.posr[p] = sdem::d4(x, Pp.w);
 
   // rotational part (Prtcl_Integration.f90:55-86)
@@ -2428,6 +2444,7 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
     rc |= put(rotVel, c.rsize, h->rv);
     rc |= put(rotAcc, c.rsize, h->ra);
     if (rc) return rc;
+    k_tag_vel<<<grid_for(n), kThreads, 0, st>>>(h->vel[0], h->gid, h->ptype, n);
   }
   // history reset: both buffers empty; near-wall list refreshed at the next step
   size_t G = (size_t)c.max_gid + 1;
