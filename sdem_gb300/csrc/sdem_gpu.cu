@@ -178,7 +178,7 @@ struct Dev {
   int* status;                    // [0] error code, [1] detail
   unsigned long long* counters;   // [0] candidates, [1] PW contacts, [2..4] sums since upload: PP, PW, steps,
                                   // [5] contacts with periodic images (numCntcts(2))
-  unsigned long long* red;        // [0] max |v| bits, [1] max |a| bits
+  unsigned long long* red;        // per block of k_step_begin: max |v| bits, max |a| bits
   int* iter;
   int* next_update;
   int* out_cnt;
@@ -271,70 +271,102 @@ __global__ void k_scan_apply(const int* __restrict__ in, long long n, const int*
 }
 
 // ---------------------------------------------------------------------------
-// UpdateNearPrtclsPW (Prtcl_ContactSearchPW.f90:159-235): near-wall bit mask per
-// particle (walls whose AABB +- DeltaXmax2 holds the particle), max |v|, max |a|.
-// The start of a step: UpdateNearPrtclsPW when iter >= Next_iter_update (the
-// near-wall mask of every particle and the max |v|, |a| reductions; the last
-// block to finish computes the next refresh iteration), and the step's image
-// and gather-order counters reset (by that last block as well).
-__global__ void k_step_begin(Dev d) {
+// The start of a step.  UpdateNearPrtclsPW (Prtcl_ContactSearchPW.f90:159-235)
+// when iter >= Next_iter_update: the near-wall bit mask of every particle
+// (walls whose AABB +- DeltaXmax2 holds it) and max |v|, max |a|, reduced per
+// block into partials; the last block to finish reduces the partials and
+// computes the next refresh iteration.  Every step: the image and
+// gather-order counters reset.  A fixed grid (grid-stride over particles), so
+// that a step without refresh costs a few hundred block launches.
+constexpr int kBeginBlocksPerSM = 4;
+
+__device__ __forceinline__ void reset_step_counters(const Dev& d) {
+  *d.ng = 0;
+  *d.nt = *d.n;
+  for (int b = 0; b < kDegBuckets; b++) d.deg_cnt[b] = 0;   // gather-order buckets of this step
+}
+
+__global__ void __launch_bounds__(kThreads) k_step_begin(Dev d) {
   const bool refresh = *d.iter >= *d.next_update;
-  if (refresh) {
-    int n = *d.n;
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    double vmax = 0.0, amax = 0.0;
-    if (p < n) {
-      dbl4 P = d.posr[p];
-      unsigned long long mask = 0ull;
-      for (int k = 0; k < d.nw; k++) {
-        const double* r = d.walls + k * SDEM_W_SIZE;
-        double pminx = r[SDEM_W_MIN] - d.dx2, pminy = r[SDEM_W_MIN + 1] - d.dx2, pminz = r[SDEM_W_MIN + 2] - d.dx2;
-        double pmaxx = r[SDEM_W_MAX] + d.dx2, pmaxy = r[SDEM_W_MAX + 1] + d.dx2, pmaxz = r[SDEM_W_MAX + 2] + d.dx2;
-        if (P.x >= pminx && P.x <= pmaxx && P.y >= pminy && P.y <= pmaxy && P.z >= pminz && P.z <= pmaxz)
-          mask |= (1ull << k);
-      }
-      d.near_mask[p] = mask;
-      vmax = sdem::norm3(sdem::xyz(d.vel0[p]));
-      amax = sdem::norm3(sdem::xyz(d.acc0[p]));
-    }
-    // non-negative doubles order like their bit patterns
-    for (int o = 16; o > 0; o >>= 1) {
-      vmax = fmax(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
-      amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-      atomicMax(&d.red[0], (unsigned long long)__double_as_longlong(vmax));
-      atomicMax(&d.red[1], (unsigned long long)__double_as_longlong(amax));
-      __threadfence();
-    }
+  if (!refresh) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) reset_step_counters(d);
+    return;
   }
-  __shared__ int last;
+  // expanded wall boxes, pmin = min - DeltaXmax2 and pmax = max + DeltaXmax2
+  // (FP64, as the reference), once per block; the tests run on the integer pipes
+  __shared__ double box[64][6];
+  for (int e = threadIdx.x; e < d.nw * 6; e += blockDim.x) {
+    const int k = e / 6, c = e % 6;
+    const double* r = d.walls + k * SDEM_W_SIZE;
+    box[k][c] = c < 3 ? r[SDEM_W_MIN + c] - d.dx2 : r[SDEM_W_MAX + c - 3] + d.dx2;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(d.ticket, 1) == (int)gridDim.x - 1;
+  const int n = *d.n;
+  // non-negative doubles order like their bit patterns
+  unsigned long long vb = 0ull, ab = 0ull;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const dbl4 P = d.posr[p];
+    unsigned long long mask = 0ull;
+    for (int k = 0; k < d.nw; k++) {
+      if (fpi::ge(P.x, box[k][0]) && fpi::le(P.x, box[k][3]) && fpi::ge(P.y, box[k][1]) && fpi::le(P.y, box[k][4]) &&
+          fpi::ge(P.z, box[k][2]) && fpi::le(P.z, box[k][5]))
+        mask |= (1ull << k);
+    }
+    d.near_mask[p] = mask;
+    const unsigned long long v = fpi::bits(sdem::norm3(sdem::xyz(d.vel0[p])));
+    const unsigned long long a = fpi::bits(sdem::norm3(sdem::xyz(d.acc0[p])));
+    vb = v > vb ? v : vb;
+    ab = a > ab ? a : ab;
+  }
+  __shared__ unsigned long long part[kThreads / 32][2];
+  __shared__ int last;
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_down_sync(0xffffffffu, vb, o), a = __shfl_down_sync(0xffffffffu, ab, o);
+    vb = v > vb ? v : vb;
+    ab = a > ab ? a : ab;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    part[threadIdx.x >> 5][0] = vb;
+    part[threadIdx.x >> 5][1] = ab;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kThreads / 32; w++) {
+      vb = part[w][0] > vb ? part[w][0] : vb;
+      ab = part[w][1] > ab ? part[w][1] : ab;
+    }
+    d.red[2 * blockIdx.x] = vb;
+    d.red[2 * blockIdx.x + 1] = ab;
+    __threadfence();
+    last = atomicAdd(d.ticket, 1) == (int)gridDim.x - 1;
+  }
   __syncthreads();
   if (!last || threadIdx.x != 0) return;
   __threadfence();
   *d.ticket = 0;
-  if (refresh) {
-    const int it = *d.iter;
-    // read and clear the reductions at L2, where the other blocks' atomics went
-    double max_v = __longlong_as_double((long long)atomicExch(&d.red[0], 0ull));
-    double max_a = __longlong_as_double((long long)atomicExch(&d.red[1], 0ull));
-    max_v = max_v + d.max_wall_vel;
-    max_v = (max_v > 0.3) ? max_v : 0.3;
-    max_v = max_v * 1.5;
-    double gn = sdem::norm3(sdem::mk3(d.g.x, d.g.y, d.g.z));
-    max_a = (max_a > gn) ? max_a : gn;
-    max_a = max_a * 1.5;
-    double t = (sqrt(max_v * max_v + 2.0 * max_a * d.dx1) - max_v) / max_a;
-    int numIter = (int)(t / d.law.dt);
-    numIter = numIter > 1 ? numIter : 1;
-    numIter = numIter < d.wall_max_update_iter ? numIter : d.wall_max_update_iter;
-    *d.next_update = it + numIter;
+  // the other blocks' partials, read at L2 (never cached in this SM's L1)
+  vb = 0ull;
+  ab = 0ull;
+  for (int b = 0; b < (int)gridDim.x; b++) {
+    const unsigned long long v = __ldcg(&d.red[2 * b]), a = __ldcg(&d.red[2 * b + 1]);
+    vb = v > vb ? v : vb;
+    ab = a > ab ? a : ab;
   }
-  *d.ng = 0;
-  *d.nt = *d.n;
-  for (int b = 0; b < kDegBuckets; b++) d.deg_cnt[b] = 0;   // gather-order buckets of this step
+  const int it = *d.iter;
+  double max_v = fpi::from_bits(vb);
+  double max_a = fpi::from_bits(ab);
+  max_v = max_v + d.max_wall_vel;
+  max_v = (max_v > 0.3) ? max_v : 0.3;
+  max_v = max_v * 1.5;
+  double gn = sdem::norm3(sdem::mk3(d.g.x, d.g.y, d.g.z));
+  max_a = (max_a > gn) ? max_a : gn;
+  max_a = max_a * 1.5;
+  double t = (sqrt(max_v * max_v + 2.0 * max_a * d.dx1) - max_v) / max_a;
+  int numIter = (int)(t / d.law.dt);
+  numIter = numIter > 1 ? numIter : 1;
+  numIter = numIter < d.wall_max_update_iter ? numIter : d.wall_max_update_iter;
+  *d.next_update = it + numIter;
+  reset_step_counters(d);
 }
 
 // ---------------------------------------------------------------------------
@@ -1639,6 +1671,7 @@ struct sdem_h {
   // upload, [5] image pairs, [6..7] max |v|, |a| reductions, [8] fixed pairs,
   // [9] cross-level candidates
   unsigned long long* ull = nullptr;
+  unsigned long long* red_part = nullptr;   // k_step_begin's per-block maxima
   int *out_list = nullptr, *moves = nullptr, *map_pos = nullptr, *map_id = nullptr;
   int* h_counters = nullptr;  // pinned
   // mapped host copy of the device scalars, written by every step's last
@@ -1866,7 +1899,7 @@ Dev make_dev(sdem_h* h) {
   d.wh_hist_prev = h->wh_hist[pv];
   d.status = h->scal + S_STATUS;
   d.counters = h->ull;
-  d.red = h->ull + 6;
+  d.red = h->red_part;
   d.iter = h->scal + S_ITER;
   d.next_update = h->scal + S_NEXT;
   d.out_cnt = h->scal + S_OUTCNT;
@@ -1898,7 +1931,7 @@ int enqueue_step(sdem_h* h) {
   long long L = 0;
   mark(PH_WALL);
   // the refresh schedule (Next_iter_update) advances with or without walls
-  k_step_begin<<<grid_for(n), kThreads, 0, st>>>(d);
+  k_step_begin<<<h->num_sms * kBeginBlocksPerSM, kThreads, 0, st>>>(d);
   L += 1;
   mark(PH_BIN);
   const int na = n + h->gcap + h->nfix;   // search arrays: locals, periodic images, fixed spheres
@@ -2187,6 +2220,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   }
   rc |= dalloc(h, &h->scal, S_SIZE);
   rc |= dalloc(h, &h->ull, 10);
+  rc |= dalloc(h, &h->red_part, 2 * (size_t)h->num_sms * kBeginBlocksPerSM);
   rc |= dalloc(h, &h->out_list, kOutCap);
   rc |= dalloc(h, &h->moves, 1 + 2 * 5 * kOutCap + 5 * kOutCap);
   rc |= dalloc(h, &h->map_pos, 5 * kOutCap);
