@@ -277,7 +277,7 @@ int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatch
  * search (num_Cnsv_cntct) on the grid that sdem_create + sdem_set_types would
  * build from cfg and the largest radius max_radius, and writes them to
  * d_counts[0..1] (device memory).  It allocates nothing: its scratch is one
- * fixed-size device array in the library (about 6.3 MB, held by every GPU
+ * fixed-size device array in the library (about 7.3 MB, held by every GPU
  * that loads the library until the process exits), which limits n to
  * SDEM_NOALLOC_MAX_PARTICLES and the grid to SDEM_NOALLOC_MAX_CELLS; larger
  * inputs are refused with SDEM_E_CAPACITY.  The first call on a device looks

@@ -295,6 +295,58 @@ __host__ __device__ __forceinline__ int floor_in_range(double q, int n) {
   return v < (uint64_t)n ? (int)v : -1;
 }
 
+// (q - k) in Q1.31, truncated, for the quotient q >= 0 and its floor k
+// (0 <= k < 2^31).
+__host__ __device__ __forceinline__ int32_t frac31(double q, int k) {
+  const uint64_t u = bits(q);
+  const uint32_t e = (uint32_t)(u >> 52) & 0x7FFu;
+  const uint64_t m = (u & kMant) | (e ? kHid : 0ull);
+  const int s = (e ? (int)e : 1) - 1023 - 20;    // q * 2^32 = m * 2^s, s <= 10
+  const uint64_t qf = s >= 0 ? (m << s) : (s > -64 ? (m >> -s) : 0ull);
+  return (int32_t)((qf - ((uint64_t)k << 32)) >> 1);
+}
+
+// floor(x / y) of the IEEE quotient as an int in [0, n), else -1 (as
+// floor_in_range of div_by), and where x / y lies inside that unit: off31 =
+// (x/y - floor) in Q1.31, within 2^-29 (an estimate for single-precision
+// copies, not part of the exact result).  Fast path (positive normal x and y,
+// quotient below 2^27): the quotient in Q32.32 from the divisor's reciprocal,
+// error below 2^-30; the rounded quotient differs from the exact one by less
+// than q*2^-53 < 2^-26, so when the estimate is at least 2^-20 from an integer
+// both have the floor of the estimate.  Other operands, and estimates inside
+// that band, take the exact division.
+__host__ __device__ __forceinline__ int floor_div(double x, const Divisor& v, int n, int32_t& off31) {
+  const uint64_t a = bits(x);
+  const uint32_t ea = (uint32_t)(a >> 52);     // the sign bit makes negatives large
+  const int sh = (int)ea - (int)v.eb;          // x/y = (mx/my) * 2^sh
+  if (ea - 1u < 2046u && v.normal && (bits(v.y) >> 63) == 0 && sh <= 26) {
+    const uint64_t ma = (a & kMant) | kHid;
+    const uint64_t r61 = mulhi(ma << 11, (uint64_t)v.z);   // mx/my in Q3.61
+    const int rs = 29 - sh;
+    const uint64_t qf = rs >= 64 ? 0ull : (r61 >> rs);     // ~x/y in Q32.32
+    const uint32_t fr = (uint32_t)qf;
+    if (fr >= (1u << 12) && fr <= 0xFFFFFFFFu - (1u << 12)) {
+      off31 = (int32_t)(fr >> 1);
+      const uint64_t k = qf >> 32;
+      return k < (uint64_t)n ? (int)k : -1;
+    }
+  }
+  const double q = div_by(x, v);
+  const int k = floor_in_range(q, n);
+  off31 = k >= 0 ? frac31(q, k) : 0;
+  return k;
+}
+
+// A single-precision copy of x for estimates: truncated (relative error below
+// 2^-23) from the bits for normal x in the float range, else converted.
+__host__ __device__ __forceinline__ float to_float_trunc(double x) {
+  const uint64_t u = bits(x);
+  const uint32_t e = (uint32_t)(u >> 52) & 0x7FFu;
+  if (e - 897u < 254u)   // 2^-126 <= |x| < 2^128
+    return ffrom((uint32_t)(u >> 63) << 31 | (e - 896u) << 23 | (uint32_t)((u & kMant) >> 29));
+  return (float)x;
+}
+
 // x * (-0.5), exact for every x whose half is a normal number or zero: the
 // exponent field drops by one and the sign flips.  Subnormal halves (which
 // round), infinities and NaNs take the hardware multiplication.

@@ -82,6 +82,7 @@ struct LevelGrid {
   long long base;
   double cell;
   float cellf;
+  fpi::Divisor div;   // the cell length as a divisor (reciprocal refined once, on the host)
 };
 constexpr int kImgFlag = 1 << 30; // c_ogid bit: a pair with a periodic image (ids < 2^30)
 
@@ -139,7 +140,9 @@ struct Dev {
   unsigned long long* near_mask;
   // binning
   int *cell_of, *cell_cnt, *cell_start, *tmp_rank, *tmp_sorted, *sorted, *sortpos;
-  float4* spos;      // cell-sorted single-precision copy (x-x0, y-y0, z-z0, r) for the prefilter
+  float4* spos;      // cell-sorted single-precision copy (offsets in the cell, r) for the prefilter
+  float4* pf;        // the same per particle index, written by the binning
+  fpi::Divisor cdiv; // the cell length as a divisor
   float pf_margin;   // prefilter margin, bounds the single-precision distance error
   float cellf;       // cell size in single precision
   // rows and in-lists
@@ -490,26 +493,31 @@ __global__ void k_bin(Dev d) {
   const dbl4 P = d.posr[p];
   // the grid of the particle's level (hierarchical search: by type,
   // NBSMH_clcBoxIndex_and_BuildYList, Prtcl_Hrchl_Munjiza.f90:247-336)
-  double cell = d.cell;
+  const fpi::Divisor* dc = &d.cdiv;
+  float cellf = d.cellf;
   int nx = d.nx, ny = d.ny, nz = d.nz;
   long long base = 0;
   if (d.hier) {
     const LevelGrid& G = d.lv[d.type_lvl[d.ptype[p] - 1]];
-    cell = G.cell;
+    dc = &G.div;
+    cellf = G.cellf;
     nx = G.nx; ny = G.ny; nz = G.nz;
     base = G.base;
   }
-  // floor((x - x0) / cell_len), the quotient IEEE-rounded; division and
-  // floor on the integer pipes.  The reference's index is this + 1.
-  const fpi::Divisor dc = fpi::divisor(cell);
-  const int fx = fpi::floor_in_range(fpi::div_by(P.x - d.x0, dc), nx);
-  const int fy = fpi::floor_in_range(fpi::div_by(P.y - d.y0, dc), ny);
-  const int fz = fpi::floor_in_range(fpi::div_by(P.z - d.z0, dc), nz);
+  // floor((x - x0) / cell_len), the quotient IEEE-rounded, on the integer
+  // pipes; the reference's index is this + 1.  The offsets inside the cell
+  // become the single-precision prefilter copy.
+  int32_t ox, oy, oz;
+  const int fx = fpi::floor_div(P.x - d.x0, *dc, nx, ox);
+  const int fy = fpi::floor_div(P.y - d.y0, *dc, ny, oy);
+  const int fz = fpi::floor_div(P.z - d.z0, *dc, nz, oz);
   if (fx < 0 || fy < 0 || fz < 0) {
     raise(d, SDEM_E_GRID, p);
     d.cell_of[p] = -1;
     return;
   }
+  const float sc = cellf * 0x1p-31f;
+  d.pf[p] = make_float4((float)ox * sc, (float)oy * sc, (float)oz * sc, fpi::to_float_trunc(P.w));
   long long key = base + ((long long)fy * nx + (long long)fx) * nz + (long long)fz;
   d.cell_of[p] = (int)key;
   d.tmp_rank[p] = atomicAdd(&d.cell_cnt[key], 1);
@@ -543,21 +551,9 @@ __global__ void k_cellorder(Dev d) {
   for (int t = a; t < b; t++) rank += (ref_key(d.tmp_sorted[t]) > kp);
   d.sorted[a + rank] = p;
   d.sortpos[p] = a + rank;
-  dbl4 P = d.posr[p];
-  // single-precision copy relative to the particle's own cell corner: all
-  // values are below one cell, so their rounding error is ~cell*2^-24
-  int lk = key, lnx = d.nx, lnz = d.nz;
-  double lcell = d.cell;
-  if (d.hier) {
-    const LevelGrid& G = d.lv[d.type_lvl[d.ptype[p] - 1]];
-    lk = (int)(key - G.base);
-    lnx = G.nx; lnz = G.nz;
-    lcell = G.cell;
-  }
-  const int cz = lk % lnz, cr = lk / lnz;
-  const int cx = cr % lnx, cy = cr / lnx;
-  d.spos[a + rank] = make_float4((float)(P.x - (d.x0 + (double)cx * lcell)), (float)(P.y - (d.y0 + (double)cy * lcell)),
-                                 (float)(P.z - (d.z0 + (double)cz * lcell)), (float)P.w);
+  // single-precision copy relative to the particle's own cell corner (made
+  // by the binning)
+  d.spos[a + rank] = d.pf[p];
 }
 
 // ---------------------------------------------------------------------------
@@ -1337,6 +1333,10 @@ __global__ void k_selftest_fp64(long long n, unsigned long long seed, unsigned l
     const double q = __ddiv_rn(x, y), f = floor(q);
     const int want = (f >= 0.0 && f < 4000.0) ? (int)f : -1;
     ok = ok && fpi::floor_in_range(q, 4000) == want;
+    int32_t off = 0;
+    const int kq = fpi::floor_div(x, fpi::divisor(y), 4000, off);
+    ok = ok && kq == want;
+    if (kq >= 0 && fabs(q) < 0x1p26) ok = ok && fabs((double)off * 0x1p-31 - (q - (double)kq)) <= 0x1p-26;
     nb += ok ? 0ull : 1ull;
   }
   if (nb) atomicAdd(bad, nb);
@@ -1492,7 +1492,7 @@ __global__ void k_finish(Dev d, int* counters_out, const int* scal, int* mirror,
 // hold on the device, e.g. to size their contact buffers before creating a
 // handle.  The scratch this needs (search grid, counting sort, prefilter copy)
 // is a file-scope device array of fixed size: every GPU that loads the library
-// holds it, ~6.3 MB, until the process exits.
+// holds it, ~7.3 MB, until the process exits.
 constexpr int kNaMaxN = 1 << 16;       // SDEM_NOALLOC_MAX_PARTICLES
 constexpr int kNaMaxCells = 1 << 19;   // SDEM_NOALLOC_MAX_CELLS
 constexpr int kNaBlocks = (kNaMaxCells + kScanTile - 1) / kScanTile;
@@ -1505,6 +1505,7 @@ struct NoAllocScratch {
   int sorted[kNaMaxN];
   int sortpos[kNaMaxN];
   float4 spos[kNaMaxN];
+  float4 pf[kNaMaxN];
   int bsum[kNaBlocks];
   int n;
   int status[2];
@@ -1659,6 +1660,7 @@ struct sdem_h {
   int *w_cnt = nullptr, *w_wall = nullptr, *wl = nullptr;
   dbl4 *w_geo = nullptr, *w_S = nullptr, *w_M = nullptr, *w_Mr = nullptr;
   float4* spos = nullptr;
+  float4* pf = nullptr;
   float pf_margin = 0.f;
   int *deg_cnt = nullptr, *deg_of = nullptr, *deg_rank = nullptr, *gorder = nullptr;
   // second stream and events of the chunked search/force pipeline
@@ -1856,6 +1858,8 @@ Dev make_dev(sdem_h* h) {
   d.sorted = h->sorted;
   d.sortpos = h->sortpos;
   d.spos = h->spos;
+  d.pf = h->pf;
+  d.cdiv = fpi::divisor(h->cell);
   d.deg_cnt = h->deg_cnt;
   d.deg_of = h->deg_of;
   d.deg_rank = h->deg_rank;
@@ -2185,6 +2189,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->sorted, NA);
   rc |= dalloc(h, &h->sortpos, NA);
   rc |= dalloc(h, &h->spos, NA);
+  rc |= dalloc(h, &h->pf, NA);
   rc |= dalloc(h, &h->deg_cnt, kDegBuckets);
   rc |= dalloc(h, &h->deg_of, N);
   rc |= dalloc(h, &h->deg_rank, N);
@@ -2308,6 +2313,7 @@ int sdem_set_types(sdem_h* h, int nT, const double* radius, const double* mass, 
         G.mult = idh;
         G.cell = cl;
         G.cellf = (float)cl;
+        G.div = fpi::divisor(cl);
       }
       nx *= 2; ny *= 2; nz *= 2;
       maxD_lvl = minD_lvl;
@@ -3185,6 +3191,8 @@ int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, c
   d.sorted = S->sorted;
   d.sortpos = S->sortpos;
   d.spos = S->spos;
+  d.pf = S->pf;
+  d.cdiv = fpi::divisor(cell);
   d.pf_margin = (float)(32.0 * cell * std::ldexp(1.0, -23));
   d.cellf = (float)cell;
   const int g = std::max(1, (n + kThreads - 1) / kThreads);

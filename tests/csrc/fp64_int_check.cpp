@@ -1,6 +1,6 @@
 // CPU check of sdem_gb300/csrc/fp64_int.cuh: the integer-pipe binary64
-// sqrt, division, comparisons, -x/2 and grid floor against the host's IEEE
-// arithmetic.
+// sqrt, division, comparisons, -x/2, grid floor and floor of a quotient
+// against the host's IEEE arithmetic.
 // Usage: fp64_int_check <seed> <pairs per family>; prints "ok <n>" or the
 // first mismatches and exits 1.
 #include <cmath>
@@ -39,7 +39,29 @@ static bool same(double a, double b) {
 }
 
 static long bad = 0, checked = 0;
+// floor_div: the floor of the IEEE quotient for a few grid sizes, and the
+// in-unit offset estimate within 2^-26 of q - floor (quotients below 2^26)
+static void check_floor_div(double x, double y) {
+  const fpi::Divisor v = fpi::divisor(y);
+  const int ns[3] = {1, 37, 1000000};
+  const double q = x / y, f = std::floor(q);
+  for (int j = 0; j < 3; j++) {
+    int32_t off = 0;
+    const int k = fpi::floor_div(x, v, ns[j], off);
+    const int want = (f >= 0.0 && f < (double)ns[j]) ? (int)f : -1;
+    checked++;
+    if (k != want) {
+      if (bad < 20) printf("MISMATCH floor_div x=%a y=%a n=%d got=%d want=%d\n", x, y, ns[j], k, want);
+      bad++;
+    } else if (k >= 0 && std::fabs(q) < 0x1p26 && std::fabs(off * 0x1p-31 - (q - (double)k)) > 0x1p-26) {
+      if (bad < 20) printf("MISMATCH floor_div offset x=%a y=%a off=%d q-k=%a\n", x, y, off, q - (double)k);
+      bad++;
+    }
+  }
+}
+
 static void check(double x, double y) {
+  check_floor_div(x, y);
   const double r[4] = {fpi::mul_neg_half(x), fpi::sqrt_rn(x), fpi::div_rn(x, y), fpi::div_rn(y, x)};
   const double e[4] = {x * -0.5, std::sqrt(x), x / y, y / x};
   const char* nm[4] = {"mul_neg_half", "sqrt", "div", "div(y,x)"};
@@ -116,6 +138,11 @@ int main(int argc, char** argv) {
       const double xx = ((double)(int64_t)(g() % 4000) - 100.0) * cell + ((double)(g() % 2001) - 1000.0) * 1e-19;
       check(xx, cell);
       check(-0.0, cell);
+      // the neighbours of an exact multiple of the cell: quotients within an
+      // ulp of an integer, on both sides
+      const double mk = (double)(int64_t)(g() % 4000) * cell;
+      check_floor_div(D(B(mk) + (g() % 9) - 4), cell);
+      check_floor_div(std::fabs(xx), cell);
     }
     // equal values, signed zeros and neighbours for the comparisons
     {
