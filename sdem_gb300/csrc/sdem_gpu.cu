@@ -66,7 +66,8 @@ constexpr int kMaxK = 64;         // row / in-list capacity limit (6-bit slot in
 constexpr int kKw = 4;            // wall contacts per particle
 constexpr int kMaxWalls = 64;     // near-wall mask is 64 bits
 constexpr int kOutCap = 4096;     // out-of-domain deletions per step
-constexpr int kScanTile = 4096;   // elements per scan block (1024 threads x 4)
+constexpr int kScanThreads = 256, kScanItems = 32;
+constexpr int kScanTile = kScanThreads * kScanItems;   // elements per scan block
 constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact records
 #ifndef SDEM_PIPELINE_CHUNKS
 #define SDEM_PIPELINE_CHUNKS 2
@@ -197,22 +198,37 @@ __device__ __forceinline__ void raise(const Dev& d, int code, int detail) {
 }
 
 // ---------------------------------------------------------------------------
-// Exclusive scan of int32 (n elements) into out[0..n], out[n] = total.
-__global__ void k_scan_reduce(const int* __restrict__ in, long long n, int* __restrict__ bsum) {
-  __shared__ int warp_sums[32];
-  long long base = (long long)blockIdx.x * kScanTile;
+// Exclusive scan of int32 (n elements) into out[0..n], out[n] = total, in
+// three launches: tile sums, a scan of the tile sums, the tiles.  A tile is
+// 256 threads x 32 elements; full, 16-byte-aligned tiles move as int4
+// (each load instruction covers 512 contiguous bytes of a warp).
+__device__ __forceinline__ bool scan_vec_ok(const int* p, long long base, long long n) {
+  return base + kScanTile <= n && ((reinterpret_cast<uintptr_t>(p) & 15u) == 0);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int* __restrict__ in, long long n,
+                                                               int* __restrict__ bsum) {
+  __shared__ int warp_sums[kScanThreads / 32];
+  const long long base = (long long)blockIdx.x * kScanTile;
   int s = 0;
-  for (int k = 0; k < 4; k++) {
-    long long i = base + (long long)k * 1024 + threadIdx.x;
-    if (i < n) s += in[i];
+  if (scan_vec_ok(in, base, n)) {
+    const int4* v = reinterpret_cast<const int4*>(in + base);
+#pragma unroll
+    for (int j = 0; j < kScanItems / 4; j++) {
+      const int4 q = v[j * kScanThreads + threadIdx.x];
+      s += (q.x + q.y) + (q.z + q.w);
+    }
+  } else {
+    for (int e = threadIdx.x; e < kScanTile; e += kScanThreads)
+      if (base + e < n) s += in[base + e];
   }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = s;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    int v = warp_sums[threadIdx.x];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (threadIdx.x == 0) bsum[blockIdx.x] = v;
+  if (threadIdx.x == 0) {
+    int v = 0;
+    for (int w = 0; w < kScanThreads / 32; w++) v += warp_sums[w];
+    bsum[blockIdx.x] = v;
   }
 }
 
@@ -256,21 +272,78 @@ __global__ void k_scan_blocks(int* bsum, int nb) {
   }
 }
 
-// out[i] = *offset + sum of in[0..i), out[n] = the total (offset may be null)
-__global__ void k_scan_apply(const int* __restrict__ in, long long n, const int* __restrict__ bsum,
-                             int* __restrict__ out, const int* __restrict__ offset) {
-  __shared__ int sh[33];
-  long long base = (long long)blockIdx.x * kScanTile;
-  int carry = bsum[blockIdx.x] + (offset ? *offset : 0);
-  for (int k = 0; k < 4; k++) {
-    long long i = base + (long long)k * 1024 + threadIdx.x;
-    int v = (i < n) ? in[i] : 0;
-    int tot;
-    int e = block_exclusive_scan_1024(v, sh, &tot);
-    if (i < n) out[i] = carry + e;
-    carry += tot;
+// out[i] = *offset + sum of in[0..i), out[n] = the total (offset may be null).
+// The tile goes through shared memory (padded: element e at e + e/32, so that
+// both the striped int4 copies and the per-thread runs of 32 are free of bank
+// conflicts); each thread scans its 32 consecutive elements, the block scans
+// the 256 thread totals.
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int* __restrict__ in, long long n,
+                                                              const int* __restrict__ bsum, int* __restrict__ out,
+                                                              const int* __restrict__ offset) {
+  __shared__ int sh[kScanTile + kScanTile / 32];
+  __shared__ int wsum[kScanThreads / 32 + 1];
+  const int t = threadIdx.x;
+  const long long base = (long long)blockIdx.x * kScanTile;
+  auto pad = [](int e) { return e + (e >> 5); };
+  if (scan_vec_ok(in, base, n)) {
+    const int4* v = reinterpret_cast<const int4*>(in + base);
+#pragma unroll
+    for (int j = 0; j < kScanItems / 4; j++) {
+      const int4 q = v[j * kScanThreads + t];
+      const int e = pad((j * kScanThreads + t) * 4);
+      sh[e] = q.x;
+      sh[e + 1] = q.y;
+      sh[e + 2] = q.z;
+      sh[e + 3] = q.w;
+    }
+  } else {
+    for (int e = t; e < kScanTile; e += kScanThreads) sh[pad(e)] = base + e < n ? in[base + e] : 0;
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = carry;
+  __syncthreads();
+  int loc[kScanItems];
+  int sum = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) {
+    const int v = sh[t * (kScanItems + 1) + i];
+    loc[i] = sum;
+    sum += v;
+  }
+  // exclusive scan of the thread totals
+  const int lane = t & 31, w = t >> 5;
+  int x = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (t == 0) {
+    int acc = 0;
+    for (int k = 0; k < kScanThreads / 32; k++) {
+      const int c = wsum[k];
+      wsum[k] = acc;
+      acc += c;
+    }
+    wsum[kScanThreads / 32] = acc;
+  }
+  __syncthreads();
+  const int carry = bsum[blockIdx.x] + (offset ? *offset : 0);
+  const int first = carry + wsum[w] + x - sum;
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) sh[t * (kScanItems + 1) + i] = first + loc[i];
+  __syncthreads();
+  if (scan_vec_ok(out, base, n)) {
+    int4* v = reinterpret_cast<int4*>(out + base);
+#pragma unroll
+    for (int j = 0; j < kScanItems / 4; j++) {
+      const int e = pad((j * kScanThreads + t) * 4);
+      v[j * kScanThreads + t] = make_int4(sh[e], sh[e + 1], sh[e + 2], sh[e + 3]);
+    }
+  } else {
+    for (int e = t; e < kScanTile; e += kScanThreads)
+      if (base + e < n) out[base + e] = sh[pad(e)];
+  }
+  if (blockIdx.x == gridDim.x - 1 && t == 0) out[n] = carry + wsum[kScanThreads / 32];
 }
 
 // ---------------------------------------------------------------------------
@@ -516,8 +589,10 @@ __global__ void k_bin(Dev d) {
     d.cell_of[p] = -1;
     return;
   }
-  const float sc = cellf * 0x1p-31f;
-  d.pf[p] = make_float4((float)ox * sc, (float)oy * sc, (float)oz * sc, fpi::to_float_trunc(P.w));
+  // offset in [0, 1) as a float from its top 23 bits (1.f - 1 is exact; an
+  // int-to-float conversion would take the FP64 pipe's rate)
+  auto unit = [](int32_t o) { return __uint_as_float(0x3F800000u | ((uint32_t)o >> 8)) - 1.0f; };
+  d.pf[p] = make_float4(unit(ox) * cellf, unit(oy) * cellf, unit(oz) * cellf, fpi::to_float_trunc(P.w));
   long long key = base + ((long long)fy * nx + (long long)fx) * nz + (long long)fz;
   d.cell_of[p] = (int)key;
   d.tmp_rank[p] = atomicAdd(&d.cell_cnt[key], 1);
@@ -1042,14 +1117,13 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
       Mr = d.w_Mr[at];
     }
     // F(pid) + (Fnij+Ftij) / F(pjd) - (Fnij+Ftij);
-    // T + r*Moment + Mrij / T + r*Moment - Mrij  (Prtcl_ContactForce_inc.f90:69-86)
-    if (p_lo) {
-      F = sdem::add3(F, sdem::xyz(S));
-      T = sdem::add3(sdem::add3(T, sdem::xyz(Ms)), sdem::xyz(Mr));
-    } else {
-      F = sdem::sub3(F, sdem::xyz(S));
-      T = sdem::sub3(sdem::add3(T, sdem::xyz(Ms)), sdem::xyz(Mr));
-    }
+    // T + r*Moment + Mrij / T + r*Moment - Mrij  (Prtcl_ContactForce_inc.f90:69-86).
+    // x - y is x + (-y) in IEEE arithmetic: the side's sign goes onto the
+    // record's sign bits, so that every lane runs the same FP64 additions.
+    const uint64_t sg = p_lo ? 0ull : fpi::kSign;
+    auto flip = [sg](double v) { return fpi::from_bits(fpi::bits(v) ^ sg); };
+    F = sdem::add3(F, sdem::mk3(flip(S.x), flip(S.y), flip(S.z)));
+    T = sdem::add3(sdem::add3(T, sdem::xyz(Ms)), sdem::mk3(flip(Mr.x), flip(Mr.y), flip(Mr.z)));
   }
   d.F[p] = sdem::d4(F, 0.0);
   d.T[p] = sdem::d4(T, 0.0);
@@ -1918,9 +1992,9 @@ int grid_for(long long n) { return (int)std::max<long long>(1, (n + kThreads - 1
 
 void scan(sdem_h* h, const int* in, long long n, int* out, const int* offset = nullptr) {
   int nb = (int)std::max<long long>(1, (n + kScanTile - 1) / kScanTile);
-  k_scan_reduce<<<nb, 1024, 0, h->stream>>>(in, n, h->scan_tmp);
+  k_scan_reduce<<<nb, kScanThreads, 0, h->stream>>>(in, n, h->scan_tmp);
   k_scan_blocks<<<1, 1024, 0, h->stream>>>(h->scan_tmp, nb);
-  k_scan_apply<<<nb, 1024, 0, h->stream>>>(in, n, h->scan_tmp, out, offset);
+  k_scan_apply<<<nb, kScanThreads, 0, h->stream>>>(in, n, h->scan_tmp, out, offset);
 }
 
 int enqueue_step(sdem_h* h) {
@@ -1973,7 +2047,11 @@ int enqueue_step(sdem_h* h) {
   // stream, so that every phase has its own events.
   const int nchunk = ev ? 1 : kChunks;
   cudaStream_t s2 = ev ? st : h->stream2;
-  auto cut = [&](int k) { return (int)((long long)na * k / nchunk); };
+  // chunk boundaries on scan tiles, so that each chunk's row scan moves whole
+  // aligned tiles
+  auto cut = [&](int k) {
+    return k == nchunk ? na : (int)(((long long)na * k / nchunk) & ~(long long)(kScanTile - 1));
+  };
   if (s2 != st) {
     cudaEventRecord(h->ev_fork, st);
     cudaStreamWaitEvent(s2, h->ev_fork, 0);
@@ -3202,9 +3280,9 @@ int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, c
   k_bin<<<g, kThreads, 0, st>>>(d);
   {
     const int nb = (int)std::max<long long>(1, (ncell + kScanTile - 1) / kScanTile);
-    k_scan_reduce<<<nb, 1024, 0, st>>>(S->cell_cnt, ncell, S->bsum);
+    k_scan_reduce<<<nb, kScanThreads, 0, st>>>(S->cell_cnt, ncell, S->bsum);
     k_scan_blocks<<<1, 1024, 0, st>>>(S->bsum, nb);
-    k_scan_apply<<<nb, 1024, 0, st>>>(S->cell_cnt, ncell, S->bsum, S->cell_start, nullptr);
+    k_scan_apply<<<nb, kScanThreads, 0, st>>>(S->cell_cnt, ncell, S->bsum, S->cell_start, nullptr);
   }
   k_scatter<<<g, kThreads, 0, st>>>(d);
   k_cellorder<<<g, kThreads, 0, st>>>(d);
