@@ -1129,16 +1129,39 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   d.T[p] = sdem::d4(T, 0.0);
 }
 
-// Per particle in index order (coalesced state): clc_Acceleration,
-// Prtcl_Integrate and the periodic wrap / out-of-domain flag.
-__global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= *d.n) return;
-  const dbl4 Pp = d.posr[p];
-  const r3 F = sdem::xyz(d.F[p]), T = sdem::xyz(d.T[p]);
-  const dbl4 v1 = d.vel0[p];
-  const dbl4 w1 = d.rv0[p];
-  const int ti = d.ptype[p];
+// Per particle: clc_Acceleration, Prtcl_Integrate and the periodic wrap /
+// out-of-domain flag.  The state records a particle's update reads (the
+// rotational history after the linear).
+enum IntField { IF_POSR, IF_F, IF_T, IF_V0, IF_W0, IF_TH, IF_V1, IF_A1, IF_V2, IF_A2, IF_W1, IF_AL1, IF_W2, IF_AL2,
+                IF_N };
+
+__device__ __forceinline__ const dbl4* int_src(const Dev& d, int f) {
+  switch (f) {
+    case IF_POSR: return d.posr;
+    case IF_F: return d.F;
+    case IF_T: return d.T;
+    case IF_V0: return d.vel0;
+    case IF_W0: return d.rv0;
+    case IF_TH: return d.theta;
+    case IF_V1: return d.vel1;
+    case IF_A1: return d.acc1;
+    case IF_V2: return d.vel2;
+    case IF_A2: return d.acc2;
+    case IF_W1: return d.rv1;
+    case IF_AL1: return d.ra1;
+    case IF_W2: return d.rv2;
+    default: return d.ra2;
+  }
+}
+
+// get(f) returns the particle's record of field f (from shared memory or HBM)
+template <class Get>
+__device__ __forceinline__ void integrate_body(const Dev& d, const int p, const Get& get) {
+  const dbl4 Pp = get(IF_POSR);
+  const r3 F = sdem::xyz(get(IF_F)), T = sdem::xyz(get(IF_T));
+  const dbl4 v1 = get(IF_V0);
+  const dbl4 w1 = get(IF_W0);
+  const int ti = tag_type(v1.w);
 
   // clc_Acceleration, Prtcl_DEMSystem.f90:174-180
   // F/Mass and T/Inertia (IEEE quotients)
@@ -1162,16 +1185,16 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
     lv1_new = sdem::add3(lv1, sdem::scale3(a1, dt));
     d.acc0[p] = sdem::d4(a1, 0.0);
   } else if (d.pi == SDEM_PIM_AB2) {
-    r3 lv2 = sdem::xyz(d.vel1[p]);
-    r3 la2 = sdem::xyz(d.acc1[p]);
+    r3 lv2 = sdem::xyz(get(IF_V1));
+    r3 la2 = sdem::xyz(get(IF_A1));
     x = sdem::add3(x, sdem::scale3(sdem::add3(sdem::scale3(lv1, AB2C1), nh3(lv2)), dt));
     lv1_new = sdem::add3(lv1, sdem::scale3(sdem::add3(sdem::scale3(a1, AB2C1), nh3(la2)), dt));
     d.vel1[p] = sdem::d4(lv1, 0.0);
     d.acc1[p] = sdem::d4(a1, 0.0);
     d.acc0[p] = sdem::d4(a1, 0.0);
   } else {
-    r3 lv2 = sdem::xyz(d.vel1[p]), lv3 = sdem::xyz(d.vel2[p]);
-    r3 la2 = sdem::xyz(d.acc1[p]), la3 = sdem::xyz(d.acc2[p]);
+    r3 lv2 = sdem::xyz(get(IF_V1)), lv3 = sdem::xyz(get(IF_V2));
+    r3 la2 = sdem::xyz(get(IF_A1)), la3 = sdem::xyz(get(IF_A2));
     x = sdem::add3(x, sdem::scale3(sdem::add3(sdem::add3(sdem::scale3(lv1, AB3C1), sdem::scale3(lv2, AB3C2)),
                                               sdem::scale3(lv3, AB3C3)), dt));
     lv1_new = sdem::add3(lv1, sdem::scale3(sdem::add3(sdem::add3(sdem::scale3(a1, AB3C1), sdem::scale3(la2, AB3C2)),
@@ -1186,7 +1209,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
   d.posr[p] = sdem::d4(x, Pp.w);
 
   // rotational part (Prtcl_Integration.f90:55-86)
-  r3 th = sdem::xyz(d.theta[p]);
+  r3 th = sdem::xyz(get(IF_TH));
   r3 rw1 = sdem::xyz(w1);
   if (d.pri == SDEM_PIM_FE) {
     th = sdem::add3(th, sdem::scale3(rw1, dt));
@@ -1195,16 +1218,16 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
   } else if (d.pri == SDEM_PIM_AB2) {
     // Prtcl_Integration.f90:64 starts from GPrtcl_linVel(1,i), already updated
     r3 wa = d.quirk ? lv1_new : rw1;
-    r3 rw2 = sdem::xyz(d.rv1[p]);
-    r3 ra2 = sdem::xyz(d.ra1[p]);
+    r3 rw2 = sdem::xyz(get(IF_W1));
+    r3 ra2 = sdem::xyz(get(IF_AL1));
     th = sdem::add3(th, sdem::scale3(sdem::add3(sdem::scale3(wa, AB2C1), nh3(rw2)), dt));
     d.rv0[p] = sdem::d4(sdem::add3(wa, sdem::scale3(sdem::add3(sdem::scale3(al1, AB2C1), nh3(ra2)), dt)), 0.0);
     d.rv1[p] = sdem::d4(wa, 0.0);
     d.ra1[p] = sdem::d4(al1, 0.0);
     d.ra0[p] = sdem::d4(al1, 0.0);
   } else {
-    r3 rw2 = sdem::xyz(d.rv1[p]), rw3 = sdem::xyz(d.rv2[p]);
-    r3 ra2 = sdem::xyz(d.ra1[p]), ra3 = sdem::xyz(d.ra2[p]);
+    r3 rw2 = sdem::xyz(get(IF_W1)), rw3 = sdem::xyz(get(IF_W2));
+    r3 ra2 = sdem::xyz(get(IF_AL1)), ra3 = sdem::xyz(get(IF_AL2));
     th = sdem::add3(th, sdem::scale3(sdem::add3(sdem::add3(sdem::scale3(rw1, AB3C1), sdem::scale3(rw2, AB3C2)),
                                                 sdem::scale3(rw3, AB3C3)), dt));
     d.rv0[p] = sdem::d4(sdem::add3(rw1, sdem::scale3(sdem::add3(sdem::add3(sdem::scale3(al1, AB3C1), sdem::scale3(ra2, AB3C2)),
@@ -1221,7 +1244,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
   // direction wraps the position (passes y, +x, -x, +z, -z); the others delete
   // what left [min, max), in the delete passes (k_finish).
   if (d.per[0] || d.per[1] || d.per[2]) {
-    dbl4 Q = d.posr[p];
+    dbl4 Q = sdem::d4(x, Pp.w);
     if (d.per[1]) {
       if (fpi::ge(Q.y, d.dmax.y)) Q.y = Q.y - d.Lbox.y;
       else if (fpi::lt(Q.y, d.dmin.y)) Q.y = Q.y + d.Lbox.y;
@@ -1244,6 +1267,13 @@ __global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
     if (k2 < kOutCap) d.out_list[k2] = p;
     else raise(d, SDEM_E_CAPACITY, p);
   }
+}
+
+// The update in index order, one thread per particle (coalesced records).
+__global__ void __launch_bounds__(kThreads) k_integrate(Dev d) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *d.n) return;
+  integrate_body(d, p, [&](int f) { return int_src(d, f)[p]; });
 }
 
 // ---------------------------------------------------------------------------
@@ -2189,6 +2219,9 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   if (c.n_capacity < 1) return bad("n_capacity must be >= 1");
   if (c.max_gid < 1) return bad("max_gid must be >= 1");
   if (c.tsize < 1 || c.tsize > 3 || c.rsize < 1 || c.rsize > 3) return bad("tsize/rsize must be 1..3");
+  if (c.pi_method < SDEM_PIM_FE || c.pi_method > SDEM_PIM_AB3 || c.pri_method < SDEM_PIM_FE ||
+      c.pri_method > SDEM_PIM_AB3)
+    return bad("PI_Method and PRI_Method must be 1 (FE), 2 (AB2) or 3 (AB3)");
   if (c.tsize < c.pi_method || c.rsize < c.pri_method) return bad("tsize >= PI_Method and rsize >= PRI_Method required");
   if (c.cf_type != SDEM_CFT_LSD && c.cf_type != SDEM_CFT_NLIN) return bad("cf_type must be 1 (LSD) or 2 (Hertz)");
   if (c.ct_model != SDEM_CTM_CONSTANT && c.ct_model != SDEM_CTM_VARIABLE) return bad("ct_model must be 1 or 2");
