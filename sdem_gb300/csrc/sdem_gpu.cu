@@ -161,8 +161,10 @@ struct Dev {
   // with a periodic image; own_c lists this step's contacts of each owner id
   int Ko;
   int* c_row;   // row (target sort position) of each contact
-  int *own_cnt, *own_c;
-  const int *own_cnt_prev, *own_c_prev;
+  int* own_cnt;
+  int2* own_c;   // (contact index, partner id): the lookup reads the partner ids of one owner in one sector
+  const int* own_cnt_prev;
+  const int2* own_c_prev;
   int *wh_cnt, *wh_wall;
   dbl4* wh_hist;
   // wall contacts of this step: per particle up to kKw slots (decreasing wall
@@ -960,9 +962,10 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     dbl4 hist = make_dbl4(0.0, 0.0, 0.0, -2.0);
     {
       const int k = d.own_cnt_prev[owner];
+      const int2* oe = d.own_c_prev + (size_t)owner * d.Ko;
       for (int j = 0; j < k; j++) {
-        const int e = d.own_c_prev[(size_t)owner * d.Ko + j];
-        if (d.c_pgid_prev[e] == partner) { hist = d.c_hist_prev[e]; break; }
+        const int2 e = oe[j];
+        if (e.y == partner) { hist = d.c_hist_prev[e.x]; break; }
       }
     }
     const double* P = d.bpp + ((size_t)(tb - 1) * d.nT + (ta - 1)) * SDEM_BP_SIZE;
@@ -986,7 +989,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     d.c_Mj[c] = sdem::d4(sdem::scale3(M, Pj.w), 0.0);  // rj*Moment
     d.c_Mr[c] = sdem::d4(Mr, 0.0);
     const int os = atomicAdd(&d.own_cnt[owner], 1);
-    if (os < d.Ko) d.own_c[(size_t)owner * d.Ko + os] = c;
+    if (os < d.Ko) d.own_c[(size_t)owner * d.Ko + os] = make_int2(c, partner);
     else raise(d, SDEM_E_CL_FULL, owner);
     // one-sided pairs: with an image (AddContactPPG) or a fixed sphere (AddContactPPFix)
     if (kOneSided) {
@@ -1744,7 +1747,8 @@ struct sdem_h {
   int *row_cnt = nullptr, *row_partner = nullptr, *row_off = nullptr, *in_cnt = nullptr;
   unsigned* in_list = nullptr;
   int ccap = 0;
-  int *c_ogid = nullptr, *c_pgid[2] = {}, *own_cnt[2] = {}, *own_c[2] = {}, *c_row = nullptr;
+  int *c_ogid = nullptr, *c_pgid[2] = {}, *own_cnt[2] = {}, *c_row = nullptr;
+  int2* own_c[2] = {};
   int nall = 0, gcap = 0;
   int fcap = 0, nfix = 0;
   bool hier = false;
@@ -2691,18 +2695,19 @@ int sdem_upload_contacts(sdem_h* h, int nc, const int* owner_idx, const int* par
   }
   if ((long long)pp.size() > h->ccap) return set_err(h, SDEM_E_CL_FULL, "sdem_upload_contacts: more records than contact capacity");
   size_t G = (size_t)c.max_gid + 1;
-  std::vector<int> ocnt(G, 0), oc(G * h->K, 0), pg(pp.size());
+  std::vector<int> ocnt(G, 0), pg(pp.size());
+  std::vector<int2> oc(G * h->K, make_int2(0, 0));
   std::vector<dbl4> hs(pp.size());
   for (size_t i = 0; i < pp.size(); i++) {
     int g = pp[i].owner;
     if (ocnt[g] >= h->K)
       return set_err(h, SDEM_E_CL_FULL, "sdem_upload_contacts: more records on one particle than max_contacts_per_particle");
-    oc[(size_t)g * h->K + ocnt[g]++] = (int)i;
+    oc[(size_t)g * h->K + ocnt[g]++] = make_int2((int)i, pp[i].partner);
     pg[i] = pp[i].partner;
     hs[i] = pp[i].hist;
   }
   CK(cudaMemcpyAsync(h->own_cnt[pv], ocnt.data(), sizeof(int) * G, cudaMemcpyHostToDevice, h->stream));
-  CK(cudaMemcpyAsync(h->own_c[pv], oc.data(), sizeof(int) * G * h->K, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->own_c[pv], oc.data(), sizeof(int2) * G * h->K, cudaMemcpyHostToDevice, h->stream));
   if (!pp.empty()) {
     CK(cudaMemcpyAsync(h->c_pgid[pv], pg.data(), sizeof(int) * pp.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->c_hist[pv], hs.data(), sizeof(dbl4) * pp.size(), cudaMemcpyHostToDevice, h->stream));
