@@ -41,7 +41,7 @@ WORKLOAD = "hertz_poly_1m"
 MEASURED_FP64_TFLOPS = 1.198   # DFMA-chain probe on GB300 (2 flops per DFMA)
 # From the ncu captures in profiles/k_force_search_gather_hertz_poly_500k.txt:
 FORCE_DRAM_BYTES_PER_CONTACT = 422.0     # dram__bytes_read.sum + dram__bytes_write.sum per contact
-FORCE_FP64_INST_PER_CONTACT = 126.6      # DADD + DMUL + DFMA thread instructions per contact
+FORCE_FP64_INST_PER_CONTACT = 120.6      # DADD + DMUL + DFMA thread instructions per contact
 FP64_INST_PER_SM_CLK = 2.0               # sm__sass_thread_inst_executed_op_dfma_pred_on peak per SM
 NUM_SMS = 152
 
@@ -276,9 +276,10 @@ def our_arm(args):
     # on the 500k-sphere bed (profiles/k_force_search_gather_hertz_poly_500k.txt),
     # scaled to this launch by its contacts
     traffic = FORCE_DRAM_BYTES_PER_CONTACT * C
-    # algorithmic FP64 operations of one Hertz contact (force law + normal vector):
-    # 127 add/sub/mul, 8 sqrt, 7 divisions, each sqrt/div counted as one operation
-    fp64_per_contact = 142
+    # algorithmic FP64 operations of k_force per Hertz contact (force law + normal
+    # vector; the two r*Moment scalings are the gather's): 121 add/sub/mul,
+    # 8 sqrt, 7 divisions, each sqrt/div counted as one operation
+    fp64_per_contact = 136
     t_step = ms / K * 1e-3
     step_bytes = n * 352.0 + C * 80.0 + 4.0 * 0   # per-step algorithmic bytes of the whole path
 

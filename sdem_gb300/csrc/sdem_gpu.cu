@@ -155,7 +155,7 @@ struct Dev {
   const int* c_pgid_prev;
   dbl4* c_hist;
   const dbl4* c_hist_prev;
-  dbl4 *c_S, *c_M, *c_Mj, *c_Mr;
+  dbl4 *c_S, *c_M, *c_Mr;   // Fnij+Ftij (.w: target is particle i), Moment = n x Ftij, Mrij
   // contact history by the reference's bucket owner (Find_insert's bkt_id):
   // the lower id for particle-particle pairs, the local particle for a pair
   // with a periodic image; own_c lists this step's contacts of each owner id
@@ -900,7 +900,7 @@ __global__ void __launch_bounds__(kThreads) k_wall_force(Dev d) {
     sdem::force_law(d.law, P, sdem::xyz(d.vel0[p]), W.vel, sdem::xyz(d.rv0[p]), sdem::mk3(0.0, 0.0, 0.0), ri,
                     1.00E20 * ri, Norm_v, geo.w, hist, S, M, Mr);
     d.w_S[at] = sdem::d4(S, 0.0);
-    d.w_M[at] = sdem::d4(sdem::scale3(M, ri), 0.0);   // ri*Moment
+    d.w_M[at] = sdem::d4(M, 0.0);   // Moment (the gather scales it by ri)
     d.w_Mr[at] = sdem::d4(Mr, 0.0);
     d.wh_wall[(size_t)g * kKw + j] = wi;
     d.wh_hist[(size_t)g * kKw + j] = hist;
@@ -985,8 +985,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     d.c_pgid[c] = partner;
     d.c_hist[c] = hist;
     d.c_S[c] = sdem::d4(S, m_lo ? 1.0 : 0.0);  // .w: is the row's target particle i
-    d.c_M[c] = sdem::d4(sdem::scale3(M, Pi.w), 0.0);   // ri*Moment
-    d.c_Mj[c] = sdem::d4(sdem::scale3(M, Pj.w), 0.0);  // rj*Moment
+    d.c_M[c] = sdem::d4(M, 0.0);   // Moment: each side's gather scales it by its own radius
     d.c_Mr[c] = sdem::d4(Mr, 0.0);
     const int os = atomicAdd(&d.own_cnt[owner], 1);
     if (os < d.Ko) d.own_c[(size_t)owner * d.Ko + os] = make_int2(c, partner);
@@ -1043,6 +1042,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   const int p = kByDegree ? d.gorder[tid] : tid;
   const int ncap = d.ncap;
   const int s = d.sortpos[p];
+  const double rp = d.posr[p].w;
   r3 F = sdem::mk3(0.0, 0.0, 0.0), T = sdem::mk3(0.0, 0.0, 0.0);
 
   // The contact records of p in the reference's scatter order: in-list
@@ -1111,7 +1111,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
     dbl4 S, Ms, Mr;
     if (c >= 0) {
       S = d.c_S[c];
-      Ms = p_lo ? d.c_M[c] : d.c_Mj[c];   // ri*Moment or rj*Moment
+      Ms = d.c_M[c];
       Mr = d.c_Mr[c];
     } else {
       const size_t at = (size_t)(-c - 1) * ncap + p;
@@ -1126,7 +1126,8 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
     const uint64_t sg = p_lo ? 0ull : fpi::kSign;
     auto flip = [sg](double v) { return fpi::from_bits(fpi::bits(v) ^ sg); };
     F = sdem::add3(F, sdem::mk3(flip(S.x), flip(S.y), flip(S.z)));
-    T = sdem::add3(sdem::add3(T, sdem::xyz(Ms)), sdem::mk3(flip(Mr.x), flip(Mr.y), flip(Mr.z)));
+    // r*Moment with p's own radius (ri*Moment or rj*Moment of the reference)
+    T = sdem::add3(sdem::add3(T, sdem::scale3(sdem::xyz(Ms), rp)), sdem::mk3(flip(Mr.x), flip(Mr.y), flip(Mr.z)));
   }
   d.F[p] = sdem::d4(F, 0.0);
   d.T[p] = sdem::d4(T, 0.0);
@@ -1762,7 +1763,7 @@ struct sdem_h {
   // owner id, partner id, listed under the partner too
   struct UpRec { int owner, partner; bool both; dbl4 hist; };
   std::vector<UpRec> h_up;
-  dbl4 *c_hist[2] = {}, *c_S = nullptr, *c_M = nullptr, *c_Mj = nullptr, *c_Mr = nullptr;
+  dbl4 *c_hist[2] = {}, *c_S = nullptr, *c_M = nullptr, *c_Mr = nullptr;
   int *wh_cnt[2] = {}, *wh_wall[2] = {};
   dbl4* wh_hist[2] = {};
   int *w_cnt = nullptr, *w_wall = nullptr, *wl = nullptr;
@@ -1995,7 +1996,6 @@ Dev make_dev(sdem_h* h) {
   d.c_hist_prev = h->c_hist[pv];
   d.c_S = h->c_S;
   d.c_M = h->c_M;
-  d.c_Mj = h->c_Mj;
   d.c_Mr = h->c_Mr;
   d.Ko = h->K;
   d.c_row = h->c_row;
@@ -2326,7 +2326,6 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->c_row, h->ccap);
   rc |= dalloc(h, &h->c_S, h->ccap);
   rc |= dalloc(h, &h->c_M, h->ccap);
-  rc |= dalloc(h, &h->c_Mj, h->ccap);
   rc |= dalloc(h, &h->c_Mr, h->ccap);
   size_t G = (size_t)c.max_gid + 1;
   for (int b = 0; b < 2; b++) {
