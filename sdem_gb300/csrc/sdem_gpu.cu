@@ -155,7 +155,7 @@ struct Dev {
   const int* c_pgid_prev;
   dbl4* c_hist;
   const dbl4* c_hist_prev;
-  dbl4 *c_S, *c_M, *c_Mr;   // Fnij+Ftij (.w: target is particle i), Moment = n x Ftij, Mrij
+  dbl4 *c_S, *c_M, *c_Mr;   // Fnij+Ftij and Mrij signed for the row's target; Moment = n x Ftij
   // contact history by the reference's bucket owner (Find_insert's bkt_id):
   // the lower id for particle-particle pairs, the local particle for a pair
   // with a periodic image; own_c lists this step's contacts of each owner id
@@ -984,9 +984,14 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     d.c_ogid[c] = owner | (img ? kImgFlag : 0);
     d.c_pgid[c] = partner;
     d.c_hist[c] = hist;
-    d.c_S[c] = sdem::d4(S, m_lo ? 1.0 : 0.0);  // .w: is the row's target particle i
+    // signed for the row's target: it adds S and Mr when it is particle i and
+    // subtracts them when it is j (x - y == x + (-y): the sign goes on the
+    // bits); the partner adds their negations
+    const uint64_t sg = m_lo ? 0ull : fpi::kSign;
+    auto flip = [sg](double v) { return fpi::from_bits(fpi::bits(v) ^ sg); };
+    d.c_S[c] = make_dbl4(flip(S.x), flip(S.y), flip(S.z), 0.0);
     d.c_M[c] = sdem::d4(M, 0.0);   // Moment: each side's gather scales it by its own radius
-    d.c_Mr[c] = sdem::d4(Mr, 0.0);
+    d.c_Mr[c] = make_dbl4(flip(Mr.x), flip(Mr.y), flip(Mr.z), 0.0);
     const int os = atomicAdd(&d.own_cnt[owner], 1);
     if (os < d.Ko) d.own_c[(size_t)owner * d.Ko + os] = make_int2(c, partner);
     else raise(d, SDEM_E_CL_FULL, owner);
@@ -1054,16 +1059,12 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   if (nin > d.Kin) nin = d.Kin;
   const int own_a = d.row_off[s], own_n = d.row_cnt[s];
   const int nwc = d.w_cnt[p];
-  // entry: (contact index << 1) | (p is particle i), or -(wall slot + 1)
+  // entry: (contact index << 1) | (p is the row's target), or -(wall slot + 1)
   int list[2 * kMaxK + kKw];
   int nl = 0;
-  auto push = [&](int c, bool p_lo) { list[nl++] = (c << 1) | (p_lo ? 1 : 0); };
-  auto push_in = [&](unsigned key) {
-    const int c = d.row_off[key >> 6] + (int)(key & 63u);
-    push(c, (__double_as_longlong(d.c_S[c].w) << 1) == 0);   // p is the row's partner: particle i iff the target is not
-  };
+  auto push_in = [&](unsigned key) { list[nl++] = (d.row_off[key >> 6] + (int)(key & 63u)) << 1; };
   auto push_own = [&]() {
-    for (int j = 0; j < own_n; j++) push(own_a + j, (__double_as_longlong(d.c_S[own_a + j].w) << 1) != 0);
+    for (int j = 0; j < own_n; j++) list[nl++] = ((own_a + j) << 1) | 1;
   };
   if (nin <= 8) {
     unsigned u[8];
@@ -1107,7 +1108,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   for (int k = 0; k < nl; k++) {
     const int e = list[k];
     const int c = e >= 0 ? (e >> 1) : e;
-    const bool p_lo = e < 0 || (e & 1);
+    const bool tgt = e < 0 || (e & 1);   // a wall record or p's own row: as stored
     dbl4 S, Ms, Mr;
     if (c >= 0) {
       S = d.c_S[c];
@@ -1121,9 +1122,10 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
     }
     // F(pid) + (Fnij+Ftij) / F(pjd) - (Fnij+Ftij);
     // T + r*Moment + Mrij / T + r*Moment - Mrij  (Prtcl_ContactForce_inc.f90:69-86).
-    // x - y is x + (-y) in IEEE arithmetic: the side's sign goes onto the
-    // record's sign bits, so that every lane runs the same FP64 additions.
-    const uint64_t sg = p_lo ? 0ull : fpi::kSign;
+    // The records are signed for the row's target; the partner adds their
+    // negations (x - y is x + (-y) in IEEE arithmetic), so that every lane
+    // runs the same FP64 additions.
+    const uint64_t sg = tgt ? 0ull : fpi::kSign;
     auto flip = [sg](double v) { return fpi::from_bits(fpi::bits(v) ^ sg); };
     F = sdem::add3(F, sdem::mk3(flip(S.x), flip(S.y), flip(S.z)));
     // r*Moment with p's own radius (ri*Moment or rj*Moment of the reference)
