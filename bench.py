@@ -40,8 +40,8 @@ UNIT = "particle-steps/s"
 WORKLOAD = "hertz_poly_1m"
 MEASURED_FP64_TFLOPS = 1.198   # DFMA-chain probe on GB300 (2 flops per DFMA)
 # From the ncu captures in profiles/k_force_search_gather_hertz_poly_500k.txt:
-FORCE_DRAM_BYTES_PER_CONTACT = 422.0     # dram__bytes_read.sum + dram__bytes_write.sum per contact
-FORCE_FP64_INST_PER_CONTACT = 120.6      # DADD + DMUL + DFMA thread instructions per contact
+FORCE_DRAM_BYTES_PER_CONTACT = 394.0     # dram__bytes_read.sum + dram__bytes_write.sum per contact
+FORCE_FP64_INST_PER_CONTACT = 133.8      # DADD + DMUL + DFMA thread instructions per contact
 FP64_INST_PER_SM_CLK = 2.0               # sm__sass_thread_inst_executed_op_dfma_pred_on peak per SM
 NUM_SMS = 152
 
