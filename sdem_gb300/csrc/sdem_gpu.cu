@@ -2619,10 +2619,13 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   CK(cudaMemsetAsync(h->ull, 0, sizeof(unsigned long long) * 10, st));
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
+  // the captured step graphs bake in launch sizes from the particle count
+  // (and nothing else that an upload changes): they stay valid for a new
+  // particle set of the same size
+  if (n != h->n_host) drop_graph(h);
   h->n_host = n;
   h->cur = 0;
   h->stepped = false;
-  drop_graph(h);
   std::memset(h->h_counters, 0, sizeof(int) * SDEM_CNT_SIZE);
   h->h_counters[SDEM_CNT_NLOCAL] = n;
   return 0;
