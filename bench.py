@@ -295,9 +295,13 @@ def our_arm(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sys2.upload(st)
-        for _ in range(Ke):
-            sys2.step_async(1)      # the counters read below waits for the step
-            sys2.counters()
+        sys2.step_async(1)
+        for k in range(1, Ke + 1):
+            if k < Ke:
+                sys2.step_async(1)          # step k+1 is queued ...
+                sys2.counters_lagged()      # ... while step k's counters are read
+            else:
+                sys2.counters()
         out = sys2.state(out=out_buf)
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
@@ -308,8 +312,9 @@ def our_arm(args):
                                                    "rotVel", "rotAcc")) + Ke * 32
         e2e = {"value": n_all * Ke / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / Ke),
                "d2h_bytes_per_step": int(d2h / Ke), "steps": Ke,
-               "note": "upload of the state from pinned host memory, K x (sdem_step_async(h,1) + sdem_counters), "
-                       "download of the state into pinned host memory"}
+               "note": "upload of the state from pinned host memory, K x (sdem_step_async(h,1) + the counters of "
+                       "each step read back: sdem_counters_lagged while the next step runs, sdem_counters after "
+                       "the last), download of the state into pinned host memory"}
         sys2.close()
 
     cpu = None

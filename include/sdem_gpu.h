@@ -219,6 +219,14 @@ int sdem_set_fixed(sdem_h* h, int nfix, const int* id, const int* ptype, const d
 /* Counters of the last step, SDEM_CNT_SIZE ints (see SDEM_CNT_*). */
 int sdem_counters(sdem_h* h, int* out);
 
+/* Counters of the step before the last one enqueued, waiting for that step
+ * only: a driver that enqueues step k+1 (sdem_step_async(h, 1)) and then reads
+ * the counters of step k keeps the device busy while it reads them.  Device
+ * errors raised up to that step are reported here.  When that step's copy is
+ * not at hand (fewer than two steps since the upload, a multi-step call, a
+ * call that rewrote the device scalars) this is sdem_counters. */
+int sdem_counters_lagged(sdem_h* h, int* out);
+
 /* ---- asynchronous output for the dump / restart steps ---------------------
  * Replaces the synchronous downloads before dump_visu and Write_Restart
  * (Prtcl_DEMSystem.f90:254,261; formats of Prtcl_IOAndVisu.f90:849-1031,

@@ -26,8 +26,9 @@ CNT_NAMES = ("pp", "ppg", "ppfix", "pw", "cnsv", "nlocal", "iter", "next_wall_up
 EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls", "sdem_upload_particles",
             "sdem_upload_contacts", "sdem_step", "sdem_step_async", "sdem_get_stream",
             "sdem_download_particles", "sdem_download_contacts", "sdem_check_restart_limit",
-            "sdem_download_forces", "sdem_counters", "sdem_counter_sums", "sdem_launch_count", "sdem_profile_begin",
-            "sdem_profile_end", "sdem_profile_phase_name", "sdem_count_contacts_noalloc", "sdem_selftest_fp64",
+            "sdem_download_forces", "sdem_counters", "sdem_counters_lagged", "sdem_counter_sums",
+            "sdem_launch_count", "sdem_profile_begin", "sdem_profile_end", "sdem_profile_phase_name",
+            "sdem_count_contacts_noalloc", "sdem_selftest_fp64",
             "sdem_snapshot_begin", "sdem_snapshot_end", "sdem_snapshot_contacts", "sdem_set_fixed", "sdem_last_error",
             "sdem_destroy")
 
@@ -120,6 +121,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_check_restart_limit.argtypes = [P]
     lib.sdem_download_forces.argtypes = [P, dp, dp]
     lib.sdem_counters.argtypes = [P, ip]
+    lib.sdem_counters_lagged.argtypes = [P, ip]
     lib.sdem_launch_count.argtypes = [P, C.POINTER(C.c_longlong)]
     lib.sdem_counter_sums.argtypes = [P, C.POINTER(C.c_longlong)]
     lib.sdem_profile_begin.argtypes = [P, C.c_int]
@@ -349,6 +351,12 @@ class DEMSystem:
     def counters(self) -> dict:
         out = np.zeros(9, np.int32)
         self._check(self.lib.sdem_counters(self.h, iptr(out)))
+        return dict(zip(CNT_NAMES, (int(x) for x in out)))
+
+    def counters_lagged(self) -> dict:
+        """Counters of the step before the last one enqueued (sdem_counters_lagged)."""
+        out = np.zeros(9, np.int32)
+        self._check(self.lib.sdem_counters_lagged(self.h, iptr(out)))
         return dict(zip(CNT_NAMES, (int(x) for x in out)))
 
     def close(self) -> None:

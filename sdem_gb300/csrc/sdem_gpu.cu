@@ -1556,7 +1556,9 @@ __global__ void k_pack3(double* __restrict__ dst, const dbl4* __restrict__ src, 
 // Ends a step: the counters of the step (CL and search logs), running sums,
 // per-step resets, and a copy of the device scalars (status, particle count,
 // counters) into mapped host memory, so that the host reads them after a
-// stream synchronisation without another copy.
+// stream synchronisation without another copy.  Two mirror slots, by the
+// parity of the new iteration number: a step's copy survives while the next
+// step runs.
 __device__ void step_end_serial(const Dev& d, int* counters_out, const int* scal, int* mirror, int nscal) {
   const int C = d.row_off[d.nall_launch];
   counters_out[SDEM_CNT_PP] = C - (int)d.counters[5] - (int)d.counters[8];
@@ -1579,8 +1581,10 @@ __device__ void step_end_serial(const Dev& d, int* counters_out, const int* scal
   d.counters[9] = 0;
   *d.out_cnt = 0;
   *d.wl_cnt = 0;
-  if (mirror)
-    for (int k = 0; k < nscal; k++) mirror[k] = scal[k];
+  if (mirror) {
+    int* slot = mirror + (*d.iter & 1) * nscal;
+    for (int k = 0; k < nscal; k++) slot[k] = scal[k];
+  }
 }
 
 // The end of a step in one block: the serial delete passes (thread 0), the
@@ -1789,9 +1793,12 @@ struct sdem_h {
   int* h_counters = nullptr;  // pinned
   // mapped host copy of the device scalars, written by every step's last
   // kernel; valid while no host write to the scalars came after the last step
-  int* h_mirror = nullptr;
+  int* h_mirror = nullptr;   // 2 slots of S_SIZE ints, by iteration parity
   int* d_mirror = nullptr;
   bool mirror_ok = false;
+  long long iter_host = 0;   // device iteration number after the last enqueued step
+  cudaEvent_t ev_step[2] = {};   // completion of the step that ends on an iteration of this parity
+  long long ev_iter[2] = {-1, -1};   // the iteration each event marks
   double* stage = nullptr;    // device staging of host-layout 3-vectors (upload, download)
   size_t stage_n = 0;
   // asynchronous output: a frozen copy of the state and contacts on the device,
@@ -2152,11 +2159,27 @@ void drop_graph(sdem_h* h) {
   }
 }
 
+// Reads the device scalars as of iteration `it` from its mirror slot (after
+// that step completed), or the device copy when the mirror does not hold it.
+int read_scalars(sdem_h* h, long long it, int* s) {
+  const int* m = h->h_mirror + (it & 1) * S_SIZE;
+  if (h->mirror_ok && m[S_ITER] == (int)it) std::memcpy(s, m, sizeof(int) * S_SIZE);
+  else CK(cudaMemcpy(s, h->scal, sizeof(int) * S_SIZE, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int check_scalars(sdem_h* h, const int* s);
+
 int sync_and_check(sdem_h* h) {
   CK(cudaStreamSynchronize(h->stream));
   int s[S_SIZE];
-  if (h->mirror_ok) std::memcpy(s, h->h_mirror, sizeof s);
-  else CK(cudaMemcpy(s, h->scal, sizeof s, cudaMemcpyDeviceToHost));
+  int rc = read_scalars(h, h->iter_host, s);
+  if (rc) return rc;
+  return check_scalars(h, s);
+}
+
+// Takes the counters and the error status of a scalar snapshot.
+int check_scalars(sdem_h* h, const int* s) {
   std::memcpy(h->h_counters, s + S_COUNTERS, sizeof(int) * SDEM_CNT_SIZE);
   if (s[S_STATUS] != 0) {
     int code = s[S_STATUS], detail = s[S_STATUS + 1];
@@ -2170,6 +2193,7 @@ int sync_and_check(sdem_h* h) {
     }
     // clear so the handle stays usable for downloads
     int z[2] = {0, 0};
+    cudaStreamSynchronize(h->stream);
     cudaMemcpyAsync(h->scal + S_STATUS, z, sizeof z, cudaMemcpyHostToDevice, h->stream);
     cudaStreamSynchronize(h->stream);
     h->mirror_ok = false;
@@ -2349,7 +2373,9 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->scan_tmp, 65536);
   if (rc) return SDEM_E_NOMEM;
   CK(cudaMallocHost(&h->h_counters, sizeof(int) * SDEM_CNT_SIZE));
-  CK(cudaHostAlloc((void**)&h->h_mirror, sizeof(int) * S_SIZE, cudaHostAllocMapped));
+  CK(cudaHostAlloc((void**)&h->h_mirror, sizeof(int) * 2 * S_SIZE, cudaHostAllocMapped));
+  std::memset(h->h_mirror, 0, sizeof(int) * 2 * S_SIZE);
+  for (int b = 0; b < 2; b++) CK(cudaEventCreateWithFlags(&h->ev_step[b], cudaEventDisableTiming));
   CK(cudaHostGetDevicePointer((void**)&h->d_mirror, h->h_mirror, 0));
   std::memset(h->h_counters, 0, sizeof(int) * SDEM_CNT_SIZE);
   CK(cudaStreamSynchronize(h->stream));
@@ -2626,6 +2652,11 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   h->n_host = n;
   h->cur = 0;
   h->stepped = false;
+  // the iteration count restarts at 0: no mirror slot or step event may
+  // stand for an iteration of the new run
+  std::memset(h->h_mirror, 0, sizeof(int) * 2 * S_SIZE);
+  h->iter_host = 0;
+  h->ev_iter[0] = h->ev_iter[1] = -1;
   std::memset(h->h_counters, 0, sizeof(int) * SDEM_CNT_SIZE);
   h->h_counters[SDEM_CNT_NLOCAL] = n;
   return 0;
@@ -2793,6 +2824,15 @@ int build_graph1(sdem_h* h) {
 }
 }  // namespace
 
+// Records the completion event of the step just enqueued (the one ending on
+// iteration iter_host).
+void mark_step(sdem_h* h) {
+  h->mirror_ok = true;   // every step ends by copying the scalars to its mirror slot
+  const int b = (int)(h->iter_host & 1);
+  if (cudaEventRecord(h->ev_step[b], h->stream) == cudaSuccess) h->ev_iter[b] = h->iter_host;
+  else h->ev_iter[b] = -1;
+}
+
 int sdem_step_async(sdem_h* h, int nsteps) {
   if (!h) return SDEM_E_ARG;
   if (!h->have_types) return set_err(h, SDEM_E_ARG, "sdem_step: call sdem_set_types first");
@@ -2807,6 +2847,8 @@ int sdem_step_async(sdem_h* h, int nsteps) {
         int rc = enqueue_step(h);  // realign the parity instead of capturing twice
         if (rc) return rc;
         left--;
+        h->iter_host += 1;
+        mark_step(h);
       }
       if (h->graph2 == nullptr) {
         int rc = build_graph(h);
@@ -2817,6 +2859,8 @@ int sdem_step_async(sdem_h* h, int nsteps) {
       CK(cudaGraphLaunch(h->graph2, h->stream));
       h->launches += h->graph_launches;
       left -= 2;
+      h->iter_host += 2;
+      mark_step(h);
     }
   }
   for (int i = 0; i < left; i++) {
@@ -2833,6 +2877,8 @@ int sdem_step_async(sdem_h* h, int nsteps) {
       int rc = enqueue_step(h);
       if (rc) return rc;
     }
+    h->iter_host += 1;
+    mark_step(h);
   }
   h->stepped = h->stepped || nsteps > 0;
   return 0;
@@ -3186,6 +3232,22 @@ int sdem_counters(sdem_h* h, int* out) {
   return 0;
 }
 
+int sdem_counters_lagged(sdem_h* h, int* out) {
+  if (!h || !out) return SDEM_E_ARG;
+  const long long it = h->iter_host - 1;   // the step before the last one enqueued
+  const int b = (int)(it & 1);
+  if (it < 1 || !h->mirror_ok || h->ev_iter[b] != it) return sdem_counters(h, out);
+  CK(cudaEventSynchronize(h->ev_step[b]));
+  int s[S_SIZE];
+  const int* m = h->h_mirror + b * S_SIZE;
+  if (m[S_ITER] != (int)it) return sdem_counters(h, out);
+  std::memcpy(s, m, sizeof s);
+  int rc = check_scalars(h, s);
+  if (rc) return rc;
+  std::memcpy(out, h->h_counters, sizeof(int) * SDEM_CNT_SIZE);
+  return 0;
+}
+
 int sdem_counter_sums(sdem_h* h, long long* out) {
   if (!h || !out) return SDEM_E_ARG;
   int rc = sync_and_check(h);
@@ -3383,6 +3445,8 @@ void sdem_destroy(sdem_h* h) {
   if (h->stream_io) cudaStreamDestroy(h->stream_io);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  for (int b = 0; b < 2; b++)
+    if (h->ev_step[b]) cudaEventDestroy(h->ev_step[b]);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   for (int k = 0; k < kChunks; k++)
     if (h->ev_chunk[k]) cudaEventDestroy(h->ev_chunk[k]);
