@@ -1,6 +1,7 @@
 """The benchmark beds at their full sizes.
 
-- the 1M-sphere polydisperse Hertz bed (41 types, five walls) and the 20k
+- the 1M-sphere polydisperse Hertz bed (41 types, five walls), the 4M-sphere
+  bidisperse hopper (one-level and hierarchical search) and the 20k
   monodisperse LSD bed (after 5000 steps of settling, restarted from the
   GPU's state and contact list): one step from identical inputs against the oracle
   (contact sets equal; history, forces, torques within 1e-12 relative;
@@ -77,6 +78,17 @@ def test_lsd_mono_20k_one_step_matches_oracle(gpu_lib):
     run.step(5000)
     case = beds.Case(case0.name, case0.opts, case0.tables, case0.walls, run.state(), contacts=run.contacts())
     run.close()
+    compare_one_step(case)
+
+
+@pytest.mark.parametrize("cs_method", [1, 2])
+def test_hopper_4m_one_step_matches_oracle(gpu_lib, cs_method):
+    # 4M bidisperse (1:3) Hertz spheres in a hopper of four inclined finite
+    # quads over a 10 mm outlet, plus a vertical column; one-level search and
+    # the hierarchical search (CS_Method 2)
+    case = beds.hopper_case(4_000_000, 3, width=0.26, outlet=10.0e-3)
+    if cs_method == 2:
+        case = beds.scaled(case, cs_method=2)
     compare_one_step(case)
 
 
