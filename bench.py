@@ -285,6 +285,8 @@ def our_arm(args):
 
     # e2e: through the C ABI with host buffers
     e2e = None
+    if args.e2e_steps < 0:
+        args.e2e_steps = K      # the same number of steps as the device-timed run
     if args.e2e_steps > 0:
         sys2 = DEMSystem(case)
         sys2.step(1)
@@ -375,7 +377,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
-    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=-1,
+                    help="steps of the end-to-end run (default: --steps; 0 skips it)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
