@@ -177,7 +177,9 @@ struct Dev {
   int* wl_cnt;
   // gather order: particles bucketed by their number of contact records, so a
   // warp's summation loops run the same trip count
-  int *deg_cnt, *deg_of, *deg_rank, *gorder;
+  int *deg_cnt, *deg_of, *deg_rank;
+  int4* gorder;   // per gather position: sphere, its sort position, its row start,
+                  // row length << 16 | in-list length << 8 | wall contacts
   const int *wh_cnt_prev, *wh_wall_prev;
   const dbl4* wh_hist_prev;
   // status and scalars
@@ -873,7 +875,12 @@ __global__ void k_degree_scatter(Dev d) {
   __syncthreads();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= *d.n) return;
-  d.gorder[start[d.deg_of[p]] + d.deg_rank[p]] = p;
+  // what the gather needs first, read here in index order (coalesced, apart
+  // from the row of p) and stored at the gather position in one record
+  const int s = d.sortpos[p];
+  const int nin = min(d.in_cnt[p], d.Kin);
+  d.gorder[start[d.deg_of[p]] + d.deg_rank[p]] =
+      make_int4(p, s, d.row_off[s], (d.row_cnt[s] << 16) | (nin << 8) | d.w_cnt[p]);
 }
 
 // One thread per wall contact: Find_insert on the particle's bucket (key = wall)
@@ -1040,13 +1047,12 @@ __device__ __forceinline__ void sort_net(unsigned (&v)[N]) {
       }
 }
 
-template <bool kByDegree>
 __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= *d.n) return;
-  const int p = kByDegree ? d.gorder[tid] : tid;
+  const int4 gr = d.gorder[tid];
+  const int p = gr.x, s = gr.y;
   const int ncap = d.ncap;
-  const int s = d.sortpos[p];
   const double rp = d.posr[p].w;
   r3 F = sdem::mk3(0.0, 0.0, 0.0), T = sdem::mk3(0.0, 0.0, 0.0);
 
@@ -1055,10 +1061,9 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   // targets, then wall contacts.  Their indices go to a small per-thread list
   // first (integer work), so the FP64 additions run in one loop whose trip
   // count is the warp's maximum, not once per branch.
-  int nin = d.in_cnt[p];
-  if (nin > d.Kin) nin = d.Kin;
-  const int own_a = d.row_off[s], own_n = d.row_cnt[s];
-  const int nwc = d.w_cnt[p];
+  const int own_a = gr.z, own_n = gr.w >> 16;
+  const int nin = (gr.w >> 8) & 0xFF;
+  const int nwc = gr.w & 0xFF;
   // entry: (contact index << 1) | (p is the row's target), or -(wall slot + 1)
   int list[2 * kMaxK + kKw];
   int nl = 0;
@@ -1777,7 +1782,8 @@ struct sdem_h {
   float4* spos = nullptr;
   float4* pf = nullptr;
   float pf_margin = 0.f;
-  int *deg_cnt = nullptr, *deg_of = nullptr, *deg_rank = nullptr, *gorder = nullptr;
+  int *deg_cnt = nullptr, *deg_of = nullptr, *deg_rank = nullptr;
+  int4* gorder = nullptr;
   // second stream and events of the chunked search/force pipeline
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chunk[kChunks] = {};
@@ -2131,7 +2137,7 @@ int enqueue_step(sdem_h* h) {
   }
   mark(PH_GATHER);
   k_degree_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
-  k_gather<true><<<grid_for(n), kThreads, 0, st>>>(d);
+  k_gather<<<grid_for(n), kThreads, 0, st>>>(d);
   k_integrate<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_DELETE);
   k_finish<<<1, kThreads, 0, st>>>(d, h->scal + S_COUNTERS, h->scal, h->d_mirror, S_SIZE);
