@@ -304,6 +304,26 @@ const char* sdem_last_error(sdem_h* h);
 
 void sdem_destroy(sdem_h* h);
 
+/* ---- batched form: one handle holds many independent beds ------------------
+ * A batch groups handles created, configured and uploaded as usual (each with
+ * its own particle count, materials, walls and domain) and advances all of
+ * them together: a batch step is one CUDA graph that runs every member's step
+ * on the member's own streams, so that beds too small to fill the GPU run side
+ * by side.  Results equal stepping each member alone, bit for bit.  The
+ * members stay usable: their downloads, counters and single steps are ordered
+ * after the batch's steps.  A handle belongs to at most one batch and must
+ * outlive it; sdem_batch_destroy does not destroy the members. */
+typedef struct sdem_batch sdem_batch;
+int sdem_batch_create(int n, sdem_h* const* members, sdem_batch** out);
+/* nsteps steps of every member, without a final synchronisation */
+int sdem_batch_step_async(sdem_batch* b, int nsteps);
+/* waits for the batch and reports the first member error (SDEM_E_*) */
+int sdem_batch_sync(sdem_batch* b);
+/* sdem_batch_step_async + sdem_batch_sync */
+int sdem_batch_step(sdem_batch* b, int nsteps);
+const char* sdem_batch_last_error(sdem_batch* b);
+void sdem_batch_destroy(sdem_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

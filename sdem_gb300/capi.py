@@ -30,7 +30,8 @@ EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls
             "sdem_launch_count", "sdem_profile_begin", "sdem_profile_end", "sdem_profile_phase_name",
             "sdem_count_contacts_noalloc", "sdem_selftest_fp64",
             "sdem_snapshot_begin", "sdem_snapshot_end", "sdem_snapshot_contacts", "sdem_set_fixed", "sdem_last_error",
-            "sdem_destroy")
+            "sdem_destroy", "sdem_batch_create", "sdem_batch_step_async", "sdem_batch_sync", "sdem_batch_step",
+            "sdem_batch_last_error", "sdem_batch_destroy")
 
 
 def selftest_fp64(n: int, seed: int = 1) -> int:
@@ -137,8 +138,17 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_last_error.restype = C.c_char_p
     lib.sdem_destroy.argtypes = [P]
     lib.sdem_destroy.restype = None
+    lib.sdem_batch_create.argtypes = [C.c_int, C.POINTER(P), C.POINTER(P)]
+    lib.sdem_batch_step_async.argtypes = [P, C.c_int]
+    lib.sdem_batch_sync.argtypes = [P]
+    lib.sdem_batch_step.argtypes = [P, C.c_int]
+    lib.sdem_batch_last_error.argtypes = [P]
+    lib.sdem_batch_last_error.restype = C.c_char_p
+    lib.sdem_batch_destroy.argtypes = [P]
+    lib.sdem_batch_destroy.restype = None
     for name in EXPORTED:
-        if name not in ("sdem_default_cfg", "sdem_last_error", "sdem_destroy", "sdem_profile_phase_name"):
+        if name not in ("sdem_default_cfg", "sdem_last_error", "sdem_destroy", "sdem_profile_phase_name",
+                        "sdem_batch_last_error", "sdem_batch_destroy"):
             getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -369,6 +379,48 @@ class DEMSystem:
 
     def __exit__(self, *a):
         self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DEMBatch:
+    """Many DEMSystem beds advanced together (sdem_batch_*): one CUDA graph
+    per batch step holds every member's step.  The members stay usable for
+    downloads and single steps; they must outlive the batch."""
+
+    def __init__(self, members):
+        self.lib = load()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        self.b = C.c_void_p()
+        rc = self.lib.sdem_batch_create(len(self.members), arr, C.byref(self.b))
+        if rc:
+            msg = self.lib.sdem_batch_last_error(self.b).decode() if self.b else ""
+            self.lib.sdem_batch_destroy(self.b)
+            self.b = None
+            raise SdemError(rc, msg)
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise SdemError(rc, self.lib.sdem_batch_last_error(self.b).decode())
+
+    def step(self, n: int = 1) -> None:
+        self._check(self.lib.sdem_batch_step(self.b, int(n)))
+
+    def step_async(self, n: int = 1) -> None:
+        self._check(self.lib.sdem_batch_step_async(self.b, int(n)))
+
+    def sync(self) -> None:
+        self._check(self.lib.sdem_batch_sync(self.b))
+
+    def close(self) -> None:
+        if self.b:
+            self.lib.sdem_batch_destroy(self.b)
+            self.b = None
 
     def __del__(self):
         try:

@@ -1827,6 +1827,7 @@ struct sdem_h {
   long long graph1_launches = 0;
   int graph_cur = -1;       // buffer parity the graph starts from
   long long graph_launches = 0;
+  long long graph_gen = 0;   // bumped whenever captured step graphs become invalid
   bool use_graphs = true;
   // diagnostics: kernel launches issued, optional per-phase CUDA events
   long long launches = 0;
@@ -2156,6 +2157,7 @@ int enqueue_step(sdem_h* h) {
 }
 
 void drop_graph(sdem_h* h) {
+  h->graph_gen++;
   if (h->graph2) cudaGraphExecDestroy(h->graph2);
   h->graph2 = nullptr;
   h->graph_cur = -1;
@@ -3459,6 +3461,217 @@ void sdem_destroy(sdem_h* h) {
   if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
+}
+
+// ---------------------------------------------------------------------------
+// Batched form: one handle for many independent beds.  A step of the batch is
+// one CUDA graph that forks from the batch stream into every member's streams,
+// holds each member's step (its own kernels, grids and tables), and joins
+// back: small beds that fill few SMs each run side by side on the GPU.  The
+// graph holds two steps (each member returns to the buffer parity it was
+// captured at) and is captured again when a member's own graphs were
+// invalidated (an upload of another size, new walls, types or fixed spheres)
+// or a member was stepped alone an odd number of times.
+}  // extern "C"
+
+struct sdem_batch {
+  std::vector<sdem_h*> m;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, after = nullptr;
+  std::vector<cudaEvent_t> done;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<long long> gen;   // members' graph generations at capture
+  std::vector<int> cur;         // members' buffer parities at capture
+  std::vector<long long> launches;   // members' kernel launches per replay
+  std::string err;
+};
+
+namespace {
+
+int batch_fail(sdem_batch* b, int code, const std::string& msg) {
+  b->err = msg;
+  return code;
+}
+
+// Enqueues one step of every member between a fork and a join on the batch
+// stream (captured or not).
+int batch_enqueue(sdem_batch* b) {
+  if (cudaEventRecord(b->fork, b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch fork event");
+  for (size_t k = 0; k < b->m.size(); k++) {
+    sdem_h* h = b->m[k];
+    if (cudaStreamWaitEvent(h->stream, b->fork, 0) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch fork");
+    if (h->n_host > 0) {
+      int rc = enqueue_step(h);
+      if (rc) return batch_fail(b, rc, std::string("member ") + std::to_string(k) + ": " + h->err);
+    }
+    if (cudaEventRecord(b->done[k], h->stream) != cudaSuccess ||
+        cudaStreamWaitEvent(b->stream, b->done[k], 0) != cudaSuccess)
+      return batch_fail(b, SDEM_E_CUDA, "batch join");
+  }
+  return 0;
+}
+
+int batch_capture(sdem_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  const size_t n = b->m.size();
+  std::vector<int> cur0(n);
+  std::vector<long long> l0(n);
+  std::vector<bool> mok(n);
+  for (size_t k = 0; k < n; k++) {
+    cur0[k] = b->m[k]->cur;
+    l0[k] = b->m[k]->launches;
+    mok[k] = b->m[k]->mirror_ok;
+  }
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return batch_fail(b, SDEM_E_CUDA, "batch capture");
+  int rc = batch_enqueue(b);
+  if (!rc) rc = batch_enqueue(b);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  // capture does not execute: the members' parities and counts stay
+  for (size_t k = 0; k < n; k++) {
+    sdem_h* h = b->m[k];
+    b->launches[k] = h->launches - l0[k];
+    h->launches = l0[k];
+    h->cur = cur0[k];
+    h->mirror_ok = mok[k];
+  }
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    b->graph = nullptr;
+    return batch_fail(b, SDEM_E_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+  }
+  for (size_t k = 0; k < n; k++) {
+    b->gen[k] = b->m[k]->graph_gen;
+    b->cur[k] = cur0[k];
+  }
+  return 0;
+}
+
+// Orders every member's later work (downloads, single steps) after the
+// batch's work so far.
+int batch_order_members(sdem_batch* b) {
+  if (cudaEventRecord(b->after, b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch event");
+  for (sdem_h* h : b->m)
+    if (cudaStreamWaitEvent(h->stream, b->after, 0) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch order");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdem_batch_create(int n, sdem_h* const* members, sdem_batch** out) {
+  if (!out) return SDEM_E_ARG;
+  *out = nullptr;
+  if (n < 1 || !members) return SDEM_E_ARG;
+  for (int k = 0; k < n; k++) {
+    if (!members[k]) return SDEM_E_ARG;
+    for (int j = 0; j < k; j++)
+      if (members[j] == members[k]) return SDEM_E_ARG;   // a handle joins once
+  }
+  sdem_batch* b = new sdem_batch();
+  *out = b;
+  b->m.assign(members, members + n);
+  b->gen.assign(n, -1);
+  b->cur.assign(n, -1);
+  b->launches.assign(n, 0);
+  b->done.assign(n, nullptr);
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->after, cudaEventDisableTiming) != cudaSuccess)
+    return batch_fail(b, SDEM_E_CUDA, "batch stream/events");
+  for (int k = 0; k < n; k++)
+    if (cudaEventCreateWithFlags(&b->done[k], cudaEventDisableTiming) != cudaSuccess)
+      return batch_fail(b, SDEM_E_CUDA, "batch events");
+  return 0;
+}
+
+int sdem_batch_step_async(sdem_batch* b, int nsteps) {
+  if (!b) return SDEM_E_ARG;
+  if (nsteps < 0) return batch_fail(b, SDEM_E_ARG, "sdem_batch_step: nsteps < 0");
+  for (size_t k = 0; k < b->m.size(); k++) {
+    sdem_h* h = b->m[k];
+    if (!h->have_types) return batch_fail(b, SDEM_E_ARG, "member " + std::to_string(k) + ": call sdem_set_types first");
+    if (h->prof) return batch_fail(b, SDEM_E_ARG, "member " + std::to_string(k) + ": profiling window open");
+  }
+  // the batch's work follows everything already enqueued on the members
+  if (cudaEventRecord(b->fork, b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch event");
+  for (size_t k = 0; k < b->m.size(); k++) {
+    if (cudaEventRecord(b->done[k], b->m[k]->stream) != cudaSuccess ||
+        cudaStreamWaitEvent(b->stream, b->done[k], 0) != cudaSuccess)
+      return batch_fail(b, SDEM_E_CUDA, "batch order");
+  }
+  int left = nsteps;
+  while (left >= 2) {
+    bool valid = b->graph != nullptr;
+    for (size_t k = 0; valid && k < b->m.size(); k++)
+      valid = b->gen[k] == b->m[k]->graph_gen && b->cur[k] == b->m[k]->cur;
+    if (!valid) {
+      int rc = batch_capture(b);
+      if (rc) return rc;
+    }
+    if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch graph launch");
+    for (size_t k = 0; k < b->m.size(); k++) {
+      sdem_h* h = b->m[k];
+      if (h->n_host == 0) continue;
+      h->launches += b->launches[k];
+      h->iter_host += 2;
+      h->ev_iter[0] = h->ev_iter[1] = -1;   // no per-step events inside the batch graph
+      h->mirror_ok = true;
+      h->stepped = true;
+    }
+    left -= 2;
+  }
+  if (left == 1) {
+    int rc = batch_enqueue(b);   // plain launches
+    if (rc) return rc;
+    for (sdem_h* h : b->m) {
+      if (h->n_host == 0) continue;
+      h->iter_host += 1;
+      h->ev_iter[0] = h->ev_iter[1] = -1;
+      h->stepped = true;
+    }
+  }
+  return batch_order_members(b);
+}
+
+int sdem_batch_sync(sdem_batch* b) {
+  if (!b) return SDEM_E_ARG;
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch synchronisation");
+  for (size_t k = 0; k < b->m.size(); k++) {
+    int rc = sync_and_check(b->m[k]);
+    if (rc) return batch_fail(b, rc, "member " + std::to_string(k) + ": " + b->m[k]->err);
+  }
+  b->err.clear();
+  return 0;
+}
+
+int sdem_batch_step(sdem_batch* b, int nsteps) {
+  int rc = sdem_batch_step_async(b, nsteps);
+  if (rc) return rc;
+  return sdem_batch_sync(b);
+}
+
+const char* sdem_batch_last_error(sdem_batch* b) { return b ? b->err.c_str() : ""; }
+
+void sdem_batch_destroy(sdem_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (cudaEvent_t e : b->done)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->after) cudaEventDestroy(b->after);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
 }
 
 }  // extern "C"
