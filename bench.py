@@ -370,6 +370,64 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
+def sandboxes_arm(args):
+    """The batched workload (not the headline line): `--instances` sandboxes
+    of 2,000-50,000 spheres with their own materials, contact models and
+    boxes (sdem_gb300.beds.sandbox_case, parameters from seed 4), advanced
+    (a) as one batch (sdem_batch_step: one graph per two steps for all of
+    them), (b) one instance after another (each instance's steps, then the
+    next instance), (c) every instance on its own stream from one host
+    thread.  Host wall-clock around synchronised runs; particle-steps/s of
+    the whole set."""
+    import torch
+    from sdem_gb300 import beds
+    from sdem_gb300.capi import DEMBatch, DEMSystem
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(4)
+    cases = [beds.sandbox_case(rng, i) for i in range(args.instances)]
+    total = sum(c.particles.n for c in cases)
+    members = [DEMSystem(c) for c in cases]
+    batch = DEMBatch(members)
+    K = args.steps + args.steps % 2          # whole graph replays
+    batch.step(2 * ((args.warmup + 1) // 2))   # even: the captured parities hold
+    t0 = time.perf_counter()
+    batch.step(K)
+    t_batch = time.perf_counter() - t0
+    contacts = sum(m.counters()["pp"] + m.counters()["pw"] for m in members)
+    for m in members:                        # each instance's own graphs, captured before timing
+        m.step(4)
+    t0 = time.perf_counter()
+    for m in members:
+        m.step(K)
+    t_seq = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for m in members:
+        m.step_async(K)
+    for m in members:
+        m.counters()
+    t_streams = time.perf_counter() - t0
+    line = {"metric": "particle-steps/s, %d sandboxes" % args.instances, "value": total * K / t_batch,
+            "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": t_batch / K * 1e3,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "sandboxes", "instances": args.instances, "particles": total,
+                       "contacts_last": contacts, "models": {
+                           "hertz": sum(1 for c in cases if c.opts.cf_type == props_cft_nlin()),
+                           "lsd": sum(1 for c in cases if c.opts.cf_type != props_cft_nlin())}},
+            "one_instance_after_another": total * K / t_seq,
+            "instances_on_own_streams": total * K / t_streams,
+            "note": "host wall clock around synchronised runs of the same sandboxes, in this order: batch, "
+                    "one instance after another, every instance on its own stream"}
+    print(json.dumps(line), flush=True)
+    batch.close()
+    for m in members:
+        m.close()
+
+
+def props_cft_nlin():
+    from sdem_gb300 import props
+    return props.CFT_NLIN
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -380,10 +438,15 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=-1,
                     help="steps of the end-to-end run (default: --steps; 0 skips it)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="hertz_poly_1m", choices=["hertz_poly_1m", "sandboxes"],
+                    help="sandboxes: the batched workload (its own line; not the headline)")
+    ap.add_argument("--instances", type=int, default=512)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload == "sandboxes":
+        sandboxes_arm(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         our_arm(args)

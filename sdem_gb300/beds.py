@@ -601,5 +601,48 @@ def fixed_floor_case(n: int, seed: int, **kw) -> Case:
     return Case(f"fixedfloor_{n}_{seed}", opts, case.tables, walls, parts, fixed=fixed)
 
 
+def sandbox_case(rng: np.random.Generator, index: int, n_lo: int = 2000, n_hi: int = 50000) -> Case:
+    """One sandbox of the batched workload: n ~ U{n_lo..n_hi} spheres with d
+    uniform in [0.8, 1.2] mm (five types, density 2500 kg/m^3), sliding
+    friction U(0.1, 0.5), restitution U(0.5, 0.95), linear spring-dashpot or
+    Hertz-Mindlin by a coin flip, dt = 2e-6 s, AB2; a jittered simple-cubic
+    lattice (pitch 1.3 d_max) filling a box of aspect ratios x:y:z = a:1:b with
+    a, b ~ U(0.5, 2), five infinite walls, velocities U(-0.05, 0.05) m/s.  The
+    parameters are drawn from `rng` in a fixed order."""
+    n = int(rng.integers(n_lo, n_hi + 1))
+    mu = float(rng.uniform(0.1, 0.5))
+    e_n = float(rng.uniform(0.5, 0.95))
+    cf = props.CFT_LSD if rng.uniform() < 0.5 else props.CFT_NLIN
+    a, b = float(rng.uniform(0.5, 2.0)), float(rng.uniform(0.5, 2.0))
+    seed = int(rng.integers(0, 2**31 - 1))
+    ntypes = 5
+    diam = np.linspace(0.8e-3, 1.2e-3, ntypes)
+    coefs = (mu, mu, 0.1, e_n, e_n)
+    if cf == props.CFT_NLIN:
+        E = 5.0e7
+    else:
+        E = props.lsd_youngs_for_stiffness(1.0e4, 0.05, float(diam.mean()), 2500.0, 0.3)
+    tables = props.build_tables(cf, list(diam), [2500.0] * ntypes, [E] * ntypes, [0.3] * ntypes, coefs, [E], [0.3],
+                                coefs)
+    pitch = 1.3 * diam[-1]
+    k = (n / (a * b)) ** (1.0 / 3.0)
+    nx, ny, nz = max(1, int(math.ceil(a * k))), max(1, int(math.ceil(k))), max(1, int(math.ceil(b * k)))
+    while nx * ny * nz < n:
+        ny += 1
+    g = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    # fill from the floor up
+    g = g[np.lexsort((g[:, 2], g[:, 0], g[:, 1]))][:n]
+    r = np.random.default_rng(seed)
+    pos = (g + 0.5) * pitch + 0.2e-3 + r.uniform(-0.05, 0.05, size=(n, 3)) * pitch
+    box = (nx * pitch + 0.4e-3, (ny + 2) * pitch + 0.4e-3, nz * pitch + 0.4e-3)
+    ptype = r.integers(1, ntypes + 1, size=n).astype(np.int32)
+    vel = r.uniform(-0.05, 0.05, size=(n, 3))
+    opts = Options(dt=2.0e-6, minpoint=(0.0, 0.0, 0.0), maxpoint=box, cf_type=cf, pi_method=2, pri_method=2)
+    parts = new_particles(pos, ptype, tables.radius, vel, opts.tsize, opts.rsize)
+    walls = box_walls(opts.minpoint, opts.maxpoint, infinite=True, base_wall_id=opts.base_wall_id, skip_axes=())
+    return Case(f"sandbox_{index}", opts, tables, walls, parts,
+                note=f"{'Hertz' if cf == props.CFT_NLIN else 'LSD'} mu={mu:.3f} e={e_n:.3f} n={n}")
+
+
 def scaled(case: Case, **opt_changes) -> Case:
     return replace(case, opts=replace(case.opts, **opt_changes))

@@ -3464,25 +3464,36 @@ void sdem_destroy(sdem_h* h) {
 }
 
 // ---------------------------------------------------------------------------
-// Batched form: one handle for many independent beds.  A step of the batch is
-// one CUDA graph that forks from the batch stream into every member's streams,
-// holds each member's step (its own kernels, grids and tables), and joins
-// back: small beds that fill few SMs each run side by side on the GPU.  The
-// graph holds two steps (each member returns to the buffer parity it was
-// captured at) and is captured again when a member's own graphs were
-// invalidated (an upload of another size, new walls, types or fixed spheres)
-// or a member was stepped alone an odd number of times.
+// Batched form: one handle for many independent beds.  The members are split
+// into groups of up to SDEM_BATCH_GROUP; a batch step is one CUDA graph per
+// group, which forks from the group's stream into every member's streams,
+// holds each member's step (its own kernels, grids and tables) and joins
+// back, and the groups' graphs run on their own streams: small beds that fill
+// few SMs each run side by side.  (512 sandboxes of 2,000-50,000 spheres: one
+// graph over all of them ran at 0.59 G particle-steps/s, the members on their
+// own streams at 1.66 G, groups of 8 / 16 / 32 / 64 / 128 at 1.40 / 1.67 /
+// 1.72 / 1.74 / 1.51 G.)  A group graph holds two steps (each member returns to the
+// buffer parity it was captured at) and is captured again when a member's
+// own graphs were invalidated (an upload of another size, new walls, types or
+// fixed spheres) or a member was stepped alone an odd number of times.
+#ifndef SDEM_BATCH_GROUP
+#define SDEM_BATCH_GROUP 64
+#endif
 }  // extern "C"
 
 struct sdem_batch {
+  struct Group {
+    std::vector<sdem_h*> m;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, after = nullptr;
+    std::vector<cudaEvent_t> done;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<long long> gen;        // members' graph generations at capture
+    std::vector<int> cur;              // members' buffer parities at capture
+    std::vector<long long> launches;   // members' kernel launches per replay
+  };
   std::vector<sdem_h*> m;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t fork = nullptr, after = nullptr;
-  std::vector<cudaEvent_t> done;
-  cudaGraphExec_t graph = nullptr;
-  std::vector<long long> gen;   // members' graph generations at capture
-  std::vector<int> cur;         // members' buffer parities at capture
-  std::vector<long long> launches;   // members' kernel launches per replay
+  std::vector<Group> g;
   std::string err;
 };
 
@@ -3493,46 +3504,46 @@ int batch_fail(sdem_batch* b, int code, const std::string& msg) {
   return code;
 }
 
-// Enqueues one step of every member between a fork and a join on the batch
-// stream (captured or not).
-int batch_enqueue(sdem_batch* b) {
-  if (cudaEventRecord(b->fork, b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch fork event");
-  for (size_t k = 0; k < b->m.size(); k++) {
-    sdem_h* h = b->m[k];
-    if (cudaStreamWaitEvent(h->stream, b->fork, 0) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch fork");
+// Enqueues one step of every member of a group between a fork and a join on
+// the group's stream (captured or not).
+int batch_enqueue(sdem_batch* b, sdem_batch::Group& G) {
+  if (cudaEventRecord(G.fork, G.stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch fork event");
+  for (size_t k = 0; k < G.m.size(); k++) {
+    sdem_h* h = G.m[k];
+    if (cudaStreamWaitEvent(h->stream, G.fork, 0) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch fork");
     if (h->n_host > 0) {
       int rc = enqueue_step(h);
-      if (rc) return batch_fail(b, rc, std::string("member ") + std::to_string(k) + ": " + h->err);
+      if (rc) return batch_fail(b, rc, "member: " + h->err);
     }
-    if (cudaEventRecord(b->done[k], h->stream) != cudaSuccess ||
-        cudaStreamWaitEvent(b->stream, b->done[k], 0) != cudaSuccess)
+    if (cudaEventRecord(G.done[k], h->stream) != cudaSuccess ||
+        cudaStreamWaitEvent(G.stream, G.done[k], 0) != cudaSuccess)
       return batch_fail(b, SDEM_E_CUDA, "batch join");
   }
   return 0;
 }
 
-int batch_capture(sdem_batch* b) {
-  if (b->graph) cudaGraphExecDestroy(b->graph);
-  b->graph = nullptr;
-  const size_t n = b->m.size();
+int batch_capture(sdem_batch* b, sdem_batch::Group& G) {
+  if (G.graph) cudaGraphExecDestroy(G.graph);
+  G.graph = nullptr;
+  const size_t n = G.m.size();
   std::vector<int> cur0(n);
   std::vector<long long> l0(n);
   std::vector<bool> mok(n);
   for (size_t k = 0; k < n; k++) {
-    cur0[k] = b->m[k]->cur;
-    l0[k] = b->m[k]->launches;
-    mok[k] = b->m[k]->mirror_ok;
+    cur0[k] = G.m[k]->cur;
+    l0[k] = G.m[k]->launches;
+    mok[k] = G.m[k]->mirror_ok;
   }
   cudaGraph_t g = nullptr;
-  if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+  if (cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return batch_fail(b, SDEM_E_CUDA, "batch capture");
-  int rc = batch_enqueue(b);
-  if (!rc) rc = batch_enqueue(b);
-  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  int rc = batch_enqueue(b, G);
+  if (!rc) rc = batch_enqueue(b, G);
+  cudaError_t e = cudaStreamEndCapture(G.stream, &g);
   // capture does not execute: the members' parities and counts stay
   for (size_t k = 0; k < n; k++) {
-    sdem_h* h = b->m[k];
-    b->launches[k] = h->launches - l0[k];
+    sdem_h* h = G.m[k];
+    G.launches[k] = h->launches - l0[k];
     h->launches = l0[k];
     h->cur = cur0[k];
     h->mirror_ok = mok[k];
@@ -3542,25 +3553,16 @@ int batch_capture(sdem_batch* b) {
     return rc;
   }
   if (e != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&b->graph, g, 0);
+  e = cudaGraphInstantiate(&G.graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
-    b->graph = nullptr;
+    G.graph = nullptr;
     return batch_fail(b, SDEM_E_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
   }
   for (size_t k = 0; k < n; k++) {
-    b->gen[k] = b->m[k]->graph_gen;
-    b->cur[k] = cur0[k];
+    G.gen[k] = G.m[k]->graph_gen;
+    G.cur[k] = cur0[k];
   }
-  return 0;
-}
-
-// Orders every member's later work (downloads, single steps) after the
-// batch's work so far.
-int batch_order_members(sdem_batch* b) {
-  if (cudaEventRecord(b->after, b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch event");
-  for (sdem_h* h : b->m)
-    if (cudaStreamWaitEvent(h->stream, b->after, 0) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch order");
   return 0;
 }
 
@@ -3572,25 +3574,35 @@ int sdem_batch_create(int n, sdem_h* const* members, sdem_batch** out) {
   if (!out) return SDEM_E_ARG;
   *out = nullptr;
   if (n < 1 || !members) return SDEM_E_ARG;
-  for (int k = 0; k < n; k++) {
+  for (int k = 0; k < n; k++)
     if (!members[k]) return SDEM_E_ARG;
-    for (int j = 0; j < k; j++)
-      if (members[j] == members[k]) return SDEM_E_ARG;   // a handle joins once
+  {
+    std::vector<sdem_h*> sorted_m(members, members + n);
+    std::sort(sorted_m.begin(), sorted_m.end());
+    if (std::adjacent_find(sorted_m.begin(), sorted_m.end()) != sorted_m.end()) return SDEM_E_ARG;   // a handle joins once
   }
   sdem_batch* b = new sdem_batch();
   *out = b;
   b->m.assign(members, members + n);
-  b->gen.assign(n, -1);
-  b->cur.assign(n, -1);
-  b->launches.assign(n, 0);
-  b->done.assign(n, nullptr);
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->after, cudaEventDisableTiming) != cudaSuccess)
-    return batch_fail(b, SDEM_E_CUDA, "batch stream/events");
-  for (int k = 0; k < n; k++)
-    if (cudaEventCreateWithFlags(&b->done[k], cudaEventDisableTiming) != cudaSuccess)
-      return batch_fail(b, SDEM_E_CUDA, "batch events");
+  const int ng = (n + SDEM_BATCH_GROUP - 1) / SDEM_BATCH_GROUP;
+  b->g.resize(ng);
+  for (int q = 0; q < ng; q++) {
+    sdem_batch::Group& G = b->g[q];
+    const int lo = q * n / ng, hi = (q + 1) * n / ng;   // groups of nearly equal size
+    G.m.assign(members + lo, members + hi);
+    const size_t m = G.m.size();
+    G.gen.assign(m, -1);
+    G.cur.assign(m, -1);
+    G.launches.assign(m, 0);
+    G.done.assign(m, nullptr);
+    if (cudaStreamCreateWithFlags(&G.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&G.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&G.after, cudaEventDisableTiming) != cudaSuccess)
+      return batch_fail(b, SDEM_E_CUDA, "batch streams/events");
+    for (size_t k = 0; k < m; k++)
+      if (cudaEventCreateWithFlags(&G.done[k], cudaEventDisableTiming) != cudaSuccess)
+        return batch_fail(b, SDEM_E_CUDA, "batch events");
+  }
   return 0;
 }
 
@@ -3602,50 +3614,55 @@ int sdem_batch_step_async(sdem_batch* b, int nsteps) {
     if (!h->have_types) return batch_fail(b, SDEM_E_ARG, "member " + std::to_string(k) + ": call sdem_set_types first");
     if (h->prof) return batch_fail(b, SDEM_E_ARG, "member " + std::to_string(k) + ": profiling window open");
   }
-  // the batch's work follows everything already enqueued on the members
-  if (cudaEventRecord(b->fork, b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch event");
-  for (size_t k = 0; k < b->m.size(); k++) {
-    if (cudaEventRecord(b->done[k], b->m[k]->stream) != cudaSuccess ||
-        cudaStreamWaitEvent(b->stream, b->done[k], 0) != cudaSuccess)
-      return batch_fail(b, SDEM_E_CUDA, "batch order");
-  }
-  int left = nsteps;
-  while (left >= 2) {
-    bool valid = b->graph != nullptr;
-    for (size_t k = 0; valid && k < b->m.size(); k++)
-      valid = b->gen[k] == b->m[k]->graph_gen && b->cur[k] == b->m[k]->cur;
-    if (!valid) {
-      int rc = batch_capture(b);
+  for (sdem_batch::Group& G : b->g) {
+    // the group's work follows everything already enqueued on its members
+    for (size_t k = 0; k < G.m.size(); k++)
+      if (cudaEventRecord(G.done[k], G.m[k]->stream) != cudaSuccess ||
+          cudaStreamWaitEvent(G.stream, G.done[k], 0) != cudaSuccess)
+        return batch_fail(b, SDEM_E_CUDA, "batch order");
+    int left = nsteps;
+    while (left >= 2) {
+      bool valid = G.graph != nullptr;
+      for (size_t k = 0; valid && k < G.m.size(); k++)
+        valid = G.gen[k] == G.m[k]->graph_gen && G.cur[k] == G.m[k]->cur;
+      if (!valid) {
+        int rc = batch_capture(b, G);
+        if (rc) return rc;
+      }
+      if (cudaGraphLaunch(G.graph, G.stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch graph launch");
+      for (size_t k = 0; k < G.m.size(); k++) {
+        sdem_h* h = G.m[k];
+        if (h->n_host == 0) continue;
+        h->launches += G.launches[k];
+        h->iter_host += 2;
+        h->ev_iter[0] = h->ev_iter[1] = -1;   // no per-step events inside the group graph
+        h->mirror_ok = true;
+        h->stepped = true;
+      }
+      left -= 2;
+    }
+    if (left == 1) {
+      int rc = batch_enqueue(b, G);   // plain launches
       if (rc) return rc;
+      for (sdem_h* h : G.m) {
+        if (h->n_host == 0) continue;
+        h->iter_host += 1;
+        h->ev_iter[0] = h->ev_iter[1] = -1;
+        h->stepped = true;
+      }
     }
-    if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch graph launch");
-    for (size_t k = 0; k < b->m.size(); k++) {
-      sdem_h* h = b->m[k];
-      if (h->n_host == 0) continue;
-      h->launches += b->launches[k];
-      h->iter_host += 2;
-      h->ev_iter[0] = h->ev_iter[1] = -1;   // no per-step events inside the batch graph
-      h->mirror_ok = true;
-      h->stepped = true;
-    }
-    left -= 2;
+    // the members' later work (downloads, single steps) follows the group's
+    if (cudaEventRecord(G.after, G.stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch event");
+    for (sdem_h* h : G.m)
+      if (cudaStreamWaitEvent(h->stream, G.after, 0) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch order");
   }
-  if (left == 1) {
-    int rc = batch_enqueue(b);   // plain launches
-    if (rc) return rc;
-    for (sdem_h* h : b->m) {
-      if (h->n_host == 0) continue;
-      h->iter_host += 1;
-      h->ev_iter[0] = h->ev_iter[1] = -1;
-      h->stepped = true;
-    }
-  }
-  return batch_order_members(b);
+  return 0;
 }
 
 int sdem_batch_sync(sdem_batch* b) {
   if (!b) return SDEM_E_ARG;
-  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch synchronisation");
+  for (sdem_batch::Group& G : b->g)
+    if (cudaStreamSynchronize(G.stream) != cudaSuccess) return batch_fail(b, SDEM_E_CUDA, "batch synchronisation");
   for (size_t k = 0; k < b->m.size(); k++) {
     int rc = sync_and_check(b->m[k]);
     if (rc) return batch_fail(b, rc, "member " + std::to_string(k) + ": " + b->m[k]->err);
@@ -3664,13 +3681,15 @@ const char* sdem_batch_last_error(sdem_batch* b) { return b ? b->err.c_str() : "
 
 void sdem_batch_destroy(sdem_batch* b) {
   if (!b) return;
-  if (b->stream) cudaStreamSynchronize(b->stream);
-  if (b->graph) cudaGraphExecDestroy(b->graph);
-  for (cudaEvent_t e : b->done)
-    if (e) cudaEventDestroy(e);
-  if (b->fork) cudaEventDestroy(b->fork);
-  if (b->after) cudaEventDestroy(b->after);
-  if (b->stream) cudaStreamDestroy(b->stream);
+  for (sdem_batch::Group& G : b->g) {
+    if (G.stream) cudaStreamSynchronize(G.stream);
+    if (G.graph) cudaGraphExecDestroy(G.graph);
+    for (cudaEvent_t e : G.done)
+      if (e) cudaEventDestroy(e);
+    if (G.fork) cudaEventDestroy(G.fork);
+    if (G.after) cudaEventDestroy(G.after);
+    if (G.stream) cudaStreamDestroy(G.stream);
+  }
   delete b;
 }
 
