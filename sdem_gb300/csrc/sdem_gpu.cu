@@ -143,6 +143,7 @@ struct Dev {
   int *cell_of, *cell_cnt, *cell_start, *tmp_rank, *tmp_sorted, *sorted, *sortpos;
   float4* spos;      // cell-sorted single-precision copy (offsets in the cell, r) for the prefilter
   float4* pf;        // the same per particle index, written by the binning
+  int4* pcell;   // per index: the cell (ix, iy, iz, key in its level's grid), written by the binning
   fpi::Divisor cdiv; // the cell length as a divisor
   float pf_margin;   // prefilter margin, bounds the single-precision distance error
   float cellf;       // cell size in single precision
@@ -597,8 +598,10 @@ __global__ void k_bin(Dev d) {
   // int-to-float conversion would take the FP64 pipe's rate)
   auto unit = [](int32_t o) { return __uint_as_float(0x3F800000u | ((uint32_t)o >> 8)) - 1.0f; };
   d.pf[p] = make_float4(unit(ox) * cellf, unit(oy) * cellf, unit(oz) * cellf, fpi::to_float_trunc(P.w));
-  long long key = base + ((long long)fy * nx + (long long)fx) * nz + (long long)fz;
+  const long long lkey = ((long long)fy * nx + (long long)fx) * nz + (long long)fz;
+  const long long key = base + lkey;
   d.cell_of[p] = (int)key;
+  if (d.pcell) d.pcell[p] = make_int4(fx, fy, fz, (int)lkey);
   d.tmp_rank[p] = atomicAdd(&d.cell_cnt[key], 1);
 }
 
@@ -668,13 +671,10 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
         lbase = G.base;
         cellf = G.cellf;
       }
-      const int key = (int)(d.cell_of[m] - lbase);
-      const int iz = key % nz;
-      const int rest = key / nz;
-      const int ix = rest % nx;
-      const int iy = rest / nx;
+      // the target's cell, as the binning found it (in its level's grid)
+      const int4 tc = d.pcell[m];
+      const int ix = tc.x, iy = tc.y, iz = tc.z, key = tc.w;
       const float4 Pf = d.spos[s];
-      const dbl4 Pm = d.posr[m];
       const float margin = d.pf_margin;
       int cnt = 0;
       const int K = d.K, Kin = d.Kin, ncap = d.ncap, nall = d.nall;
@@ -698,7 +698,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
         const int q = d.sorted[t];
         const float blo = rs - margin;
         if (!(d2f < blo * blo)) {
-          const dbl4 Pq = d.posr[q];
+          const dbl4 Pm = d.posr[m], Pq = d.posr[q];
           double dr = Pm.w + Pq.w;
           double dr2 = dr * dr;
           double dx = Pm.x - Pq.x;
@@ -1781,6 +1781,7 @@ struct sdem_h {
   dbl4 *w_geo = nullptr, *w_S = nullptr, *w_M = nullptr, *w_Mr = nullptr;
   float4* spos = nullptr;
   float4* pf = nullptr;
+  int4* pcell = nullptr;
   float pf_margin = 0.f;
   int *deg_cnt = nullptr, *deg_of = nullptr, *deg_rank = nullptr;
   int4* gorder = nullptr;
@@ -1984,6 +1985,7 @@ Dev make_dev(sdem_h* h) {
   d.sortpos = h->sortpos;
   d.spos = h->spos;
   d.pf = h->pf;
+  d.pcell = h->pcell;
   d.cdiv = fpi::divisor(h->cell);
   d.deg_cnt = h->deg_cnt;
   d.deg_of = h->deg_of;
@@ -2339,6 +2341,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   rc |= dalloc(h, &h->sortpos, NA);
   rc |= dalloc(h, &h->spos, NA);
   rc |= dalloc(h, &h->pf, NA);
+  rc |= dalloc(h, &h->pcell, NA);
   rc |= dalloc(h, &h->deg_cnt, kDegBuckets);
   rc |= dalloc(h, &h->deg_of, N);
   rc |= dalloc(h, &h->deg_rank, N);
