@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
         if (cx < 0 || cx >= nx || cy < 0) {
           cb[c][0] = cb[c][1] = cb[c][2] = cb[c][3] = 0;
         } else {
-          const long long kb = ((long long)cy * nx + cx) * nz + iz;
+          const int kb = (cy * nx + cx) * nz + iz;   // the grid holds fewer than 2^31 cells
           cb[c][1] = cs[kb];
           cb[c][2] = cs[kb + 1];
           cb[c][0] = iz > 0 ? cs[kb - 1] : cb[c][1];
@@ -779,7 +779,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
             for (int lx = -1; lx <= 1; lx++) {
               const int cx = cx0 + lx;
               if (cx < 0 || cx >= X.nx) continue;
-              const long long kc = ((long long)cy * X.nx + cx) * X.nz;
+              const int kc = (cy * X.nx + cx) * X.nz;
               const float ox = (float)(ix - cx * coe) * cellf, oy = (float)(iy - cy * coe) * cellf;
               for (int l = -1; l <= 1; l++) {
                 const int cz = cz0 + l;
