@@ -237,7 +237,7 @@ int sdem_counters_lagged(sdem_h* h, int* out);
  * travels.  The host arrays take the layouts of sdem_download_particles
  * (n_capacity rows suffice) plus F and T (3 doubles per particle); any may be
  * NULL.  Page-locked host arrays let the copy run at full speed; others are
- * staged by the driver.  They must stay valid and untouched until
+ * staged by the CUDA driver.  They must stay valid and untouched until
  * sdem_snapshot_end returns.  want_contacts != 0 also freezes the contact
  * list (history included), read after sdem_snapshot_end with
  * sdem_snapshot_contacts in the listing of sdem_download_contacts.  A new
