@@ -93,3 +93,23 @@ def test_batch_reports_member_errors(gpu_lib):
     batch.close()
     ok.close()
     bad.close()
+
+
+def test_batch_of_many_sandboxes_in_groups(gpu_lib):
+    # more members than one group holds (64): two group graphs on two streams
+    rng = np.random.default_rng(4)
+    cs = [beds.sandbox_case(rng, i, n_lo=200, n_hi=800) for i in range(70)]
+    alone = [DEMSystem(c) for c in cs]
+    members = [DEMSystem(c) for c in cs]
+    batch = DEMBatch(members)
+    for a in alone:
+        a.step(7)
+    batch.step(7)
+    for k, (a, m) in enumerate(zip(alone, members)):
+        sa, sm = a.state(), m.state()
+        for f in FIELDS:
+            np.testing.assert_array_equal(getattr(sa, f), getattr(sm, f), err_msg=f"sandbox {k}: {f}")
+        assert a.counters() == m.counters(), f"sandbox {k}"
+    batch.close()
+    for s in alone + members:
+        s.close()
