@@ -94,6 +94,18 @@ const char* const kPhaseNames[kPhases] = {"wall_refresh", "bin", "scan_cells", "
                                           "scan_rows", "row_fill", "force", "wall_force", "gather_integrate",
                                           "delete", "step_end"};
 
+// What the gather reads first for the sphere at one gather position, written
+// by the degree scatter in index order (coalesced there) so that the gather
+// reads one record instead of several scattered values.
+struct __align__(32) GRec {
+  int p;        // the sphere
+  int s;        // its sort position
+  int own_a;    // its row start
+  int counts;   // row length << 16 | in-list length << 8 | wall contacts
+  double r;     // its radius
+  double pad;
+};
+
 // ---------------------------------------------------------------------------
 // Device view of one handle, passed by value to every kernel.
 struct Dev {
@@ -179,8 +191,7 @@ struct Dev {
   // gather order: particles bucketed by their number of contact records, so a
   // warp's summation loops run the same trip count
   int *deg_cnt, *deg_of, *deg_rank;
-  int4* gorder;   // per gather position: sphere, its sort position, its row start,
-                  // row length << 16 | in-list length << 8 | wall contacts
+  struct GRec* gorder;   // per gather position: what the gather reads first
   const int *wh_cnt_prev, *wh_wall_prev;
   const dbl4* wh_hist_prev;
   // status and scalars
@@ -879,8 +890,14 @@ __global__ void k_degree_scatter(Dev d) {
   // from the row of p) and stored at the gather position in one record
   const int s = d.sortpos[p];
   const int nin = min(d.in_cnt[p], d.Kin);
-  d.gorder[start[d.deg_of[p]] + d.deg_rank[p]] =
-      make_int4(p, s, d.row_off[s], (d.row_cnt[s] << 16) | (nin << 8) | d.w_cnt[p]);
+  GRec g;
+  g.p = p;
+  g.s = s;
+  g.own_a = d.row_off[s];
+  g.counts = (d.row_cnt[s] << 16) | (nin << 8) | d.w_cnt[p];
+  g.r = d.posr[p].w;
+  g.pad = 0.0;
+  d.gorder[start[d.deg_of[p]] + d.deg_rank[p]] = g;
 }
 
 // One thread per wall contact: Find_insert on the particle's bucket (key = wall)
@@ -1050,10 +1067,10 @@ __device__ __forceinline__ void sort_net(unsigned (&v)[N]) {
 __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= *d.n) return;
-  const int4 gr = d.gorder[tid];
-  const int p = gr.x, s = gr.y;
+  const GRec gr = d.gorder[tid];
+  const int p = gr.p, s = gr.s;
   const int ncap = d.ncap;
-  const double rp = d.posr[p].w;
+  const double rp = gr.r;
   r3 F = sdem::mk3(0.0, 0.0, 0.0), T = sdem::mk3(0.0, 0.0, 0.0);
 
   // The contact records of p in the reference's scatter order: in-list
@@ -1061,9 +1078,9 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   // targets, then wall contacts.  Their indices go to a small per-thread list
   // first (integer work), so the FP64 additions run in one loop whose trip
   // count is the warp's maximum, not once per branch.
-  const int own_a = gr.z, own_n = gr.w >> 16;
-  const int nin = (gr.w >> 8) & 0xFF;
-  const int nwc = gr.w & 0xFF;
+  const int own_a = gr.own_a, own_n = gr.counts >> 16;
+  const int nin = (gr.counts >> 8) & 0xFF;
+  const int nwc = gr.counts & 0xFF;
   // entry: (contact index << 1) | (p is the row's target), or -(wall slot + 1)
   int list[2 * kMaxK + kKw];
   int nl = 0;
@@ -1784,7 +1801,7 @@ struct sdem_h {
   int4* pcell = nullptr;
   float pf_margin = 0.f;
   int *deg_cnt = nullptr, *deg_of = nullptr, *deg_rank = nullptr;
-  int4* gorder = nullptr;
+  GRec* gorder = nullptr;
   // second stream and events of the chunked search/force pipeline
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chunk[kChunks] = {};
