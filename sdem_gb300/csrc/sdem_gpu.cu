@@ -985,11 +985,18 @@ __global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s
     const int tb = img ? (m_loc ? tq : tm) : (m_lo ? tq : tm);
     dbl4 hist = make_dbl4(0.0, 0.0, 0.0, -2.0);
     {
-      const int k = d.own_cnt_prev[owner];
       const int2* oe = d.own_c_prev + (size_t)owner * d.Ko;
-      for (int j = 0; j < k; j++) {
-        const int2 e = oe[j];
-        if (e.y == partner) { hist = d.c_hist_prev[e.x]; break; }
+      // the first entry is read beside the count (the table always holds Ko
+      // entries per owner; an entry past the count is not used)
+      const int2 e0 = oe[0];
+      const int k = d.own_cnt_prev[owner];
+      if (k > 0 && e0.y == partner) {
+        hist = d.c_hist_prev[e0.x];
+      } else {
+        for (int j = 1; j < k; j++) {
+          const int2 e = oe[j];
+          if (e.y == partner) { hist = d.c_hist_prev[e.x]; break; }
+        }
       }
     }
     const double* P = d.bpp + ((size_t)(tb - 1) * d.nT + (ta - 1)) * SDEM_BP_SIZE;
