@@ -1582,26 +1582,27 @@ __global__ void k_pack3(double* __restrict__ dst, const dbl4* __restrict__ src, 
   v[2] = a.z;
 }
 
-// Ends a step: the counters of the step (CL and search logs), running sums,
-// per-step resets, and a copy of the device scalars (status, particle count,
-// counters) into mapped host memory, so that the host reads them after a
-// stream synchronisation without another copy.  Two mirror slots, by the
-// parity of the new iteration number: a step's copy survives while the next
-// step runs.
-__device__ void step_end_serial(const Dev& d, int* counters_out, const int* scal, int* mirror, int nscal) {
+// Ends a step: the counters of the step (CL and search logs), running sums and
+// per-step resets.
+__device__ void step_end_serial(const Dev& d, int* counters_out) {
+  // every value first (the loads issue together), then the stores
   const int C = d.row_off[d.nall_launch];
-  counters_out[SDEM_CNT_PP] = C - (int)d.counters[5] - (int)d.counters[8];
-  counters_out[SDEM_CNT_PPG] = (int)d.counters[5];
-  counters_out[SDEM_CNT_PPFIX] = (int)d.counters[8];
-  counters_out[SDEM_CNT_PW] = (int)d.counters[1];
-  counters_out[SDEM_CNT_CNSV] = (int)d.counters[0];
-  counters_out[SDEM_CNT_NLOCAL] = *d.n;
-  *d.iter += 1;
-  counters_out[SDEM_CNT_ITER] = *d.iter;
-  counters_out[SDEM_CNT_NEXTWALL] = *d.next_update;
-  counters_out[SDEM_CNT_CNSV_CROSS] = (int)d.counters[9];
-  d.counters[2] += (unsigned long long)(C - (int)d.counters[5] - (int)d.counters[8]);
-  d.counters[3] += d.counters[1];
+  const unsigned long long cnsv = d.counters[0], pw = d.counters[1], ppg = d.counters[5], fx = d.counters[8],
+                           cross = d.counters[9];
+  const int n = *d.n, it = *d.iter + 1, next = *d.next_update;
+  const int pp = C - (int)ppg - (int)fx;
+  counters_out[SDEM_CNT_PP] = pp;
+  counters_out[SDEM_CNT_PPG] = (int)ppg;
+  counters_out[SDEM_CNT_PPFIX] = (int)fx;
+  counters_out[SDEM_CNT_PW] = (int)pw;
+  counters_out[SDEM_CNT_CNSV] = (int)cnsv;
+  counters_out[SDEM_CNT_NLOCAL] = n;
+  *d.iter = it;
+  counters_out[SDEM_CNT_ITER] = it;
+  counters_out[SDEM_CNT_NEXTWALL] = next;
+  counters_out[SDEM_CNT_CNSV_CROSS] = (int)cross;
+  d.counters[2] += (unsigned long long)pp;
+  d.counters[3] += pw;
   d.counters[4] += 1ull;
   d.counters[0] = 0;
   d.counters[1] = 0;
@@ -1610,20 +1611,25 @@ __device__ void step_end_serial(const Dev& d, int* counters_out, const int* scal
   d.counters[9] = 0;
   *d.out_cnt = 0;
   *d.wl_cnt = 0;
-  if (mirror) {
-    int* slot = mirror + (*d.iter & 1) * nscal;
-    for (int k = 0; k < nscal; k++) slot[k] = scal[k];
-  }
 }
 
 // The end of a step in one block: the serial delete passes (thread 0), the
-// moves they imply (all threads), then the counters (thread 0).
+// moves they imply (all threads), the counters (thread 0), then a copy of the
+// device scalars (status, particle count, counters) into mapped host memory,
+// one word per thread, so that the host reads them after a stream
+// synchronisation without another copy.  Two mirror slots, by the parity of
+// the new iteration number: a step's copy survives while the next step runs.
 __global__ void k_finish(Dev d, int* counters_out, const int* scal, int* mirror, int nscal) {
   if (threadIdx.x == 0) delete_serial(d);
   __syncthreads();
   apply_moves(d, threadIdx.x, blockDim.x);
   __syncthreads();
-  if (threadIdx.x == 0) step_end_serial(d, counters_out, scal, mirror, nscal);
+  if (threadIdx.x == 0) step_end_serial(d, counters_out);
+  __syncthreads();
+  if (mirror && threadIdx.x < nscal) {
+    int* slot = mirror + (*d.iter & 1) * nscal;
+    slot[threadIdx.x] = scal[threadIdx.x];
+  }
 }
 
 // ---------------------------------------------------------------------------
