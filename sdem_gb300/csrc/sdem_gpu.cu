@@ -12,7 +12,9 @@
 //   k_bin, scan, k_scatter, k_cellorder
 //                                      NBSM_clcBoxIndex + Y/X/Z lists (Prtcl_NBS_Munjiza.f90:163-296)
 //                                      as a counting sort; within a cell particles are ordered by
-//                                      decreasing index, the order the reference's Z lists walk
+//                                      decreasing index, the order the reference's Z lists walk; the
+//                                      binning also makes the single-precision prefilter copy and
+//                                      each particle's cell coordinates
 //   k_search                           LoopNBSMask + FineSearch2/3 (:302-473, :503-557): one thread per
 //                                      target particle, same 13-cell half shell + same-cell tail, same
 //                                      exact FP64 overlap test; contacts go to the target's row (in visit
@@ -24,14 +26,16 @@
 //                                      (Prtcl_CL_and_CF.f90:142-198, 256-296, 732-798): one thread per
 //                                      contact, full warps of FP64 work
 //   k_wall_force                       ContactForce_PW (:832-856), one thread per wall contact
-//   k_degree_scatter                   particles grouped by contact count (the gather order)
+//   k_degree_scatter                   particles grouped by contact count (the gather order), one
+//                                      record per gather position with what the gather reads first
 //
 // Search, row offsets, row fill and forces run in chunks of target sort
 // positions on two streams, so that the search of one chunk (integer and
 // memory work) overlaps the force kernel of the one before (FP64 work).
 //   k_gather                           per particle, sums its contact records in the reference's scatter
-//                                      order (a deterministic gather), then its wall contacts in
-//                                      near-list order
+//                                      order (a deterministic gather; records signed for the row's
+//                                      target, moments scaled by the particle's own radius), then its
+//                                      wall contacts in near-list order
 //   k_integrate                        clc_Acceleration (Prtcl_DEMSystem.f90:166-181), Prtcl_Integrate
 //                                      (Prtcl_Integration.f90:15-88) and the periodic wrap, in index
 //                                      order
