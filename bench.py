@@ -423,6 +423,86 @@ def sandboxes_arm(args):
         m.close()
 
 
+def surrogate_arm(args):
+    """The learned surrogate (its own line; not the headline): a network
+    trained on plain-DEM trajectories of `--train-beds` sandboxes (2,000-4,000
+    spheres, parameters from seed 5, 15,000 settling steps, then 12 frames a
+    stride of 100 steps apart) for `--train-iters` Adam steps, then on the 1M
+    Hertz bed: K surrogate strides (graph build, features, forward, stride
+    update) against K x 100 plain DEM steps, and a run of the runner with the
+    plain-DEM judge every `--judge-every` strides (bound: 2% relative bed
+    height).  Simulated seconds per wall second, host clock around
+    synchronised runs."""
+    import torch
+    from sdem_gb300 import beds, surrogate as sg
+    from sdem_gb300.capi import DEMSystem
+    torch.cuda.set_device(0)
+    S, vscale = 100, 0.05
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(5)
+    sets = []
+    for k in range(args.train_beds + 1):
+        case = beds.sandbox_case(rng, k, n_lo=2000, n_hi=4000)
+        s = DEMSystem(case)
+        sets.append([sg.to_device(x, case, 1.2e-3, vscale) for x in sg.record_samples(s, case, S, 12, settle=15000)])
+        s.close()
+    train, held = [x for ss in sets[:-1] for x in ss], sets[-1]
+    t_data = time.perf_counter() - t0
+    net = sg.Network(seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = [float(net.train_step(train[i % len(train)].graph, train[i % len(train)].xn,
+                                   train[i % len(train)].target, lr=2e-3)) for i in range(args.train_iters)]
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    mse, mse_free = sg.evaluate(net, held)
+
+    case = make_case(args.n, 2)
+    dem = DEMSystem(case)
+    dem.step(args.warmup)
+    dmax = 2.0 * float(case.tables.radius.max())
+    runner = sg.SurrogateRunner(net, dem, case, S, dmax, vscale, judge_every=args.judge_every, bound=0.02,
+                                fallback_strides=args.judge_every)
+    K = max(1, args.strides)
+    runner._surrogate_stride(runner.posR, runner.vel, runner.omega)     # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        runner._surrogate_stride(runner.posR, runner.vel, runner.omega)
+    torch.cuda.synchronize()
+    t_sur = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dem.step(K * S)
+    dem.counters()
+    t_plain = time.perf_counter() - t0
+    h = S * case.opts.dt
+    t0 = time.perf_counter()
+    stats = runner.run(2 * args.judge_every)
+    torch.cuda.synchronize()
+    t_run = time.perf_counter() - t0
+    run_strides = stats["surrogate_strides"] + stats["dem_strides"] - 2
+    line = {"metric": "simulated s per wall s, surrogate vs plain DEM, 1M Hertz spheres",
+            "value": K * h / t_sur, "unit": "sim-s/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "bf16 (network), f64 (plain DEM and stride update)",
+            "data": "synthetic",
+            "plain_dem": K * h / t_plain, "ratio_vs_plain": t_plain / t_sur,
+            "ms_per_stride": {"surrogate": t_sur / K * 1e3, "plain_dem": t_plain / K * 1e3},
+            "with_judge": {"strides": 2 * args.judge_every, "sim_s_per_s": run_strides * h / t_run,
+                           "judged": stats["judged"], "fallbacks": stats["fallbacks"],
+                           "bed_height_rel_err": stats["errors"]},
+            "training": {"beds": args.train_beds, "samples": len(train), "iters": args.train_iters,
+                         "loss_first10": float(np.mean(losses[:10])), "loss_last10": float(np.mean(losses[-10:])),
+                         "heldout_mse": mse, "heldout_mse_free_flight": mse_free, "data_s": t_data,
+                         "train_s": t_train},
+            "config": {"workload": "surrogate_hertz_poly_1m", "particles": case.particles.n, "stride_steps": S,
+                       "dt": case.opts.dt,
+                       "latent": sg.LATENT, "layers": sg.LAYERS, "cutoff_dmax": sg.CUTOFF_FACTOR},
+            "note": "host wall clock around synchronised runs; the stride update integrates the predicted "
+                    "stride-mean accelerations (semi-implicit Euler over the stride)"}
+    print(json.dumps(line), flush=True)
+    dem.close()
+
+
 def props_cft_nlin():
     from sdem_gb300 import props
     return props.CFT_NLIN
@@ -438,14 +518,21 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=-1,
                     help="steps of the end-to-end run (default: --steps; 0 skips it)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="hertz_poly_1m", choices=["hertz_poly_1m", "sandboxes"],
-                    help="sandboxes: the batched workload (its own line; not the headline)")
+    ap.add_argument("--workload", default="hertz_poly_1m", choices=["hertz_poly_1m", "sandboxes", "surrogate"],
+                    help="sandboxes: the batched workload; surrogate: the learned surrogate against the plain "
+                         "DEM (each its own line; not the headline)")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--train-beds", type=int, default=3)
+    ap.add_argument("--train-iters", type=int, default=300)
+    ap.add_argument("--strides", type=int, default=10)
+    ap.add_argument("--judge-every", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.workload == "sandboxes":
         sandboxes_arm(args)
+    elif args.workload == "surrogate":
+        surrogate_arm(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:

@@ -1,9 +1,12 @@
-"""Build recipe of the native library libsdem_gpu.so (in-tree, sm_103a only).
+"""Build recipe of the native libraries (in-tree, sm_103a only).
 
     python -m sdem_gb300.build
 
-One translation unit, compiled with -fmad=false: the force law and the
-integrator must round exactly as the reference's Fortran (no FMA contraction).
+libsdem_gpu.so (the particle step, include/sdem_gpu.h) and
+libsdem_surrogate.so (the learned surrogate, include/sdem_surrogate.h), one
+translation unit each, compiled in parallel with -fmad=false: the force law
+and the integrator must round exactly as the reference's Fortran (no FMA
+contraction), and the surrogate's graph features as its numpy statement.
 """
 from __future__ import annotations
 
@@ -18,6 +21,9 @@ SRC = os.path.join(HERE, "csrc", "sdem_gpu.cu")
 DEPS = [SRC, os.path.join(HERE, "csrc", "dem_device.cuh"), os.path.join(HERE, "csrc", "fp64_int.cuh"),
         os.path.join(ROOT, "include", "sdem_gpu.h")]
 LIB = os.path.join(HERE, "libsdem_gpu.so")
+SG_SRC = os.path.join(HERE, "csrc", "surrogate.cu")
+SG_DEPS = [SG_SRC, os.path.join(ROOT, "include", "sdem_surrogate.h")]
+SG_LIB = os.path.join(HERE, "libsdem_surrogate.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
@@ -31,23 +37,34 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the sm_103a library cannot be built")
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+def up_to_date(lib: str = LIB, deps=None) -> bool:
+    deps = DEPS if deps is None else deps
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(p) <= t for p in DEPS)
+    t = os.path.getmtime(lib)
+    return all(os.path.getmtime(p) <= t for p in deps)
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles libsdem_gpu.so next to this file; returns its path."""
-    if not force and up_to_date():
-        return LIB
-    tmp = f"{LIB}.{os.getpid()}.tmp"
-    cmd = [nvcc(), *ARCH, *FLAGS, "-o", tmp, SRC, "-lcudart"]
-    if verbose:
-        print(" ".join(cmd), flush=True)
-    subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB)
+    """Compiles libsdem_gpu.so and libsdem_surrogate.so next to this file
+    (the stale ones, in parallel); returns the path of libsdem_gpu.so."""
+    jobs = []
+    for src, deps, lib in ((SRC, DEPS, LIB), (SG_SRC, SG_DEPS, SG_LIB)):
+        if not force and up_to_date(lib, deps):
+            continue
+        tmp = f"{lib}.{os.getpid()}.tmp"
+        cmd = [nvcc(), *ARCH, *FLAGS, "-o", tmp, src, "-lcudart"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        jobs.append((subprocess.Popen(cmd), cmd, tmp, lib))
+    failed = None
+    for proc, cmd, tmp, lib in jobs:
+        if proc.wait() != 0:
+            failed = failed or subprocess.CalledProcessError(proc.returncode, cmd)
+        else:
+            os.replace(tmp, lib)
+    if failed:
+        raise failed
     return LIB
 
 

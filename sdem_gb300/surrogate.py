@@ -1,0 +1,698 @@
+"""Learned surrogate of the particle step, driven through libsdem_surrogate.so
+(include/sdem_surrogate.h).
+
+A message-passing network over the neighbour graph of the cell search
+(radius 1.5 d_max) predicts each sphere's mean linear and angular
+acceleration over a stride of S DEM steps:
+
+- node features (32): velocity frames v(t), v(t-S), v(t-2S), spin omega r,
+  diameter and the distances to the five planes of the box;
+- edge features (16): relative displacement, distance, overlap;
+- encoders: 2-layer MLPs to a latent width of 128 (nodes and edges);
+- 6 processor layers: edge MLP over [h_dst, h_src, e] -> message m, e += m;
+  node MLP over [h, sum of incoming m] -> h += u;
+- decoder: 2-layer MLP to 6 outputs, (a - g)/|g| and alpha r/|g|.
+
+Every layer runs on the tensor cores of the library's GEMM (bf16 operands,
+fp32 accumulation, fused bias/ReLU/residual epilogues), forward and
+backward; the aggregation and its adjoints, the loss, Adam and the stride
+update are the library's kernels too.  PyTorch holds the device memory and
+provides the sorts and prefix sums of the graph build.  The product path has
+no CPU fallback: loading fails loudly when the library is missing.
+
+SurrogateRunner advances a bed by surrogate strides and, every `judge_every`
+strides, re-advances one stride with the plain FP64 DEM (include/sdem_gpu.h)
+from the surrogate's state as the error judge; when the relative bed-height
+difference exceeds the bound the plain DEM takes over for the next strides.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsdem_surrogate.so")
+
+LATENT = 128
+LAYERS = 6
+NODE_IN = 32
+EDGE_IN = 16
+OUT = 16          # decoder rows (6 used, the rest stay zero)
+OUT_USED = 6
+CUTOFF_FACTOR = 1.5
+DCLIP = 10.0
+OVERLAP_GAIN = 100.0
+
+EXPORTED = ("sdem_sg_cells", "sdem_sg_edge_count", "sdem_sg_edge_fill", "sdem_sg_node_features", "sdem_sg_gemm",
+            "sdem_sg_segsum", "sdem_sg_gather_add", "sdem_sg_colsum_blocks", "sdem_sg_colsum", "sdem_sg_mse",
+            "sdem_sg_adam", "sdem_sg_to_bf16", "sdem_sg_advance")
+
+
+class SgGrid(C.Structure):
+    _fields_ = [("lo", C.c_double * 3), ("cell", C.c_double), ("cutoff", C.c_double), ("scale", C.c_double),
+                ("dim", C.c_int * 3), ("pad_", C.c_int)]
+
+
+class SgOperand(C.Structure):
+    _fields_ = [("ptr", C.c_void_p * 3), ("idx", C.c_void_p * 3), ("ld", C.c_int * 3), ("width", C.c_int * 3),
+                ("nseg", C.c_int), ("trans", C.c_int)]
+
+
+class SgEpilogue(C.Structure):
+    _fields_ = [("bias", C.c_void_p), ("relu", C.c_int), ("accumulate", C.c_int),
+                ("mask", C.c_void_p), ("ld_mask", C.c_int),
+                ("out", C.c_void_p), ("ld_out", C.c_int),
+                ("out_bf", C.c_void_p), ("ld_out_bf", C.c_int),
+                ("resid", C.c_void_p), ("ld_resid", C.c_int),
+                ("res_out", C.c_void_p), ("ld_res_out", C.c_int),
+                ("res_out_bf", C.c_void_p), ("ld_res_out_bf", C.c_int)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads libsdem_surrogate.so (no fallback: a missing library raises)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m sdem_gb300.build` (sm_103a only)")
+    lib = C.CDLL(path)
+    P, I, D, LL, F = C.c_void_p, C.c_int, C.c_double, C.c_longlong, C.c_float
+    sig = {
+        "sdem_sg_cells": [I, P, C.POINTER(SgGrid), P, P],
+        "sdem_sg_edge_count": [I, P, C.POINTER(SgGrid), P, P, P, P, P],
+        "sdem_sg_edge_fill": [I, P, C.POINTER(SgGrid), P, P, P, P, P, P, P, P],
+        "sdem_sg_node_features": [I, P, P, P, I, P, D, D, D, P, P],
+        "sdem_sg_gemm": [I, I, I, C.POINTER(SgOperand), C.POINTER(SgOperand), C.POINTER(SgEpilogue), I, P, P],
+        "sdem_sg_segsum": [I, I, P, P, P, I, P, I, I, P, I, P],
+        "sdem_sg_gather_add": [I, I, P, P, I, P, I, P, I, P, I, P],
+        "sdem_sg_colsum_blocks": [],
+        "sdem_sg_colsum": [I, I, P, I, P, I, P, P],
+        "sdem_sg_mse": [I, I, P, I, P, P, P, P, P],
+        "sdem_sg_adam": [LL, P, P, P, P, P, F, F, F, F, F, I, P],
+        "sdem_sg_to_bf16": [LL, P, P, P],
+        "sdem_sg_advance": [I, P, I, D, D, D, D, D, P, P, P, P],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _check(rc: int, what: str) -> None:
+    if rc:
+        raise RuntimeError(f"{what} failed (code {rc})")
+
+
+def _ptr(t: Optional[torch.Tensor], offset: int = 0) -> Optional[int]:
+    if t is None:
+        return None
+    return t.data_ptr() + offset * t.element_size()
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+# ----------------------------------------------------------- parameters
+
+def param_layout(latent: int = LATENT, layers: int = LAYERS) -> List[Tuple[str, Tuple[int, ...], int]]:
+    """(name, shape, offset) of every tensor in the flat parameter vector;
+    weights are (out, in) row-major, offsets multiples of 8 elements."""
+    entries: List[Tuple[str, Tuple[int, ...]]] = []
+
+    def mlp(prefix: str, kin: int, kout: int) -> None:
+        entries.extend([(f"{prefix}.w1", (latent, kin)), (f"{prefix}.b1", (latent,)),
+                        (f"{prefix}.w2", (kout, latent)), (f"{prefix}.b2", (kout,))])
+
+    mlp("enc_n", NODE_IN, latent)
+    mlp("enc_e", EDGE_IN, latent)
+    for l in range(layers):
+        mlp(f"edge{l}", 3 * latent, latent)
+        mlp(f"node{l}", 2 * latent, latent)
+    mlp("dec", latent, OUT)
+    out, off = [], 0
+    for name, shape in entries:
+        out.append((name, shape, off))
+        off += (int(np.prod(shape)) + 7) // 8 * 8
+    return out
+
+
+def param_count(latent: int = LATENT, layers: int = LAYERS) -> int:
+    name, shape, off = param_layout(latent, layers)[-1]
+    return off + (int(np.prod(shape)) + 7) // 8 * 8
+
+
+def init_params(seed: int, latent: int = LATENT, layers: int = LAYERS) -> np.ndarray:
+    """He-uniform first layers, 0.1-scaled second layers of the residual
+    MLPs, zero biases, zero unused decoder rows (float32)."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(param_count(latent, layers), np.float32)
+    for name, shape, off in param_layout(latent, layers):
+        if name.endswith(".b1") or name.endswith(".b2"):
+            continue
+        kin = shape[1]
+        bound = math.sqrt(6.0 / kin)
+        if name.endswith(".w2") and (name.startswith("edge") or name.startswith("node") or name.startswith("dec")):
+            bound *= 0.1
+        w = rng.uniform(-bound, bound, size=shape).astype(np.float32)
+        if name == "dec.w2":
+            w[OUT_USED:] = 0.0
+        p[off:off + w.size] = w.reshape(-1)
+    return p
+
+
+def bf16_round(x: np.ndarray) -> np.ndarray:
+    """float32 -> nearest bfloat16 (ties to even), returned as float32."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+# ---------------------------------------------------------------- graph
+
+@dataclass
+class Graph:
+    n: int
+    E: int
+    row_off: torch.Tensor      # int32 (n+1): CSR by receiver
+    dst: torch.Tensor          # int32 (E)
+    src: torch.Tensor          # int32 (E)
+    efeat: torch.Tensor        # bf16 (E, 16)
+    src_perm: torch.Tensor     # int32 (E): edges ordered by sender
+    src_off: torch.Tensor      # int32 (n+1)
+
+
+def make_grid(lo, hi, d_max: float) -> SgGrid:
+    """Cells of edge 1.5 d_max covering [lo, hi] with one cell of margin."""
+    cut = CUTOFF_FACTOR * d_max
+    g = SgGrid()
+    dims = []
+    for a in range(3):
+        g.lo[a] = float(lo[a]) - cut
+        dims.append(max(1, int(math.floor((float(hi[a]) - float(lo[a]) + 2 * cut) / cut)) + 1))
+    g.cell = cut
+    g.cutoff = cut
+    g.scale = float(d_max)
+    for a in range(3):
+        g.dim[a] = dims[a]
+    return g
+
+
+def build_graph(posR: torch.Tensor, grid: SgGrid) -> Graph:
+    """Neighbour graph of the spheres in posR (cuda float64, n x 4)."""
+    lib = load()
+    n = posR.shape[0]
+    dev = posR.device
+    s = _stream()
+    ncell = grid.dim[0] * grid.dim[1] * grid.dim[2]
+    cell = torch.empty(n, dtype=torch.int32, device=dev)
+    _check(lib.sdem_sg_cells(n, _ptr(posR), C.byref(grid), _ptr(cell), s), "sdem_sg_cells")
+    key = cell.to(torch.int64) * max(n, 1) + torch.arange(n, device=dev, dtype=torch.int64)
+    sorted_idx = torch.argsort(key).to(torch.int32)
+    counts = torch.bincount(cell.to(torch.int64), minlength=ncell)
+    cell_start = torch.zeros(ncell + 1, dtype=torch.int32, device=dev)
+    cell_start[1:] = torch.cumsum(counts, 0).to(torch.int32)
+    degree = torch.empty(n, dtype=torch.int32, device=dev)
+    _check(lib.sdem_sg_edge_count(n, _ptr(posR), C.byref(grid), _ptr(cell), _ptr(cell_start), _ptr(sorted_idx),
+                                  _ptr(degree), s), "sdem_sg_edge_count")
+    row_off = torch.zeros(n + 1, dtype=torch.int32, device=dev)
+    row_off[1:] = torch.cumsum(degree.to(torch.int64), 0).to(torch.int32)
+    E = int(row_off[-1].item())
+    dst = torch.empty(E, dtype=torch.int32, device=dev)
+    src = torch.empty(E, dtype=torch.int32, device=dev)
+    efeat = torch.empty((max(E, 1), EDGE_IN), dtype=torch.bfloat16, device=dev)
+    _check(lib.sdem_sg_edge_fill(n, _ptr(posR), C.byref(grid), _ptr(cell), _ptr(cell_start), _ptr(sorted_idx),
+                                 _ptr(row_off), _ptr(dst), _ptr(src), _ptr(efeat), s), "sdem_sg_edge_fill")
+    skey = src.to(torch.int64) * max(E, 1) + torch.arange(E, device=dev, dtype=torch.int64)
+    src_perm = torch.argsort(skey).to(torch.int32)
+    src_off = torch.zeros(n + 1, dtype=torch.int32, device=dev)
+    src_off[1:] = torch.cumsum(torch.bincount(src.to(torch.int64), minlength=n), 0).to(torch.int32)
+    return Graph(n, E, row_off, dst, src, efeat[:E], src_perm, src_off)
+
+
+def node_features(posR: torch.Tensor, vel: torch.Tensor, omega: torch.Tensor, planes: torch.Tensor, d_max: float,
+                  vscale: float) -> torch.Tensor:
+    """bf16 (n, 32) node features; vel (3, n, 3) frames, planes (nw, 4)."""
+    lib = load()
+    n = posR.shape[0]
+    out = torch.empty((max(n, 1), NODE_IN), dtype=torch.bfloat16, device=posR.device)
+    _check(lib.sdem_sg_node_features(n, _ptr(posR), _ptr(vel), _ptr(omega), int(planes.shape[0]), _ptr(planes),
+                                     float(d_max), float(vscale), DCLIP, _ptr(out), _stream()),
+           "sdem_sg_node_features")
+    return out[:n]
+
+
+def planes_of(walls) -> np.ndarray:
+    """(nw, 4) plane normals and offsets (n.x + d) of a WallSet."""
+    return np.array([[w[12], w[13], w[14], w[15]] for w in walls.walls], dtype=np.float64).reshape(-1, 4)
+
+
+# --------------------------------------------------------------- network
+
+class _Op:
+    """Builder of an sdem_sg_operand: segments (tensor, element offset, ld,
+    width, gather index)."""
+
+    def __init__(self, trans: int, *segs):
+        self.o = SgOperand()
+        self.o.trans = trans
+        self.o.nseg = len(segs)
+        self.keep = segs
+        for k, (t, off, ld, width, idx) in enumerate(segs):
+            self.o.ptr[k] = _ptr(t, off)
+            self.o.idx[k] = _ptr(idx) if idx is not None else None
+            self.o.ld[k] = ld
+            self.o.width[k] = width
+
+
+def _ep(**kw) -> SgEpilogue:
+    e = SgEpilogue()
+    for k, v in kw.items():
+        if isinstance(v, torch.Tensor):
+            v = _ptr(v)
+        setattr(e, k, v)
+    return e
+
+
+class Network:
+    """Parameters (fp32 master + bf16 copy), forward, backward and Adam of
+    the surrogate network on one CUDA device."""
+
+    def __init__(self, seed: int = 0, device: str = "cuda", latent: int = LATENT, layers: int = LAYERS,
+                 params: Optional[np.ndarray] = None):
+        self.lib = load()
+        self.latent, self.layers = latent, layers
+        self.layout = {name: (shape, off) for name, shape, off in param_layout(latent, layers)}
+        host = init_params(seed, latent, layers) if params is None else np.asarray(params, np.float32)
+        self.p = torch.from_numpy(host.copy()).to(device)
+        self.pb = torch.empty(self.p.numel(), dtype=torch.bfloat16, device=device)
+        self.grad = torch.zeros_like(self.p)
+        self.m = torch.zeros_like(self.p)
+        self.v = torch.zeros_like(self.p)
+        self.step_count = 0
+        self.device = device
+        self.colsum_partial = torch.empty(self.lib.sdem_sg_colsum_blocks() * 4 * latent, dtype=torch.float32,
+                                          device=device)
+        self.refresh_bf16()
+        self.saved = None
+
+    def refresh_bf16(self) -> None:
+        _check(self.lib.sdem_sg_to_bf16(self.p.numel(), _ptr(self.p), _ptr(self.pb), _stream()), "sdem_sg_to_bf16")
+
+    def host_params(self) -> np.ndarray:
+        return self.p.cpu().numpy()
+
+    def off(self, name: str) -> int:
+        return self.layout[name][1]
+
+    def shape(self, name: str):
+        return self.layout[name][0]
+
+    # -- GEMM helpers
+    def _gemm(self, I, J, R, a: _Op, b: _Op, ep: SgEpilogue, splits: int = 1, partial=None) -> None:
+        _check(self.lib.sdem_sg_gemm(I, J, R, C.byref(a.o), C.byref(b.o), C.byref(ep), splits, _ptr(partial),
+                                     _stream()), "sdem_sg_gemm")
+
+    def _w(self, name: str, trans: int) -> _Op:
+        kout, kin = self.shape(name)
+        return _Op(trans, (self.pb, self.off(name), kin, kin, None))
+
+    def _linear(self, M, a: _Op, name: str, **ep) -> None:
+        """act(A W^T + b): A is M x kin (trans 0 segments)."""
+        kout, kin = self.shape(name)
+        bias = name[:-2] + "b" + name[-1]
+        self._gemm(M, kout, kin, a, self._w(name, 0), _ep(bias=_ptr(self.p, self.off(bias)), **ep))
+
+    def _wgrad(self, name: str, R: int, dy: _Op, x: _Op) -> None:
+        """grad[name] += dY^T X over R rows (dy, x: trans 1 operands)."""
+        kout, kin = self.shape(name)
+        gx, gy = (kout + 63) // 64, (kin + 63) // 64
+        splits = max(1, min(R // 256, 608 // (gx * gy)))
+        partial = torch.empty(splits * kout * kin, dtype=torch.float32, device=self.device) if splits > 1 else None
+        self._gemm(kout, kin, R, dy, x, _ep(out=_ptr(self.grad, self.off(name)), ld_out=kin, accumulate=1),
+                   splits, partial)
+
+    def _dgrad(self, M, dy: _Op, name: str, **ep) -> None:
+        """dX = dY W (M x kin)."""
+        kout, kin = self.shape(name)
+        self._gemm(M, kin, kout, dy, self._w(name, 1), _ep(**ep))
+
+    def _bgrad(self, name: str, M: int, x: torch.Tensor, ldx: int) -> None:
+        kout = self.shape(name)[0]
+        _check(self.lib.sdem_sg_colsum(M, kout, _ptr(x), ldx, _ptr(self.grad, self.off(name)), 1,
+                                       _ptr(self.colsum_partial), _stream()), "sdem_sg_colsum")
+
+    # -- forward
+    def forward(self, g: Graph, xn: torch.Tensor, keep: bool = True) -> torch.Tensor:
+        """(n, 16) fp32 predictions; keep=True saves what backward needs."""
+        L, n, E, dev = self.latent, g.n, g.E, self.device
+        bf, f32 = torch.bfloat16, torch.float32
+        zb = torch.empty((n, L), dtype=bf, device=dev)
+        self._linear(n, _Op(0, (xn, 0, NODE_IN, NODE_IN, None)), "enc_n.w1", relu=1, out_bf=zb, ld_out_bf=L)
+        h = torch.empty((n, L), dtype=f32, device=dev)
+        hb = torch.empty((n, L), dtype=bf, device=dev)
+        self._linear(n, _Op(0, (zb, 0, L, L, None)), "enc_n.w2", out=h, ld_out=L, out_bf=hb, ld_out_bf=L)
+        zeb = torch.empty((max(E, 1), L), dtype=bf, device=dev)
+        self._linear(E, _Op(0, (g.efeat, 0, EDGE_IN, EDGE_IN, None)), "enc_e.w1", relu=1, out_bf=zeb, ld_out_bf=L)
+        e = torch.empty((max(E, 1), L), dtype=f32, device=dev)
+        eb = torch.empty((max(E, 1), L), dtype=bf, device=dev)
+        self._linear(E, _Op(0, (zeb, 0, L, L, None)), "enc_e.w2", out=e, ld_out=L, out_bf=eb, ld_out_bf=L)
+        saved = {"xn": xn, "zb_enc": zb, "zeb_enc": zeb, "hb": [hb], "eb": [eb], "ze": [], "zn": [], "agg": []}
+        m = torch.empty((max(E, 1), L), dtype=f32, device=dev)
+        for l in range(self.layers):
+            ze = torch.empty((max(E, 1), L), dtype=bf, device=dev)
+            a_in = _Op(0, (hb, 0, L, L, g.dst), (hb, 0, L, L, g.src), (eb, 0, L, L, None))
+            self._linear(E, a_in, f"edge{l}.w1", relu=1, out_bf=ze, ld_out_bf=L)
+            e2 = torch.empty_like(e)
+            eb2 = torch.empty_like(eb)
+            self._linear(E, _Op(0, (ze, 0, L, L, None)), f"edge{l}.w2", out=m, ld_out=L, resid=e, ld_resid=L,
+                         res_out=e2, ld_res_out=L, res_out_bf=eb2, ld_res_out_bf=L)
+            aggb = torch.empty((n, L), dtype=bf, device=dev)
+            _check(self.lib.sdem_sg_segsum(n, L, _ptr(g.row_off), None, _ptr(m), L, None, L, 0, _ptr(aggb), L,
+                                           _stream()), "sdem_sg_segsum")
+            zn = torch.empty((n, L), dtype=bf, device=dev)
+            self._linear(n, _Op(0, (hb, 0, L, L, None), (aggb, 0, L, L, None)), f"node{l}.w1", relu=1, out_bf=zn,
+                         ld_out_bf=L)
+            h2 = torch.empty_like(h)
+            hb2 = torch.empty_like(hb)
+            self._linear(n, _Op(0, (zn, 0, L, L, None)), f"node{l}.w2", resid=h, ld_resid=L, res_out=h2,
+                         ld_res_out=L, res_out_bf=hb2, ld_res_out_bf=L)
+            if keep:
+                saved["ze"].append(ze)
+                saved["zn"].append(zn)
+                saved["agg"].append(aggb)
+                saved["hb"].append(hb2)
+                saved["eb"].append(eb2)
+            h, hb, e, eb = h2, hb2, e2, eb2
+        zd = torch.empty((n, L), dtype=bf, device=dev)
+        self._linear(n, _Op(0, (hb, 0, L, L, None)), "dec.w1", relu=1, out_bf=zd, ld_out_bf=L)
+        y = torch.empty((n, OUT), dtype=f32, device=dev)
+        self._linear(n, _Op(0, (zd, 0, L, L, None)), "dec.w2", out=y, ld_out=OUT)
+        saved["zd"] = zd
+        self.saved = saved if keep else None
+        self.graph = g if keep else None
+        return y
+
+    def loss(self, y: torch.Tensor, target: torch.Tensor):
+        """(mse, dy fp32, dy bf16) of predictions against (n, 6) targets."""
+        n = y.shape[0]
+        rowerr = torch.empty(n, dtype=torch.float32, device=self.device)
+        dy = torch.empty((n, OUT), dtype=torch.float32, device=self.device)
+        dyb = torch.empty((n, OUT), dtype=torch.bfloat16, device=self.device)
+        _check(self.lib.sdem_sg_mse(n, OUT_USED, _ptr(y), OUT, _ptr(target), _ptr(rowerr), _ptr(dy), _ptr(dyb),
+                                    _stream()), "sdem_sg_mse")
+        return rowerr.sum() / (n * OUT_USED), dy, dyb
+
+    # -- backward
+    def backward(self, dy: torch.Tensor, dyb: torch.Tensor) -> None:
+        """Accumulates d loss / d params into self.grad (zero it first)."""
+        s, g = self.saved, self.graph
+        if s is None:
+            raise RuntimeError("backward needs a forward with keep=True")
+        L, n, E, dev = self.latent, g.n, g.E, self.device
+        bf, f32 = torch.bfloat16, torch.float32
+        lib = self.lib
+        # decoder
+        self._wgrad("dec.w2", n, _Op(1, (dyb, 0, OUT, OUT, None)), _Op(1, (s["zd"], 0, L, L, None)))
+        self._bgrad("dec.b2", n, dy, OUT)
+        dz = torch.empty((n, L), dtype=f32, device=dev)
+        dzb = torch.empty((n, L), dtype=bf, device=dev)
+        self._dgrad(n, _Op(0, (dyb, 0, OUT, OUT, None)), "dec.w2", mask=s["zd"], ld_mask=L, out=dz, ld_out=L,
+                    out_bf=dzb, ld_out_bf=L)
+        hb6 = s["hb"][-1]
+        self._wgrad("dec.w1", n, _Op(1, (dzb, 0, L, L, None)), _Op(1, (hb6, 0, L, L, None)))
+        self._bgrad("dec.b1", n, dz, L)
+        dh = torch.empty((n, L), dtype=f32, device=dev)
+        dhb = torch.empty((n, L), dtype=bf, device=dev)
+        self._dgrad(n, _Op(0, (dzb, 0, L, L, None)), "dec.w1", out=dh, ld_out=L, out_bf=dhb, ld_out_bf=L)
+        de = torch.zeros((max(E, 1), L), dtype=f32, device=dev)
+        din_n = torch.empty((n, 2 * L), dtype=f32, device=dev)
+        din_e = torch.empty((max(E, 1), 3 * L), dtype=f32, device=dev)
+        dm = torch.empty((max(E, 1), L), dtype=f32, device=dev)
+        dmb = torch.empty((max(E, 1), L), dtype=bf, device=dev)
+        dze = torch.empty((max(E, 1), L), dtype=f32, device=dev)
+        dzeb = torch.empty((max(E, 1), L), dtype=bf, device=dev)
+        for l in reversed(range(self.layers)):
+            hb_prev, eb_prev = s["hb"][l], s["eb"][l]
+            zn, ze, aggb = s["zn"][l], s["ze"][l], s["agg"][l]
+            # node MLP: h_l = h_{l-1} + W2 relu(W1 [h, agg] + b1) + b2
+            self._wgrad(f"node{l}.w2", n, _Op(1, (dhb, 0, L, L, None)), _Op(1, (zn, 0, L, L, None)))
+            self._bgrad(f"node{l}.b2", n, dh, L)
+            self._dgrad(n, _Op(0, (dhb, 0, L, L, None)), f"node{l}.w2", mask=zn, ld_mask=L, out=dz, ld_out=L,
+                        out_bf=dzb, ld_out_bf=L)
+            self._wgrad(f"node{l}.w1", n, _Op(1, (dzb, 0, L, L, None)),
+                        _Op(1, (hb_prev, 0, L, L, None), (aggb, 0, L, L, None)))
+            self._bgrad(f"node{l}.b1", n, dz, L)
+            self._dgrad(n, _Op(0, (dzb, 0, L, L, None)), f"node{l}.w1", out=din_n, ld_out=2 * L)
+            dh_prev = torch.empty_like(dh)
+            _check(lib.sdem_sg_gather_add(n, L, None, _ptr(din_n), 2 * L, _ptr(dh), L, _ptr(dh_prev), L, None, L,
+                                          _stream()), "sdem_sg_gather_add")
+            # messages: dm = de_l + dagg[dst]
+            _check(lib.sdem_sg_gather_add(E, L, _ptr(g.dst), _ptr(din_n, L), 2 * L, _ptr(de), L, _ptr(dm), L,
+                                          _ptr(dmb), L, _stream()), "sdem_sg_gather_add")
+            # edge MLP: m = W2 relu(W1 [h_dst, h_src, e] + b1) + b2
+            self._wgrad(f"edge{l}.w2", E, _Op(1, (dmb, 0, L, L, None)), _Op(1, (ze, 0, L, L, None)))
+            self._bgrad(f"edge{l}.b2", E, dm, L)
+            self._dgrad(E, _Op(0, (dmb, 0, L, L, None)), f"edge{l}.w2", mask=ze, ld_mask=L, out=dze, ld_out=L,
+                        out_bf=dzeb, ld_out_bf=L)
+            self._wgrad(f"edge{l}.w1", E, _Op(1, (dzeb, 0, L, L, None)),
+                        _Op(1, (hb_prev, 0, L, L, g.dst), (hb_prev, 0, L, L, g.src), (eb_prev, 0, L, L, None)))
+            self._bgrad(f"edge{l}.b1", E, dze, L)
+            self._dgrad(E, _Op(0, (dzeb, 0, L, L, None)), f"edge{l}.w1", out=din_e, ld_out=3 * L)
+            de_prev = torch.empty_like(de)
+            _check(lib.sdem_sg_gather_add(E, L, None, _ptr(din_e, 2 * L), 3 * L, _ptr(de), L, _ptr(de_prev), L, None,
+                                          L, _stream()), "sdem_sg_gather_add")
+            _check(lib.sdem_sg_segsum(n, L, _ptr(g.row_off), None, _ptr(din_e), 3 * L, _ptr(dh_prev), L, 1, None, L,
+                                      _stream()), "sdem_sg_segsum")
+            _check(lib.sdem_sg_segsum(n, L, _ptr(g.src_off), _ptr(g.src_perm), _ptr(din_e, L), 3 * L, _ptr(dh_prev),
+                                      L, 1, _ptr(dhb), L, _stream()), "sdem_sg_segsum")
+            dh, de = dh_prev, de_prev
+        # encoders
+        self._wgrad("enc_n.w2", n, _Op(1, (dhb, 0, L, L, None)), _Op(1, (s["zb_enc"], 0, L, L, None)))
+        self._bgrad("enc_n.b2", n, dh, L)
+        self._dgrad(n, _Op(0, (dhb, 0, L, L, None)), "enc_n.w2", mask=s["zb_enc"], ld_mask=L, out=dz, ld_out=L,
+                    out_bf=dzb, ld_out_bf=L)
+        self._wgrad("enc_n.w1", n, _Op(1, (dzb, 0, L, L, None)), _Op(1, (s["xn"], 0, NODE_IN, NODE_IN, None)))
+        self._bgrad("enc_n.b1", n, dz, L)
+        deb = torch.empty((max(E, 1), L), dtype=bf, device=dev)
+        _check(lib.sdem_sg_to_bf16(E * L, _ptr(de), _ptr(deb), _stream()), "sdem_sg_to_bf16")
+        self._wgrad("enc_e.w2", E, _Op(1, (deb, 0, L, L, None)), _Op(1, (s["zeb_enc"], 0, L, L, None)))
+        self._bgrad("enc_e.b2", E, de, L)
+        self._dgrad(E, _Op(0, (deb, 0, L, L, None)), "enc_e.w2", mask=s["zeb_enc"], ld_mask=L, out=dze, ld_out=L,
+                    out_bf=dzeb, ld_out_bf=L)
+        self._wgrad("enc_e.w1", E, _Op(1, (dzeb, 0, L, L, None)), _Op(1, (g.efeat, 0, EDGE_IN, EDGE_IN, None)))
+        self._bgrad("enc_e.b1", E, dze, L)
+
+    def adam(self, lr: float = 1e-3, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
+             weight_decay: float = 0.0) -> None:
+        self.step_count += 1
+        _check(self.lib.sdem_sg_adam(self.p.numel(), _ptr(self.p), _ptr(self.grad), _ptr(self.m), _ptr(self.v),
+                                     _ptr(self.pb), lr, beta1, beta2, eps, weight_decay, self.step_count, _stream()),
+               "sdem_sg_adam")
+
+    def train_step(self, g: Graph, xn: torch.Tensor, target: torch.Tensor, lr: float = 1e-3) -> torch.Tensor:
+        self.grad.zero_()
+        y = self.forward(g, xn, keep=True)
+        loss, dy, dyb = self.loss(y, target)
+        self.backward(dy, dyb)
+        self.adam(lr)
+        self.saved = None
+        return loss
+
+
+# --------------------------------------------------------------- samples
+
+@dataclass
+class Sample:
+    """One training frame: state at t, the two earlier velocity frames and
+    the stride-mean accelerations over (t, t + S) as targets."""
+    posR: np.ndarray      # (n, 4)
+    vel: np.ndarray       # (3, n, 3): v(t), v(t-S), v(t-2S)
+    omega: np.ndarray     # (n, 3)
+    target: np.ndarray    # (n, 6) float32
+
+
+def targets(v0, v1, w0, w1, r, h: float, gravity) -> np.ndarray:
+    """((v1 - v0)/h - g)/|g| and ((w1 - w0)/h) r/|g|, float32 (n, 6)."""
+    gm = float(np.linalg.norm(gravity))
+    a = ((v1 - v0) / h - np.asarray(gravity)[None, :]) / gm
+    al = (w1 - w0) / h * r[:, None] / gm
+    return np.concatenate([a, al], axis=1).astype(np.float32)
+
+
+def record_samples(system, case, stride: int, frames: int, settle: int = 0) -> List[Sample]:
+    """Runs the plain DEM (a DEMSystem of `case`) and turns consecutive
+    stride frames into samples (frames - 3 of them)."""
+    if settle:
+        system.step(settle)
+    snaps = []
+    for k in range(frames):
+        if k:
+            system.step(stride)
+        st = system.state()
+        snaps.append((st.posR.copy(), st.linVel[:, 0, :].copy(), st.rotVel[:, 0, :].copy(), st.id.copy()))
+    h = stride * case.opts.dt
+    out = []
+    for k in range(2, frames - 1):
+        ids = snaps[k][3]
+        if not all(np.array_equal(ids, snaps[j][3]) for j in (k - 2, k - 1, k + 1)):
+            continue  # a sphere left the domain in between: the frames do not line up
+        posR, v, w = snaps[k][0], snaps[k][1], snaps[k][2]
+        vel = np.stack([v, snaps[k - 1][1], snaps[k - 2][1]])
+        tgt = targets(v, snaps[k + 1][1], w, snaps[k + 1][2], posR[:, 3], h, case.opts.gravity)
+        out.append(Sample(posR, vel, w, tgt))
+    return out
+
+
+@dataclass
+class DeviceSample:
+    graph: Graph
+    xn: torch.Tensor
+    target: torch.Tensor
+
+
+def to_device(sample: Sample, case, d_max: float, vscale: float, device: str = "cuda") -> DeviceSample:
+    posR = torch.from_numpy(np.ascontiguousarray(sample.posR)).to(device)
+    vel = torch.from_numpy(np.ascontiguousarray(sample.vel)).to(device)
+    om = torch.from_numpy(np.ascontiguousarray(sample.omega)).to(device)
+    planes = torch.from_numpy(planes_of(case.walls)).to(device)
+    grid = make_grid(case.opts.minpoint, case.opts.maxpoint, d_max)
+    g = build_graph(posR, grid)
+    xn = node_features(posR, vel, om, planes, d_max, vscale)
+    return DeviceSample(g, xn, torch.from_numpy(sample.target).to(device))
+
+
+def evaluate(net: Network, samples: List[DeviceSample]) -> Tuple[float, float]:
+    """(network MSE, MSE of the prediction without the network: a = g,
+    alpha = 0, i.e. zero output) over the samples, node-weighted."""
+    num = den = base = 0.0
+    for s in samples:
+        y = net.forward(s.graph, s.xn, keep=False)
+        loss, _, _ = net.loss(y, s.target)
+        n = s.graph.n
+        num += float(loss) * n
+        base += float((s.target.double() ** 2).mean()) * n
+        den += n
+    return num / den, base / den
+
+
+# --------------------------------------------------------------- rollout
+
+class SurrogateRunner:
+    """Advances a bed by surrogate strides with a plain-DEM judge.
+
+    Every `judge_every` strides the plain DEM re-advances one stride from the
+    surrogate's state; the relative bed-height difference (mean sphere
+    height above the floor) between that stride and the surrogate's own
+    stride from the same state is the error.  Above `bound` the plain DEM
+    advances the next `fallback_strides` strides itself.  The run continues
+    from the plain DEM's state after every judged stride."""
+
+    def __init__(self, net: Network, system, case, stride: int, d_max: float, vscale: float,
+                 judge_every: int = 20, bound: float = 0.02, fallback_strides: int = 20):
+        self.net, self.sys, self.case = net, system, case
+        self.stride, self.d_max, self.vscale = stride, d_max, vscale
+        self.judge_every, self.bound, self.fallback = judge_every, bound, fallback_strides
+        self.h = stride * case.opts.dt
+        self.grid = make_grid(case.opts.minpoint, case.opts.maxpoint, d_max)
+        self.planes = torch.from_numpy(planes_of(case.walls)).to(net.device)
+        self.floor = float(case.opts.minpoint[1])
+        self.stats = {"surrogate_strides": 0, "dem_strides": 0, "judged": 0, "fallbacks": 0, "errors": []}
+        self._frames_from_dem(3)
+
+    def _pull(self):
+        st = self.sys.state()
+        return st
+
+    def _frames_from_dem(self, k: int) -> None:
+        """k plain strides; the last three velocity frames seed the state."""
+        vs = []
+        for i in range(k):
+            if i:
+                self.sys.step(self.stride)
+                self.stats["dem_strides"] += 1
+            st = self._pull()
+            vs.append(st.linVel[:, 0, :].copy())
+        self.parts = st
+        dev = self.net.device
+        self.posR = torch.from_numpy(np.ascontiguousarray(st.posR)).to(dev)
+        self.vel = torch.from_numpy(np.ascontiguousarray(np.stack([vs[-1], vs[-2], vs[-3]]))).to(dev)
+        self.omega = torch.from_numpy(np.ascontiguousarray(st.rotVel[:, 0, :])).to(dev)
+
+    def bed_height(self, posR: torch.Tensor) -> float:
+        return float((posR[:, 1] - self.floor).mean())
+
+    def _surrogate_stride(self, posR, vel, omega) -> None:
+        g = build_graph(posR, self.grid)
+        xn = node_features(posR, vel, omega, self.planes, self.d_max, self.vscale)
+        y = self.net.forward(g, xn, keep=False)
+        gx, gy, gz = self.case.opts.gravity
+        _check(self.net.lib.sdem_sg_advance(posR.shape[0], _ptr(y), OUT, float(np.linalg.norm(self.case.opts.gravity)),
+                                            gx, gy, gz, self.h, _ptr(posR), _ptr(vel), _ptr(omega), _stream()),
+               "sdem_sg_advance")
+
+    def _upload(self) -> None:
+        """The surrogate state into the plain DEM (contact history restarts)."""
+        p = self.parts.copy()
+        p.posR[:] = self.posR.cpu().numpy()
+        v = self.vel[0].cpu().numpy()
+        w = self.omega.cpu().numpy()
+        for k in range(p.linVel.shape[1]):
+            p.linVel[:, k, :] = v
+            p.linAcc[:, k, :] = np.asarray(self.case.opts.gravity)[None, :]
+        for k in range(p.rotVel.shape[1]):
+            p.rotVel[:, k, :] = w
+            p.rotAcc[:, k, :] = 0.0
+        self.sys.upload(p)
+
+    def run(self, strides: int) -> dict:
+        done = 0
+        pending_dem = 0
+        while done < strides:
+            if pending_dem:
+                self.sys.step(self.stride)
+                self.stats["dem_strides"] += 1
+                pending_dem -= 1
+                done += 1
+                if pending_dem == 0:
+                    self._frames_from_dem(3)
+                    done += 2
+                continue
+            if (self.stats["surrogate_strides"] + 1) % self.judge_every == 0:
+                self._upload()
+                p2, v2, w2 = self.posR.clone(), self.vel.clone(), self.omega.clone()
+                self._surrogate_stride(p2, v2, w2)
+                self.sys.step(self.stride)
+                self.stats["dem_strides"] += 1
+                self.stats["judged"] += 1
+                st = self._pull()
+                h_dem = float((st.posR[:, 1] - self.floor).mean())
+                err = abs(self.bed_height(p2) - h_dem) / max(abs(h_dem), 1e-300)
+                self.stats["errors"].append(err)
+                self.stats["surrogate_strides"] += 1
+                done += 1
+                if err > self.bound:
+                    self.stats["fallbacks"] += 1
+                    pending_dem = self.fallback
+                else:
+                    self.parts = st
+                    self.posR = torch.from_numpy(np.ascontiguousarray(st.posR)).to(self.net.device)
+                    self.vel = torch.stack([torch.from_numpy(st.linVel[:, 0, :].copy()).to(self.net.device),
+                                            self.vel[0], self.vel[1]])
+                    self.omega = torch.from_numpy(np.ascontiguousarray(st.rotVel[:, 0, :])).to(self.net.device)
+                continue
+            self._surrogate_stride(self.posR, self.vel, self.omega)
+            self.stats["surrogate_strides"] += 1
+            done += 1
+        return self.stats
