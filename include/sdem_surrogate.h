@@ -146,12 +146,20 @@ int sdem_sg_adam(long long n, float* p, const float* g, float* m, float* v, uint
 /* bf16(x) elementwise (round to nearest even). */
 int sdem_sg_to_bf16(long long n, const float* x, uint16_t* y, void* stream);
 
+/* Planes of the box that hold the spheres in a surrogate stride: x_a >= lo[a]
+ * + r and x_a <= hi[a] - r (use -/+1e300 for an open side). */
+typedef struct sdem_sg_box {
+    double lo[3];
+    double hi[3];
+} sdem_sg_box;
+
 /* One surrogate stride of length h: with a_k = ascale * pred[i][k] + g_k (k <
  * 3, g = (gx, gy, gz)) and alpha_k = ascale * pred[i][3+k] / r_i, v' = v(t) + a h,
- * x' = x + v' h, omega' = omega + alpha h; the velocity frames shift
- * (vel[2] <- vel[1] <- vel[0] <- v').  pred: n x ldp fp32. */
+ * x' = x + v' h, omega' = omega + alpha h; a sphere that would cross a plane of
+ * the box is put back against it and keeps no velocity into it; the velocity
+ * frames shift (vel[2] <- vel[1] <- vel[0] <- v').  pred: n x ldp fp32. */
 int sdem_sg_advance(int n, const float* pred, int ldp, double ascale, double gx, double gy, double gz, double h,
-                    double* posR, double* vel, double* omega, void* stream);
+                    const sdem_sg_box* box, double* posR, double* vel, double* omega, void* stream);
 
 #ifdef __cplusplus
 }

@@ -385,7 +385,7 @@ __global__ void k_to_bf16(long long n, const float* __restrict__ x, uint16_t* __
 }
 
 __global__ void k_advance(int n, const float* __restrict__ pred, int ldp, double ascale, double gx, double gy,
-                          double gz, double h, double* __restrict__ posR, double* __restrict__ vel,
+                          double gz, double h, sdem_sg_box box, double* __restrict__ posR, double* __restrict__ vel,
                           double* __restrict__ omega) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -395,11 +395,20 @@ __global__ void k_advance(int n, const float* __restrict__ pred, int ldp, double
     for (int a = 0; a < 3; ++a) {
         const double acc = ascale * (double)pred[(size_t)i * ldp + a] + g[a];
         const double v0 = vel[(size_t)i * 3 + a];
-        const double vn = v0 + acc * h;
+        double vn = v0 + acc * h;
+        double x = posR[4 * (size_t)i + a] + vn * h;
+        const double lo = box.lo[a] + r, hi = box.hi[a] - r;
+        if (x < lo) {
+            x = lo;
+            vn = fmax(vn, 0.0);
+        } else if (x > hi) {
+            x = hi;
+            vn = fmin(vn, 0.0);
+        }
         vel[((size_t)2 * n + i) * 3 + a] = vel[((size_t)n + i) * 3 + a];
         vel[((size_t)n + i) * 3 + a] = v0;
         vel[(size_t)i * 3 + a] = vn;
-        posR[4 * (size_t)i + a] += vn * h;
+        posR[4 * (size_t)i + a] = x;
         const double al = ascale * (double)pred[(size_t)i * ldp + 3 + a] / r;
         omega[(size_t)i * 3 + a] += al * h;
     }
@@ -579,11 +588,11 @@ int sdem_sg_to_bf16(long long n, const float* x, uint16_t* y, void* stream) {
 }
 
 int sdem_sg_advance(int n, const float* pred, int ldp, double ascale, double gx, double gy, double gz, double h,
-                    double* posR, double* vel, double* omega, void* stream) {
-    if (n < 0 || ldp < 6) return SDEM_SG_E_ARG;
+                    const sdem_sg_box* box, double* posR, double* vel, double* omega, void* stream) {
+    if (n < 0 || ldp < 6 || !box) return SDEM_SG_E_ARG;
     if (n == 0) return SDEM_SG_OK;
     if (!pred || !posR || !vel || !omega) return SDEM_SG_E_ARG;
-    k_advance<<<blocks(n, 128), 128, 0, st(stream)>>>(n, pred, ldp, ascale, gx, gy, gz, h, posR, vel, omega);
+    k_advance<<<blocks(n, 128), 128, 0, st(stream)>>>(n, pred, ldp, ascale, gx, gy, gz, h, *box, posR, vel, omega);
     return launched();
 }
 

@@ -64,6 +64,10 @@ class SgOperand(C.Structure):
                 ("nseg", C.c_int), ("trans", C.c_int)]
 
 
+class SgBox(C.Structure):
+    _fields_ = [("lo", C.c_double * 3), ("hi", C.c_double * 3)]
+
+
 class SgEpilogue(C.Structure):
     _fields_ = [("bias", C.c_void_p), ("relu", C.c_int), ("accumulate", C.c_int),
                 ("mask", C.c_void_p), ("ld_mask", C.c_int),
@@ -99,7 +103,7 @@ def load(path: str = LIB_PATH):
         "sdem_sg_mse": [I, I, P, I, P, P, P, P, P],
         "sdem_sg_adam": [LL, P, P, P, P, P, F, F, F, F, F, I, P],
         "sdem_sg_to_bf16": [LL, P, P, P],
-        "sdem_sg_advance": [I, P, I, D, D, D, D, D, P, P, P, P],
+        "sdem_sg_advance": [I, P, I, D, D, D, D, D, C.POINTER(SgBox), P, P, P, P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -256,6 +260,37 @@ def node_features(posR: torch.Tensor, vel: torch.Tensor, omega: torch.Tensor, pl
 def planes_of(walls) -> np.ndarray:
     """(nw, 4) plane normals and offsets (n.x + d) of a WallSet."""
     return np.array([[w[12], w[13], w[14], w[15]] for w in walls.walls], dtype=np.float64).reshape(-1, 4)
+
+
+def box_of(walls) -> SgBox:
+    """The axis-aligned walls of a WallSet as the box that holds the spheres
+    in a surrogate stride: a plane n.x + d = 0 with n = +e_a (spheres on its
+    positive side) bounds x_a from below at -d, with n = -e_a from above at d;
+    open sides get -/+1e300."""
+    b = SgBox()
+    for a in range(3):
+        b.lo[a], b.hi[a] = -1e300, 1e300
+    for nx, ny, nz, d in planes_of(walls):
+        nrm = (nx, ny, nz)
+        for a in range(3):
+            if nrm[a] > 0.999999:
+                b.lo[a] = max(b.lo[a], -d / nrm[a])
+            elif nrm[a] < -0.999999:
+                b.hi[a] = min(b.hi[a], d / -nrm[a])
+    return b
+
+
+def align_frames(ids_now: np.ndarray, ids_old: np.ndarray, v_old: np.ndarray, v_now: np.ndarray) -> np.ndarray:
+    """The velocities of the spheres `ids_now` in an older frame (ids_old,
+    v_old); a sphere absent there keeps its current velocity (v_now)."""
+    out = np.array(v_now, dtype=np.float64, copy=True)
+    if len(ids_old) == 0 or len(ids_now) == 0:
+        return out
+    order = np.argsort(ids_old, kind="stable")
+    pos = np.clip(np.searchsorted(ids_old[order], ids_now), 0, len(ids_old) - 1)
+    hit = ids_old[order][pos] == ids_now
+    out[hit] = np.asarray(v_old)[order][pos[hit]]
+    return out
 
 
 # --------------------------------------------------------------- network
@@ -592,12 +627,16 @@ def evaluate(net: Network, samples: List[DeviceSample]) -> Tuple[float, float]:
 class SurrogateRunner:
     """Advances a bed by surrogate strides with a plain-DEM judge.
 
-    Every `judge_every` strides the plain DEM re-advances one stride from the
-    surrogate's state; the relative bed-height difference (mean sphere
-    height above the floor) between that stride and the surrogate's own
-    stride from the same state is the error.  Above `bound` the plain DEM
-    advances the next `fallback_strides` strides itself.  The run continues
-    from the plain DEM's state after every judged stride."""
+    Every `judge_every` surrogate strides the plain DEM re-advances one
+    stride from the surrogate's state; the relative bed-height difference
+    (mean sphere height above the floor, over the spheres both keep) between
+    that stride and the surrogate's own stride from the same state is the
+    error.  Within the bound the run continues from the plain DEM's state;
+    above it, or when the plain stride fails (a state the DEM rejects), the
+    last state the plain DEM produced is restored (simulated time rewinds to
+    it) and the plain DEM advances the next `fallback_strides` strides
+    itself.  Spheres the plain DEM deletes (out of the domain) leave the
+    surrogate's state with it; velocity frames are matched by sphere id."""
 
     def __init__(self, net: Network, system, case, stride: int, d_max: float, vscale: float,
                  judge_every: int = 20, bound: float = 0.02, fallback_strides: int = 20):
@@ -607,28 +646,35 @@ class SurrogateRunner:
         self.h = stride * case.opts.dt
         self.grid = make_grid(case.opts.minpoint, case.opts.maxpoint, d_max)
         self.planes = torch.from_numpy(planes_of(case.walls)).to(net.device)
+        self.box = box_of(case.walls)
         self.floor = float(case.opts.minpoint[1])
-        self.stats = {"surrogate_strides": 0, "dem_strides": 0, "judged": 0, "fallbacks": 0, "errors": []}
-        self._frames_from_dem(3)
+        self.t = 0                    # strides of simulated time since the start
+        self.since_judge = 0
+        self.stats = {"surrogate_strides": 0, "dem_strides": 0, "judged": 0, "fallbacks": 0, "rewound_strides": 0,
+                      "errors": []}
+        self._seed_from_dem()
 
-    def _pull(self):
-        st = self.sys.state()
-        return st
+    def _dem_stride(self) -> None:
+        self.sys.step(self.stride)
+        self.stats["dem_strides"] += 1
+        self.t += 1
 
-    def _frames_from_dem(self, k: int) -> None:
-        """k plain strides; the last three velocity frames seed the state."""
-        vs = []
-        for i in range(k):
-            if i:
-                self.sys.step(self.stride)
-                self.stats["dem_strides"] += 1
-            st = self._pull()
-            vs.append(st.linVel[:, 0, :].copy())
-        self.parts = st
+    def _adopt(self, st, vframes) -> None:
         dev = self.net.device
+        self.parts, self.good, self.good_t = st, st, self.t
         self.posR = torch.from_numpy(np.ascontiguousarray(st.posR)).to(dev)
-        self.vel = torch.from_numpy(np.ascontiguousarray(np.stack([vs[-1], vs[-2], vs[-3]]))).to(dev)
+        self.vel = torch.from_numpy(np.ascontiguousarray(np.stack(vframes))).to(dev)
         self.omega = torch.from_numpy(np.ascontiguousarray(st.rotVel[:, 0, :])).to(dev)
+
+    def _seed_from_dem(self) -> None:
+        """Two plain strides; the three frames (matched by id) seed the state."""
+        frames = [self.sys.state()]
+        for _ in range(2):
+            self._dem_stride()
+            frames.append(self.sys.state())
+        st = frames[-1]
+        v = st.linVel[:, 0, :]
+        self._adopt(st, [v] + [align_frames(st.id, f.id, f.linVel[:, 0, :], v) for f in (frames[1], frames[0])])
 
     def bed_height(self, posR: torch.Tensor) -> float:
         return float((posR[:, 1] - self.floor).mean())
@@ -639,8 +685,8 @@ class SurrogateRunner:
         y = self.net.forward(g, xn, keep=False)
         gx, gy, gz = self.case.opts.gravity
         _check(self.net.lib.sdem_sg_advance(posR.shape[0], _ptr(y), OUT, float(np.linalg.norm(self.case.opts.gravity)),
-                                            gx, gy, gz, self.h, _ptr(posR), _ptr(vel), _ptr(omega), _stream()),
-               "sdem_sg_advance")
+                                            gx, gy, gz, self.h, C.byref(self.box), _ptr(posR), _ptr(vel), _ptr(omega),
+                                            _stream()), "sdem_sg_advance")
 
     def _upload(self) -> None:
         """The surrogate state into the plain DEM (contact history restarts)."""
@@ -656,43 +702,49 @@ class SurrogateRunner:
             p.rotAcc[:, k, :] = 0.0
         self.sys.upload(p)
 
+    def _judged_stride(self) -> None:
+        ids = self.parts.id
+        self._upload()
+        p2 = self.posR.clone()
+        self._surrogate_stride(p2, self.vel.clone(), self.omega.clone())
+        try:
+            self._dem_stride()
+            st = self.sys.state()
+        except Exception:       # the plain DEM rejected the surrogate's state
+            st = None
+        self.stats["judged"] += 1
+        self.stats["surrogate_strides"] += 1
+        if st is None:
+            err = math.inf
+        else:
+            keep = np.isin(ids, st.id)
+            h_sur = float((p2[:, 1].cpu().numpy()[keep] - self.floor).mean())
+            h_dem = float((st.posR[:, 1] - self.floor).mean())
+            err = abs(h_sur - h_dem) / max(abs(h_dem), 1e-300)
+        self.stats["errors"].append(err)
+        if err > self.bound:
+            self.stats["fallbacks"] += 1
+            if st is None:
+                self.sys.upload(self.good)
+                self.stats["rewound_strides"] += self.t - self.good_t
+                self.t = self.good_t
+            for _ in range(self.fallback):
+                self._dem_stride()
+            self._seed_from_dem()
+        else:
+            v = st.linVel[:, 0, :]
+            vprev = self.vel.cpu().numpy()
+            self._adopt(st, [v, align_frames(st.id, ids, vprev[0], v), align_frames(st.id, ids, vprev[1], v)])
+
     def run(self, strides: int) -> dict:
-        done = 0
-        pending_dem = 0
-        while done < strides:
-            if pending_dem:
-                self.sys.step(self.stride)
-                self.stats["dem_strides"] += 1
-                pending_dem -= 1
-                done += 1
-                if pending_dem == 0:
-                    self._frames_from_dem(3)
-                    done += 2
-                continue
-            if (self.stats["surrogate_strides"] + 1) % self.judge_every == 0:
-                self._upload()
-                p2, v2, w2 = self.posR.clone(), self.vel.clone(), self.omega.clone()
-                self._surrogate_stride(p2, v2, w2)
-                self.sys.step(self.stride)
-                self.stats["dem_strides"] += 1
-                self.stats["judged"] += 1
-                st = self._pull()
-                h_dem = float((st.posR[:, 1] - self.floor).mean())
-                err = abs(self.bed_height(p2) - h_dem) / max(abs(h_dem), 1e-300)
-                self.stats["errors"].append(err)
-                self.stats["surrogate_strides"] += 1
-                done += 1
-                if err > self.bound:
-                    self.stats["fallbacks"] += 1
-                    pending_dem = self.fallback
-                else:
-                    self.parts = st
-                    self.posR = torch.from_numpy(np.ascontiguousarray(st.posR)).to(self.net.device)
-                    self.vel = torch.stack([torch.from_numpy(st.linVel[:, 0, :].copy()).to(self.net.device),
-                                            self.vel[0], self.vel[1]])
-                    self.omega = torch.from_numpy(np.ascontiguousarray(st.rotVel[:, 0, :])).to(self.net.device)
+        """Advances the bed by at least `strides` strides of simulated time."""
+        target = self.t + strides
+        while self.t < target:
+            self.since_judge += 1
+            if self.since_judge % self.judge_every == 0:
+                self._judged_stride()
                 continue
             self._surrogate_stride(self.posR, self.vel, self.omega)
             self.stats["surrogate_strides"] += 1
-            done += 1
+            self.t += 1
         return self.stats

@@ -13,6 +13,8 @@ int main(void) {
     printf("sdem_sg_operand %zu\n", sizeof(sdem_sg_operand));
     F(sdem_sg_operand, idx); F(sdem_sg_operand, ld); F(sdem_sg_operand, width); F(sdem_sg_operand, nseg);
     F(sdem_sg_operand, trans);
+    printf("sdem_sg_box %zu\n", sizeof(sdem_sg_box));
+    F(sdem_sg_box, hi);
     printf("sdem_sg_epilogue %zu\n", sizeof(sdem_sg_epilogue));
     F(sdem_sg_epilogue, relu); F(sdem_sg_epilogue, accumulate); F(sdem_sg_epilogue, mask);
     F(sdem_sg_epilogue, ld_mask); F(sdem_sg_epilogue, out); F(sdem_sg_epilogue, ld_out);

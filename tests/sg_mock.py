@@ -188,16 +188,24 @@ class SgMock:
         _flat(y, np.uint16, n)[:] = _bf_enc(_flat(x, np.float32, n))
         return 0
 
-    def sdem_sg_advance(self, n, pred, ldp, ascale, gx, gy, gz, h, posR, vel, omega, stream):
+    def sdem_sg_advance(self, n, pred, ldp, ascale, gx, gy, gz, h, box, posR, vel, omega, stream):
+        b = _obj(box)
         p = _mat(pred, np.float32, n, ldp, ldp).astype(np.float64)
         pos = _mat(posR, np.float64, n, 4, 4)
         v = _flat(vel, np.float64, 9 * n).reshape(3, n, 3)
         w = _mat(omega, np.float64, n, 3, 3)
+        r = pos[:, 3:4]
         a = ascale * p[:, :3] + np.array([gx, gy, gz])[None, :]
         vn = v[0] + a * h
+        x = pos[:, :3] + vn * h
+        lo = np.array(list(b.lo))[None, :] + r
+        hi = np.array(list(b.hi))[None, :] - r
+        below, above = x < lo, x > hi
+        x = np.where(below, lo, np.where(above, hi, x))
+        vn = np.where(below, np.maximum(vn, 0.0), np.where(above, np.minimum(vn, 0.0), vn))
         v[2] = v[1]
         v[1] = v[0]
         v[0] = vn
-        pos[:, :3] += vn * h
-        w += ascale * p[:, 3:6] / pos[:, 3:4] * h
+        pos[:, :3] = x
+        w += ascale * p[:, 3:6] / r * h
         return 0

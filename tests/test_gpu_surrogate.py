@@ -240,15 +240,27 @@ def test_training_beats_free_flight(sg_lib):
 
 
 def test_runner_judges_and_falls_back(sg_lib):
-    for bound, expect_fallback in ((1.0, False), (0.0, True)):
+    # an untrained network: its strides let spheres close in on each other, so
+    # a judged stride may also meet a state the plain DEM rejects (explosive
+    # repulsion); the runner must restore the last plain state then
+    for bound in (1.0, 0.0):
         case, s = settled_sandbox(1500, 20, 2000)
         dmax = 2.0 * float(case.tables.radius.max())
         net = sg.Network(seed=1)
         r = sg.SurrogateRunner(net, s, case, stride=100, d_max=dmax, vscale=0.05, judge_every=4, bound=bound,
                                fallback_strides=3)
         st = r.run(12)
-        assert st["judged"] >= 1 and all(math.isfinite(x) for x in st["errors"])
-        assert (st["fallbacks"] > 0) == expect_fallback
-        assert st["surrogate_strides"] + st["dem_strides"] >= 12
-        assert torch.isfinite(r.posR).all()
+        assert r.t >= 14 and st["judged"] >= 1
+        errs = st["errors"]
+        assert len(errs) == st["judged"] and all(e >= 0.0 for e in errs)
+        # a fallback exactly when a judged error exceeds the bound
+        assert st["fallbacks"] == sum(1 for e in errs if e > bound)
+        if bound == 0.0:
+            assert st["fallbacks"] >= 1
+        assert torch.isfinite(r.posR).all() and r.posR.shape[0] == s.counters()["nlocal"]
+        # the centres stay inside the box's walls (open top)
+        box = sg.box_of(case.walls)
+        p = r.posR.cpu().numpy()
+        for a in range(3):
+            assert np.all(p[:, a] >= box.lo[a]) and np.all(p[:, a] <= box.hi[a])
         s.close()

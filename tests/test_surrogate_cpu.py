@@ -41,7 +41,8 @@ def test_struct_layouts_match_the_compiler(tmp_path):
         if line:
             k, v = line.split()
             want[k] = int(v)
-    mirrors = {"sdem_sg_grid": sg.SgGrid, "sdem_sg_operand": sg.SgOperand, "sdem_sg_epilogue": sg.SgEpilogue}
+    mirrors = {"sdem_sg_grid": sg.SgGrid, "sdem_sg_operand": sg.SgOperand, "sdem_sg_epilogue": sg.SgEpilogue,
+               "sdem_sg_box": sg.SgBox}
     for key, val in want.items():
         if "." in key:
             s, f = key.split(".")

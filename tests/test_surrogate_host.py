@@ -3,6 +3,8 @@ features, forward, backward, Adam, one stride) run on CPU tensors through a
 numpy statement of the C ABI (tests/sg_mock.py) and compared with the
 oracle: operand segments, gather indices, strides, offsets and the order of
 the backward pass are checked without a GPU."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -108,11 +110,43 @@ def test_stride_update(mock):
     om = torch.from_numpy(rng.normal(size=(n, 3)))
     v0, v1, p0, w0 = vel[0].clone(), vel[1].clone(), pos.clone(), om.clone()
     h = 2e-4
-    assert sg.load().sdem_sg_advance(n, sg._ptr(pred), sg.OUT, 9.81, 0.0, -9.81, 0.0, h, sg._ptr(pos), sg._ptr(vel),
-                                     sg._ptr(om), 0) == 0
+    box = sg.SgBox()
+    for a in range(3):
+        box.lo[a], box.hi[a] = -1e300, 1e300
+    box.lo[1] = float(np.sort(posR[:, 1] - posR[:, 3])[n // 2])   # half of the spheres start against a floor
+    assert sg.load().sdem_sg_advance(n, sg._ptr(pred), sg.OUT, 9.81, 0.0, -9.81, 0.0, h, ctypes.byref(box),
+                                     sg._ptr(pos), sg._ptr(vel), sg._ptr(om), 0) == 0
     a = 9.81 * pred[:, :3].double() + torch.tensor([0.0, -9.81, 0.0], dtype=torch.float64)
-    torch.testing.assert_close(vel[0], v0 + a * h)
+    vfree = v0 + a * h
+    xfree = p0[:, :3] + vfree * h
+    floor = box.lo[1] + p0[:, 3]
+    held = xfree[:, 1] < floor
+    assert held.any() and (~held).any()
     torch.testing.assert_close(vel[1], v0)
     torch.testing.assert_close(vel[2], v1)
-    torch.testing.assert_close(pos[:, :3], p0[:, :3] + vel[0] * h)
+    torch.testing.assert_close(vel[0][:, [0, 2]], vfree[:, [0, 2]])
+    torch.testing.assert_close(pos[:, [0, 2]], xfree[:, [0, 2]])
+    torch.testing.assert_close(pos[~held, 1], xfree[~held, 1])
+    torch.testing.assert_close(vel[0][~held, 1], vfree[~held, 1])
+    torch.testing.assert_close(pos[held, 1], floor[held])
+    torch.testing.assert_close(vel[0][held, 1], vfree[held, 1].clamp(min=0.0))
     torch.testing.assert_close(om, w0 + 9.81 * pred[:, 3:6].double() / p0[:, 3:4] * h)
+
+
+def test_box_of_walls():
+    from sdem_gb300 import beds
+    case = beds.sandbox_case(np.random.default_rng(4), 0, n_lo=300, n_hi=300)
+    b = sg.box_of(case.walls)
+    lo, hi = case.opts.minpoint, case.opts.maxpoint
+    for a in range(3):
+        assert b.lo[a] == pytest.approx(lo[a], abs=1e-15)
+    assert b.hi[0] == pytest.approx(hi[0]) and b.hi[2] == pytest.approx(hi[2])
+    assert b.hi[1] == 1e300          # open top
+
+
+def test_frames_aligned_by_id():
+    now = np.array([5, 2, 9], np.int32)
+    old = np.array([9, 5, 7], np.int32)
+    v_old = np.array([[9.0] * 3, [5.0] * 3, [7.0] * 3])
+    v_now = np.zeros((3, 3))
+    np.testing.assert_array_equal(sg.align_frames(now, old, v_old, v_now)[:, 0], [5.0, 0.0, 9.0])
