@@ -465,6 +465,7 @@ def surrogate_arm(args):
                                 fallback_strides=args.judge_every)
     K = max(1, args.strides)
     runner._surrogate_stride(runner.posR, runner.vel, runner.omega)     # warm-up
+    phases, E = surrogate_phases(runner, net, sg, torch)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(K):
@@ -488,6 +489,10 @@ def surrogate_arm(args):
             "data": "synthetic",
             "plain_dem": K * h / t_plain, "ratio_vs_plain": t_plain / t_sur,
             "ms_per_stride": {"surrogate": t_sur / K * 1e3, "plain_dem": t_plain / K * 1e3},
+            "surrogate_phases_ms": phases,
+            "forward_tensor": {"flop": surrogate_forward_flop(case.particles.n, E),
+                               "achieved_tflops": surrogate_forward_flop(case.particles.n, E) / phases["forward"] / 1e9,
+                               "peak_tflops": measured_bf16_tflops(), "peak_note": "bf16 dense, burst, of measured"},
             "with_judge": {"strides": 2 * args.judge_every, "sim_s_per_s": run_strides * h / t_run,
                            "rewound_strides": stats["rewound_strides"],
                            "judged": stats["judged"], "fallbacks": stats["fallbacks"],
@@ -496,13 +501,61 @@ def surrogate_arm(args):
                          "loss_first10": float(np.mean(losses[:10])), "loss_last10": float(np.mean(losses[-10:])),
                          "heldout_mse": mse, "heldout_mse_free_flight": mse_free, "data_s": t_data,
                          "train_s": t_train},
-            "config": {"workload": "surrogate_hertz_poly_1m", "particles": case.particles.n, "stride_steps": S,
+            "config": {"workload": "surrogate_hertz_poly_1m", "particles": case.particles.n, "edges": E,
+                       "stride_steps": S,
                        "dt": case.opts.dt,
                        "latent": sg.LATENT, "layers": sg.LAYERS, "cutoff_dmax": sg.CUTOFF_FACTOR},
             "note": "host wall clock around synchronised runs; the stride update integrates the predicted "
                     "stride-mean accelerations (semi-implicit Euler over the stride)"}
     print(json.dumps(line), flush=True)
     dem.close()
+
+
+def surrogate_forward_flop(n: int, E: int, latent: int = 128, layers: int = 6) -> float:
+    """Tensor-core flops of one surrogate forward pass (2 per multiply-add):
+    encoders, `layers` edge MLPs over [h_dst, h_src, e] and node MLPs over
+    [h, agg], decoder."""
+    L = latent
+    edge = 2 * (16 * L + L * L) + layers * 2 * (3 * L * L + L * L)
+    node = 2 * (32 * L + L * L) + layers * 2 * (2 * L * L + L * L) + 2 * (L * L + L * 16)
+    return float(E * edge + n * node)
+
+
+def measured_bf16_tflops():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except Exception:
+        return 1900.0
+
+
+def surrogate_phases(runner, net, sg, torch, reps: int = 3):
+    """Median CUDA-event times (ms) of the parts of one surrogate stride on
+    the runner's state (graph build, node features, forward, stride update)
+    and the edge count."""
+    import ctypes
+    out = {"graph": [], "features": [], "forward": [], "update": []}
+    E = 0
+    for _ in range(reps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        ev[0].record()
+        g = sg.build_graph(runner.posR, runner.grid, sender_order=False)
+        ev[1].record()
+        xn = sg.node_features(runner.posR, runner.vel, runner.omega, runner.planes, runner.d_max, runner.vscale)
+        ev[2].record()
+        y = net.forward(g, xn, keep=False)
+        ev[3].record()
+        gx, gy, gz = runner.case.opts.gravity
+        rc = net.lib.sdem_sg_advance(runner.posR.shape[0], sg._ptr(y), sg.OUT, 9.81, gx, gy, gz, runner.h,
+                                     ctypes.byref(runner.box), sg._ptr(runner.posR), sg._ptr(runner.vel),
+                                     sg._ptr(runner.omega), sg._stream())
+        assert rc == 0
+        ev[4].record()
+        torch.cuda.synchronize()
+        for k, name in enumerate(("graph", "features", "forward", "update")):
+            out[name].append(ev[k].elapsed_time(ev[k + 1]))
+        E = g.E
+    return {k: statistics.median(v) for k, v in out.items()}, E
 
 
 def props_cft_nlin():

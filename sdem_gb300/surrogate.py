@@ -193,8 +193,8 @@ class Graph:
     dst: torch.Tensor          # int32 (E)
     src: torch.Tensor          # int32 (E)
     efeat: torch.Tensor        # bf16 (E, 16)
-    src_perm: torch.Tensor     # int32 (E): edges ordered by sender
-    src_off: torch.Tensor      # int32 (n+1)
+    src_perm: Optional[torch.Tensor]   # int32 (E): edges ordered by sender (backward only)
+    src_off: Optional[torch.Tensor]    # int32 (n+1)
 
 
 def make_grid(lo, hi, d_max: float) -> SgGrid:
@@ -213,8 +213,10 @@ def make_grid(lo, hi, d_max: float) -> SgGrid:
     return g
 
 
-def build_graph(posR: torch.Tensor, grid: SgGrid) -> Graph:
-    """Neighbour graph of the spheres in posR (cuda float64, n x 4)."""
+def build_graph(posR: torch.Tensor, grid: SgGrid, sender_order: bool = True) -> Graph:
+    """Neighbour graph of the spheres in posR (cuda float64, n x 4); the
+    sender-ordered permutation (needed by the backward pass only) is built
+    when sender_order is set."""
     lib = load()
     n = posR.shape[0]
     dev = posR.device
@@ -238,10 +240,12 @@ def build_graph(posR: torch.Tensor, grid: SgGrid) -> Graph:
     efeat = torch.empty((max(E, 1), EDGE_IN), dtype=torch.bfloat16, device=dev)
     _check(lib.sdem_sg_edge_fill(n, _ptr(posR), C.byref(grid), _ptr(cell), _ptr(cell_start), _ptr(sorted_idx),
                                  _ptr(row_off), _ptr(dst), _ptr(src), _ptr(efeat), s), "sdem_sg_edge_fill")
-    skey = src.to(torch.int64) * max(E, 1) + torch.arange(E, device=dev, dtype=torch.int64)
-    src_perm = torch.argsort(skey).to(torch.int32)
-    src_off = torch.zeros(n + 1, dtype=torch.int32, device=dev)
-    src_off[1:] = torch.cumsum(torch.bincount(src.to(torch.int64), minlength=n), 0).to(torch.int32)
+    src_perm = src_off = None
+    if sender_order:
+        skey = src.to(torch.int64) * max(E, 1) + torch.arange(E, device=dev, dtype=torch.int64)
+        src_perm = torch.argsort(skey).to(torch.int32)
+        src_off = torch.zeros(n + 1, dtype=torch.int32, device=dev)
+        src_off[1:] = torch.cumsum(torch.bincount(src.to(torch.int64), minlength=n), 0).to(torch.int32)
     return Graph(n, E, row_off, dst, src, efeat[:E], src_perm, src_off)
 
 
@@ -455,6 +459,8 @@ class Network:
         s, g = self.saved, self.graph
         if s is None:
             raise RuntimeError("backward needs a forward with keep=True")
+        if g.src_perm is None:
+            raise RuntimeError("backward needs a graph built with sender_order=True")
         L, n, E, dev = self.latent, g.n, g.E, self.device
         bf, f32 = torch.bfloat16, torch.float32
         lib = self.lib
@@ -680,7 +686,7 @@ class SurrogateRunner:
         return float((posR[:, 1] - self.floor).mean())
 
     def _surrogate_stride(self, posR, vel, omega) -> None:
-        g = build_graph(posR, self.grid)
+        g = build_graph(posR, self.grid, sender_order=False)
         xn = node_features(posR, vel, omega, self.planes, self.d_max, self.vscale)
         y = self.net.forward(g, xn, keep=False)
         gx, gy, gz = self.case.opts.gravity
