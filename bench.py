@@ -464,6 +464,7 @@ def surrogate_arm(args):
     runner = sg.SurrogateRunner(net, dem, case, S, dmax, vscale, judge_every=args.judge_every, bound=0.02,
                                 fallback_strides=args.judge_every)
     K = max(1, args.strides)
+    start = (runner.posR.clone(), runner.vel.clone(), runner.omega.clone())
     runner._surrogate_stride(runner.posR, runner.vel, runner.omega)     # warm-up
     phases, E = surrogate_phases(runner, net, sg, torch)
     torch.cuda.synchronize()
@@ -476,6 +477,9 @@ def surrogate_arm(args):
     dem.step(K * S)
     dem.counters()
     t_plain = time.perf_counter() - t0
+    # the judged run starts again from the plain state the timing started from
+    runner.posR, runner.vel, runner.omega = start
+    runner.edge_ref = None
     h = S * case.opts.dt
     t_sim0 = runner.t
     t0 = time.perf_counter()
@@ -496,6 +500,7 @@ def surrogate_arm(args):
             "with_judge": {"strides": 2 * args.judge_every, "sim_s_per_s": run_strides * h / t_run,
                            "rewound_strides": stats["rewound_strides"],
                            "judged": stats["judged"], "fallbacks": stats["fallbacks"],
+                           "diverged": stats["diverged"],
                            "bed_height_rel_err": stats["errors"]},
             "training": {"beds": args.train_beds, "samples": len(train), "iters": args.train_iters,
                          "loss_first10": float(np.mean(losses[:10])), "loss_last10": float(np.mean(losses[-10:])),
@@ -579,8 +584,8 @@ def main():
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--train-beds", type=int, default=3)
     ap.add_argument("--train-iters", type=int, default=300)
-    ap.add_argument("--strides", type=int, default=10)
-    ap.add_argument("--judge-every", type=int, default=10)
+    ap.add_argument("--strides", type=int, default=5)
+    ap.add_argument("--judge-every", type=int, default=5)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

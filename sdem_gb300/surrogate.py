@@ -630,6 +630,11 @@ def evaluate(net: Network, samples: List[DeviceSample]) -> Tuple[float, float]:
 
 # --------------------------------------------------------------- rollout
 
+class Diverged(RuntimeError):
+    """The surrogate's state has collapsed: its neighbour graph outgrew the
+    limit set from the last plain-DEM state."""
+
+
 class SurrogateRunner:
     """Advances a bed by surrogate strides with a plain-DEM judge.
 
@@ -642,11 +647,18 @@ class SurrogateRunner:
     last state the plain DEM produced is restored (simulated time rewinds to
     it) and the plain DEM advances the next `fallback_strides` strides
     itself.  Spheres the plain DEM deletes (out of the domain) leave the
-    surrogate's state with it; velocity frames are matched by sphere id."""
+    surrogate's state with it; velocity frames are matched by sphere id.
+    A surrogate stride whose graph has more than `edge_growth` times the
+    edges of the first graph after the last plain state counts as a failed
+    judgement too (spheres interpenetrating without the contact repulsion
+    the network has not learned: the graph and its memory would grow
+    without bound)."""
 
     def __init__(self, net: Network, system, case, stride: int, d_max: float, vscale: float,
-                 judge_every: int = 20, bound: float = 0.02, fallback_strides: int = 20):
+                 judge_every: int = 20, bound: float = 0.02, fallback_strides: int = 20, edge_growth: float = 3.0):
         self.net, self.sys, self.case = net, system, case
+        self.edge_growth = edge_growth
+        self.edge_ref = None
         self.stride, self.d_max, self.vscale = stride, d_max, vscale
         self.judge_every, self.bound, self.fallback = judge_every, bound, fallback_strides
         self.h = stride * case.opts.dt
@@ -657,7 +669,7 @@ class SurrogateRunner:
         self.t = 0                    # strides of simulated time since the start
         self.since_judge = 0
         self.stats = {"surrogate_strides": 0, "dem_strides": 0, "judged": 0, "fallbacks": 0, "rewound_strides": 0,
-                      "errors": []}
+                      "diverged": 0, "errors": []}
         self._seed_from_dem()
 
     def _dem_stride(self) -> None:
@@ -668,6 +680,8 @@ class SurrogateRunner:
     def _adopt(self, st, vframes) -> None:
         dev = self.net.device
         self.parts, self.good, self.good_t = st, st, self.t
+        self.edge_ref = None
+        self.since_judge = 0
         self.posR = torch.from_numpy(np.ascontiguousarray(st.posR)).to(dev)
         self.vel = torch.from_numpy(np.ascontiguousarray(np.stack(vframes))).to(dev)
         self.omega = torch.from_numpy(np.ascontiguousarray(st.rotVel[:, 0, :])).to(dev)
@@ -687,6 +701,10 @@ class SurrogateRunner:
 
     def _surrogate_stride(self, posR, vel, omega) -> None:
         g = build_graph(posR, self.grid, sender_order=False)
+        if self.edge_ref is None:
+            self.edge_ref = max(g.E, 1)
+        elif g.E > self.edge_growth * self.edge_ref:
+            raise Diverged(f"{g.E} edges against {self.edge_ref} after the last plain state")
         xn = node_features(posR, vel, omega, self.planes, self.d_max, self.vscale)
         y = self.net.forward(g, xn, keep=False)
         gx, gy, gz = self.case.opts.gravity
@@ -707,6 +725,18 @@ class SurrogateRunner:
             p.rotVel[:, k, :] = w
             p.rotAcc[:, k, :] = 0.0
         self.sys.upload(p)
+
+    def _fall_back(self, rewind: bool) -> None:
+        """Restores the last plain state (rewind) or keeps the plain DEM's
+        current one, then lets the plain DEM advance `fallback_strides`."""
+        self.stats["fallbacks"] += 1
+        if rewind:
+            self.sys.upload(self.good)
+            self.stats["rewound_strides"] += self.t - self.good_t
+            self.t = self.good_t
+        for _ in range(self.fallback):
+            self._dem_stride()
+        self._seed_from_dem()
 
     def _judged_stride(self) -> None:
         ids = self.parts.id
@@ -729,14 +759,7 @@ class SurrogateRunner:
             err = abs(h_sur - h_dem) / max(abs(h_dem), 1e-300)
         self.stats["errors"].append(err)
         if err > self.bound:
-            self.stats["fallbacks"] += 1
-            if st is None:
-                self.sys.upload(self.good)
-                self.stats["rewound_strides"] += self.t - self.good_t
-                self.t = self.good_t
-            for _ in range(self.fallback):
-                self._dem_stride()
-            self._seed_from_dem()
+            self._fall_back(rewind=st is None)
         else:
             v = st.linVel[:, 0, :]
             vprev = self.vel.cpu().numpy()
@@ -747,10 +770,15 @@ class SurrogateRunner:
         target = self.t + strides
         while self.t < target:
             self.since_judge += 1
-            if self.since_judge % self.judge_every == 0:
-                self._judged_stride()
+            try:
+                if self.since_judge % self.judge_every == 0:
+                    self._judged_stride()
+                    continue
+                self._surrogate_stride(self.posR, self.vel, self.omega)
+            except Diverged:
+                self.stats["diverged"] += 1
+                self._fall_back(rewind=True)
                 continue
-            self._surrogate_stride(self.posR, self.vel, self.omega)
             self.stats["surrogate_strides"] += 1
             self.t += 1
         return self.stats

@@ -150,3 +150,27 @@ def test_frames_aligned_by_id():
     v_old = np.array([[9.0] * 3, [5.0] * 3, [7.0] * 3])
     v_now = np.zeros((3, 3))
     np.testing.assert_array_equal(sg.align_frames(now, old, v_old, v_now)[:, 0], [5.0, 0.0, 9.0])
+
+
+@pytest.mark.parametrize("bound,growth", [(1.0, 100.0), (0.0, 100.0), (1.0, 0.5)])
+def test_runner_over_the_oracle(mock, bound, growth):
+    # the runner's bookkeeping with the oracle as the plain DEM: judged
+    # strides, fallbacks above the bound, divergence of the graph (a limit
+    # below one edge-count ratio makes every second stride diverge), rewinds
+    from oracle.oracle import OracleSystem
+    from sdem_gb300 import beds
+    case = beds.sandbox_case(np.random.default_rng(30), 0, n_lo=300, n_hi=300)
+    dem = OracleSystem(case)
+    dem.step(500)
+    net = sg.Network(seed=1, device="cpu", latent=LATENT, layers=LAYERS)
+    r = sg.SurrogateRunner(net, dem, case, stride=20, d_max=2.0 * float(case.tables.radius.max()), vscale=0.05,
+                           judge_every=3, bound=bound, fallback_strides=2, edge_growth=growth)
+    t0 = r.t
+    st = r.run(9)
+    assert r.t >= t0 + 9
+    assert st["fallbacks"] == sum(1 for e in st["errors"] if e > bound) + st["diverged"]
+    if bound == 0.0:
+        assert st["fallbacks"] >= 1 and st["diverged"] == 0
+    if growth < 1.0:
+        assert st["diverged"] >= 1 and st["rewound_strides"] >= 1
+    assert r.posR.shape[0] == dem.counters()["nlocal"] and torch.isfinite(r.posR).all()
