@@ -232,9 +232,13 @@ def build_graph(posR: torch.Tensor, grid: SgGrid, sender_order: bool = True) -> 
     degree = torch.empty(n, dtype=torch.int32, device=dev)
     _check(lib.sdem_sg_edge_count(n, _ptr(posR), C.byref(grid), _ptr(cell), _ptr(cell_start), _ptr(sorted_idx),
                                   _ptr(degree), s), "sdem_sg_edge_count")
+    csum = torch.cumsum(degree.to(torch.int64), 0)
+    E = int(csum[-1].item()) if n else 0
+    if E > 2**31 - 1:
+        # the CSR offsets and edge indices are int32 on the device
+        raise RuntimeError(f"{E} edges: more than the int32 offsets of the graph can address")
     row_off = torch.zeros(n + 1, dtype=torch.int32, device=dev)
-    row_off[1:] = torch.cumsum(degree.to(torch.int64), 0).to(torch.int32)
-    E = int(row_off[-1].item())
+    row_off[1:] = csum.to(torch.int32)
     dst = torch.empty(E, dtype=torch.int32, device=dev)
     src = torch.empty(E, dtype=torch.int32, device=dev)
     efeat = torch.empty((max(E, 1), EDGE_IN), dtype=torch.bfloat16, device=dev)
