@@ -134,3 +134,17 @@ def test_oracle_backward_against_finite_differences():
         pm[k] -= h
         fd = (loss(pp) - loss(pm)) / (2 * h)
         assert abs(fd - g[k]) <= 1e-7 + 1e-4 * abs(fd), (k, fd, g[k])
+
+
+def test_forward_flop_count_of_the_bench():
+    # the tensor roofline's flop figure equals 2 M kin kout summed over the
+    # weights of the layout (M = edges for edge layers, spheres otherwise)
+    import bench
+    n, E = 1000, 24000
+    want = 0
+    for name, shape, off in sg.param_layout():
+        if len(shape) != 2:
+            continue
+        rows = E if (name.startswith("edge") or name.startswith("enc_e")) else n
+        want += 2 * rows * shape[0] * shape[1]
+    assert bench.surrogate_forward_flop(n, E) == float(want)
