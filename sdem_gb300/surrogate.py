@@ -119,9 +119,16 @@ def _check(rc: int, what: str) -> None:
 
 
 def _ptr(t: Optional[torch.Tensor], offset: int = 0) -> Optional[int]:
+    """Address of element `offset` of t.  A zero-element view reports a null
+    data pointer; its address inside its storage is used instead, so an
+    empty slice of an allocated buffer still passes the library's checks."""
     if t is None:
         return None
-    return t.data_ptr() + offset * t.element_size()
+    if t.numel():
+        base = t.data_ptr()
+    else:
+        base = t.untyped_storage().data_ptr() + t.storage_offset() * t.element_size()
+    return base + offset * t.element_size()
 
 
 def _stream() -> int:
@@ -239,8 +246,10 @@ def build_graph(posR: torch.Tensor, grid: SgGrid, sender_order: bool = True) -> 
         raise RuntimeError(f"{E} edges: more than the int32 offsets of the graph can address")
     row_off = torch.zeros(n + 1, dtype=torch.int32, device=dev)
     row_off[1:] = csum.to(torch.int32)
-    dst = torch.empty(E, dtype=torch.int32, device=dev)
-    src = torch.empty(E, dtype=torch.int32, device=dev)
+    # at least one row: an empty tensor has a null data pointer, which the
+    # library refuses even when there is nothing to write
+    dst = torch.empty(max(E, 1), dtype=torch.int32, device=dev)[:E]
+    src = torch.empty(max(E, 1), dtype=torch.int32, device=dev)[:E]
     efeat = torch.empty((max(E, 1), EDGE_IN), dtype=torch.bfloat16, device=dev)
     _check(lib.sdem_sg_edge_fill(n, _ptr(posR), C.byref(grid), _ptr(cell), _ptr(cell_start), _ptr(sorted_idx),
                                  _ptr(row_off), _ptr(dst), _ptr(src), _ptr(efeat), s), "sdem_sg_edge_fill")

@@ -68,6 +68,8 @@ class SgMock:
         return 0
 
     def sdem_sg_edge_fill(self, n, posR, g, cell, cell_start, sorted_idx, row_off, dst, src, efeat, stream):
+        if n and not (posR and cell and cell_start and sorted_idx and row_off and dst and src and efeat):
+            return 1          # SDEM_SG_E_ARG, as the library
         _, (ro, d, s, ef) = self._graph(n, posR, _obj(g))
         assert np.array_equal(_flat(row_off, np.int32, n + 1), ro)
         E = len(d)
@@ -88,6 +90,7 @@ class SgMock:
     def _operand(self, op, rows, cover):
         """(rows, cover) float64 logical matrix of an operand."""
         parts = []
+        assert all(op.ptr[s] for s in range(op.nseg)), "null operand pointer"
         for s in range(op.nseg):
             idx = _flat(op.idx[s], np.int32, rows) if op.idx[s] else np.arange(rows)
             nsrc = int(idx.max()) + 1 if rows else 0
@@ -99,6 +102,8 @@ class SgMock:
 
     def sdem_sg_gemm(self, I, J, R, a, b, ep, splits, partial, stream):
         a, b, ep = _obj(a), _obj(b), _obj(ep)
+        if I == 0 or J == 0:
+            return 0
         A = self._operand(a, R, I).T if a.trans else self._operand(a, I, R)
         B = self._operand(b, R, J).T if b.trans else self._operand(b, J, R)
         v = (A @ B.T).astype(np.float32)
@@ -142,6 +147,8 @@ class SgMock:
         return 0
 
     def sdem_sg_gather_add(self, rows, J, idx, x, ldx, y, ldy, out, ld_out, out_bf, ld_out_bf, stream):
+        if rows == 0:
+            return 0
         ix = _flat(idx, np.int32, rows) if idx else np.arange(rows)
         nsrc = int(ix.max()) + 1 if rows else 0
         v = _mat(x, np.float32, nsrc, J, ldx)[ix]

@@ -174,3 +174,27 @@ def test_runner_over_the_oracle(mock, bound, growth):
     if growth < 1.0:
         assert st["diverged"] >= 1 and st["rewound_strides"] >= 1
     assert r.posR.shape[0] == dem.counters()["nlocal"] and torch.isfinite(r.posR).all()
+
+
+def test_graph_without_edges(mock):
+    # spheres farther apart than the cutoff: an empty graph; forward, loss,
+    # backward and Adam still run (encoder and node layers only)
+    n = 8
+    pos = np.stack([np.arange(n) * 5e-3 + 1e-3, np.full(n, 1e-3), np.full(n, 1e-3)], axis=1)
+    posR = np.concatenate([pos, np.full((n, 1), 0.5e-3)], axis=1)
+    grid = sg.make_grid((0, 0, 0), (0.05, 0.01, 0.01), 1.2e-3)
+    g = sg.build_graph(torch.from_numpy(posR), grid)
+    assert g.E == 0 and g.dst.numel() == 0 and g.src_perm.numel() == 0
+    xn = sg.node_features(torch.from_numpy(posR), torch.zeros((3, n, 3), dtype=torch.float64),
+                          torch.zeros((n, 3), dtype=torch.float64), torch.zeros((0, 4), dtype=torch.float64),
+                          1.2e-3, 0.05)
+    net = sg.Network(seed=0, device="cpu", latent=LATENT, layers=LAYERS)
+    tgt = torch.ones((n, sg.OUT_USED))
+    l0 = float(net.train_step(g, xn, tgt, lr=1e-2))
+    for _ in range(10):
+        l1 = float(net.train_step(g, xn, tgt, lr=1e-2))
+    assert np.isfinite(l1) and l1 < l0
+    # every edge-layer gradient of the last step is zero: no edge contributed
+    for name, shape, off in sg.param_layout(LATENT, LAYERS):
+        if name.startswith("edge") or name.startswith("enc_e"):
+            assert float(net.grad[off:off + int(np.prod(shape))].abs().max()) == 0.0, name
