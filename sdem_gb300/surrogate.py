@@ -23,7 +23,9 @@ no CPU fallback: loading fails loudly when the library is missing.
 SurrogateRunner advances a bed by surrogate strides and, every `judge_every`
 strides, re-advances one stride with the plain FP64 DEM (include/sdem_gpu.h)
 from the surrogate's state as the error judge; when the relative bed-height
-difference exceeds the bound the plain DEM takes over for the next strides.
+difference exceeds the bound, when the plain DEM rejects the state, or when
+the neighbour graph outgrows its limit, the plain DEM takes over for the next
+strides (from its last own state where the surrogate's was rejected).
 """
 from __future__ import annotations
 
@@ -31,7 +33,7 @@ import ctypes as C
 import math
 import os
 from dataclasses import dataclass
-from typing import Dict, List, Optional, Tuple
+from typing import List, Optional, Tuple
 
 import numpy as np
 import torch
