@@ -288,11 +288,18 @@ int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatch
  * fixed-size device array in the library (about 7.3 MB, held by every GPU
  * that loads the library until the process exits), which limits n to
  * SDEM_NOALLOC_MAX_PARTICLES and the grid to SDEM_NOALLOC_MAX_CELLS; larger
- * inputs are refused with SDEM_E_CAPACITY.  The first call on a device looks
- * up the array's device address, so make it before any stream capture.  All
- * calls share the array: calls that overlap on the GPU (other streams or host
- * threads) race.  The call returns after the work on `stream` finished; on
- * failure sdem_last_error(NULL) gives the message. */
+ * inputs are refused with SDEM_E_CAPACITY.  It restates the one-level search
+ * of a bed without periodic directions or fixed spheres: a cfg with
+ * periodic[*] set, cs_method other than SDEM_CSM_NBS_MUNJIZA or
+ * n_fixed_capacity > 0 is refused with SDEM_E_UNSUPPORTED (count such beds
+ * with a handle).  A particle outside the padded grid gives SDEM_E_GRID and no
+ * counts.  The first call on a device looks up the array's device address, so
+ * make that first call before any stream capture.  All calls share the array
+ * and it keeps the last call's contents (each call clears what must start at
+ * zero): calls that overlap on the GPU (other streams or host threads) race.
+ * The call is synchronous: it returns after its work on `stream` has finished
+ * and its status has been read back.  On failure sdem_last_error(NULL) gives
+ * the message. */
 #define SDEM_NOALLOC_MAX_PARTICLES 65536
 #define SDEM_NOALLOC_MAX_CELLS     524288
 int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, const double* d_posR,

@@ -10,6 +10,7 @@ contraction), and the surrogate's graph features as its numpy statement.
 """
 from __future__ import annotations
 
+import hashlib
 import os
 import shutil
 import subprocess
@@ -37,32 +38,59 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the sm_103a library cannot be built")
 
 
-def up_to_date(lib: str = LIB, deps=None) -> bool:
-    deps = DEPS if deps is None else deps
-    if not os.path.exists(lib):
+def _nvcc_version(exe: str) -> str:
+    try:
+        return subprocess.run([exe, "--version"], capture_output=True, text=True, check=True).stdout
+    except (OSError, subprocess.CalledProcessError):
+        return "unknown"
+
+
+def stamp_of(deps, cmd_flags, compiler_version: str) -> str:
+    """Content key of one library: its sources and headers, the flags and the
+    compiler's version string.  A library whose stamp file differs (or is
+    missing) is rebuilt, whatever the files' modification times say."""
+    h = hashlib.sha256()
+    for p in deps:
+        h.update(os.path.basename(p).encode())
+        with open(p, "rb") as f:
+            h.update(hashlib.sha256(f.read()).digest())
+    h.update("\0".join(cmd_flags).encode())
+    h.update(compiler_version.encode())
+    return h.hexdigest()
+
+
+def up_to_date(lib: str, stamp: str) -> bool:
+    try:
+        with open(lib + ".stamp") as f:
+            return os.path.exists(lib) and f.read().strip() == stamp
+    except OSError:
         return False
-    t = os.path.getmtime(lib)
-    return all(os.path.getmtime(p) <= t for p in deps)
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compiles libsdem_gpu.so and libsdem_surrogate.so next to this file
-    (the stale ones, in parallel); returns the path of libsdem_gpu.so."""
+    (those whose content stamp changed, in parallel); returns the path of
+    libsdem_gpu.so."""
+    exe = nvcc()
+    version = _nvcc_version(exe)
     jobs = []
     for src, deps, lib in ((SRC, DEPS, LIB), (SG_SRC, SG_DEPS, SG_LIB)):
-        if not force and up_to_date(lib, deps):
+        stamp = stamp_of(deps, ARCH + FLAGS, version)
+        if not force and up_to_date(lib, stamp):
             continue
         tmp = f"{lib}.{os.getpid()}.tmp"
-        cmd = [nvcc(), *ARCH, *FLAGS, "-o", tmp, src, "-lcudart"]
+        cmd = [exe, *ARCH, *FLAGS, "-o", tmp, src, "-lcudart"]
         if verbose:
             print(" ".join(cmd), flush=True)
-        jobs.append((subprocess.Popen(cmd), cmd, tmp, lib))
+        jobs.append((subprocess.Popen(cmd), cmd, tmp, lib, stamp))
     failed = None
-    for proc, cmd, tmp, lib in jobs:
+    for proc, cmd, tmp, lib, stamp in jobs:
         if proc.wait() != 0:
             failed = failed or subprocess.CalledProcessError(proc.returncode, cmd)
         else:
             os.replace(tmp, lib)
+            with open(lib + ".stamp", "w") as f:
+                f.write(stamp + "\n")
     if failed:
         raise failed
     return LIB

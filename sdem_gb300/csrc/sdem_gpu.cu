@@ -1676,11 +1676,16 @@ __global__ void k_na_begin(NoAllocScratch* S, int n) {
 
 // The search of k_search without its rows: the same half shell, the same
 // single-precision decision with the FP64 test in the ambiguous band; it only
-// counts numCntcts(1) and num_Cnsv_cntct.
+// counts numCntcts(1) and num_Cnsv_cntct.  Only the sort positions this call
+// wrote are searched: a particle outside the grid (SDEM_E_GRID) is not placed,
+// so sorted[cell_start[ncell] .. n) still holds an earlier call's indices,
+// which may lie beyond this call's d_posR.  After a binning error nothing is
+// searched at all.
 __global__ void __launch_bounds__(kThreads) k_na_count(Dev d, unsigned long long* counts) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long cand = 0, hits = 0;
-  if (s < *d.n) {
+  const int placed = d.cell_start[d.ncell];
+  if (d.status[0] == 0 && s < *d.n && s < placed) {
     const int m = d.sorted[s];
     const int key = d.cell_of[m];
     const int iz = key % d.nz;
@@ -3369,20 +3374,43 @@ int sdem_count_contacts_noalloc(const sdem_cfg* cfg, double max_radius, int n, c
   if (n > kNaMaxN)
     return noalloc_fail(SDEM_E_CAPACITY, "sdem_count_contacts_noalloc: more than SDEM_NOALLOC_MAX_PARTICLES "
                                          "(65536) particles");
-  if (((uintptr_t)d_posR & 31u) != 0 || ((uintptr_t)d_counts & 7u) != 0)
+  if (((uintptr_t)d_posR & 31u) != 0)
     return noalloc_fail(SDEM_E_ARG, "sdem_count_contacts_noalloc: d_posR must be 32-byte aligned");
+  if (((uintptr_t)d_counts & 7u) != 0)
+    return noalloc_fail(SDEM_E_ARG, "sdem_count_contacts_noalloc: d_counts must be 8-byte aligned");
+  // The one-level, non-periodic search without fixed spheres is all this
+  // entry point restates; the handle path covers the rest.
+  if (cfg->periodic[0] || cfg->periodic[1] || cfg->periodic[2])
+    return noalloc_fail(SDEM_E_UNSUPPORTED, "sdem_count_contacts_noalloc: periodic directions are not supported");
+  if (cfg->cs_method != SDEM_CSM_NBS_MUNJIZA)
+    return noalloc_fail(SDEM_E_UNSUPPORTED,
+                        "sdem_count_contacts_noalloc: only the one-level search (CS_Method 1) is supported");
+  if (cfg->n_fixed_capacity > 0)
+    return noalloc_fail(SDEM_E_UNSUPPORTED, "sdem_count_contacts_noalloc: fixed spheres are not supported");
   if (!(cfg->cs_ratio >= 1.0))
     return noalloc_fail(SDEM_E_ARG, "sdem_count_contacts_noalloc: Prtcl_cs_ratio must be >= 1");
-  // Init_NBSM grid (Prtcl_NBS_Munjiza.f90:66-77), as sdem_set_types builds it
+  // Init_NBSM grid (Prtcl_NBS_Munjiza.f90:66-77), as sdem_set_types builds it.
+  // The extents are checked in double before any conversion to int: a tiny
+  // cell or a huge or non-finite domain is refused, not cast.
   const double cell = cfg->cs_ratio * (2.0 * max_radius);
+  if (!std::isfinite(cell) || !(cell > 0.0))
+    return noalloc_fail(SDEM_E_ARG, "sdem_count_contacts_noalloc: the search cell is not a positive finite length");
   const double x0 = cfg->dom_min[0] - cell * 1.05, y0 = cfg->dom_min[1] - cell * 1.05, z0 = cfg->dom_min[2] - cell * 1.05;
-  const int nx = (int)((cfg->dom_max[0] + cell * 1.05 - x0) / cell) + 1;
-  const int ny = (int)((cfg->dom_max[1] + cell * 1.05 - y0) / cell) + 1;
-  const int nz = (int)((cfg->dom_max[2] + cell * 1.05 - z0) / cell) + 1;
-  const long long ncell = (long long)nx * ny * nz;
-  if (ncell > kNaMaxCells)
+  const double ext[3] = {std::floor((cfg->dom_max[0] + cell * 1.05 - x0) / cell) + 1.0,
+                         std::floor((cfg->dom_max[1] + cell * 1.05 - y0) / cell) + 1.0,
+                         std::floor((cfg->dom_max[2] + cell * 1.05 - z0) / cell) + 1.0};
+  for (int a = 0; a < 3; a++) {
+    if (!std::isfinite(ext[a]) || !(ext[a] >= 1.0))
+      return noalloc_fail(SDEM_E_ARG, "sdem_count_contacts_noalloc: the domain gives no valid search grid");
+    if (ext[a] > (double)kNaMaxCells)
+      return noalloc_fail(SDEM_E_CAPACITY, "sdem_count_contacts_noalloc: the search grid has more than "
+                                           "SDEM_NOALLOC_MAX_CELLS (524288) cells");
+  }
+  if (ext[0] * ext[1] * ext[2] > (double)kNaMaxCells)
     return noalloc_fail(SDEM_E_CAPACITY, "sdem_count_contacts_noalloc: the search grid has more than "
                                          "SDEM_NOALLOC_MAX_CELLS (524288) cells");
+  const int nx = (int)ext[0], ny = (int)ext[1], nz = (int)ext[2];
+  const long long ncell = (long long)nx * ny * nz;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
     return noalloc_fail(SDEM_E_CUDA, "sdem_count_contacts_noalloc: no usable CUDA device");
