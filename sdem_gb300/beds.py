@@ -369,6 +369,82 @@ def hertz_poly_case(n: int = 1_000_000, seed: int = 2, box=(0.1, 0.6, 0.1), ntyp
                 note="Hertz E=5e7 Pa, nu=0.3, e=0.8, mu=0.4, mu_r=0.1, 41 types d=0.80..1.20 mm")
 
 
+_bedgen = None
+
+
+def _bedgen_lib():
+    """libsdem_bedgen.so (host C, built by sdem_gb300.build)."""
+    global _bedgen
+    if _bedgen is None:
+        import ctypes as C
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsdem_bedgen.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build it with `python -m sdem_gb300.build`")
+        lib = C.CDLL(path)
+        dp = C.POINTER(C.c_double)
+        lib.bedgen_rsp.argtypes = [C.c_int, dp, dp, dp, C.c_ulonglong, C.c_longlong, dp,
+                                   C.POINTER(C.c_longlong), C.POINTER(C.c_int)]
+        lib.bedgen_rsp.restype = C.c_int
+        _bedgen = lib
+    return _bedgen
+
+
+def rsp_positions(radius: np.ndarray, lo, hi, seed: int, max_tries: int = 10_000_000) -> np.ndarray:
+    """Seeded random sequential placement: sphere i (in index order) takes the
+    first uniform random centre in [lo + r_i, hi - r_i] that overlaps no sphere
+    placed before it (sdem_gb300/csrc/bedgen.c).  Raises when one sphere needs
+    more than max_tries proposals."""
+    import ctypes as C
+    lib = _bedgen_lib()
+    r = np.ascontiguousarray(radius, dtype=np.float64)
+    lo_ = np.ascontiguousarray(lo, dtype=np.float64)
+    hi_ = np.ascontiguousarray(hi, dtype=np.float64)
+    pos = np.zeros((len(r), 3))
+    dp = C.POINTER(C.c_double)
+    props_ = C.c_longlong()
+    fail = C.c_int()
+    rc = lib.bedgen_rsp(len(r), r.ctypes.data_as(dp), lo_.ctypes.data_as(dp), hi_.ctypes.data_as(dp),
+                        int(seed) & 0xFFFFFFFFFFFFFFFF, int(max_tries), pos.ctypes.data_as(dp), C.byref(props_),
+                        C.byref(fail))
+    if rc == 2:
+        raise ValueError(f"rsp_positions: sphere {fail.value} found no free place in {max_tries} proposals")
+    if rc:
+        raise ValueError(f"rsp_positions: bad arguments or no memory (code {rc})")
+    return pos
+
+
+def hertz_poly_setup(box=(0.1, 0.6, 0.1), dt: float = 1.0e-6, pi: int = 2, pri: int = 2):
+    """Options and walls of the 1M polydisperse Hertz configuration: Hertz,
+    AB2, dt = 1e-6 s, gravity -y, a floor and four infinite side walls."""
+    opts = Options(dt=dt, minpoint=(0.0, 0.0, 0.0), maxpoint=tuple(box), cf_type=props.CFT_NLIN,
+                   pi_method=pi, pri_method=pri)
+    walls = box_walls(opts.minpoint, opts.maxpoint, infinite=True, base_wall_id=opts.base_wall_id)
+    return opts, walls
+
+
+def hertz_poly_rsp_case(n: int = 1_000_000, seed: int = 2, box=(0.1, 0.6, 0.1), ntypes: int = 41,
+                        fill: float = 0.25, dt: float = 1.0e-6, pi: int = 2, pri: int = 2, **table_kw) -> Case:
+    """The 1M polydisperse Hertz configuration as placed, before settling:
+    d uniform in [0.8, 1.2] mm as `ntypes` discrete types, seeded random
+    sequential placement (rsp_positions) in the bottom of the 0.1 x 0.6 x 0.1 m
+    box, as high as a solid fraction `fill` needs (0.218 m for 1M spheres at
+    0.25), at rest, no contacts.  Floor and four side walls, gravity -y.
+    table_kw passes other material values to hertz_poly_tables."""
+    rng = np.random.default_rng(seed)
+    diam, tables = hertz_poly_tables(ntypes, **table_kw)
+    ptype = rng.integers(1, ntypes + 1, size=n).astype(np.int32)
+    r = tables.radius[ptype - 1]
+    height = float((4.0 / 3.0 * math.pi * r ** 3).sum() / fill / (box[0] * box[2]))
+    if height > box[1]:
+        raise ValueError("hertz_poly_rsp_case: the box is too short for this fill")
+    pos = rsp_positions(r, (0.0, 0.0, 0.0), (box[0], height, box[2]), seed=seed)
+    opts, walls = hertz_poly_setup(box, dt, pi, pri)
+    parts = new_particles(pos, ptype, tables.radius, np.zeros((n, 3)), opts.tsize, opts.rsize)
+    return Case(f"hertz_poly_rsp_{n}", opts, tables, walls, parts,
+                note=f"random sequential placement at solid fraction {fill} up to y={height:.4f} m")
+
+
 def random_cloud_case(n: int, seed: int, box=(0.01, 0.01, 0.01), ntypes: int = 5, cf_type: int = props.CFT_NLIN,
                       d_lo: float = 0.8e-3, d_hi: float = 1.2e-3, vmax: float = 0.3, pi: int = 2, pri: int = 2,
                       dt: float = 1.0e-6, overlap_frac: float = 0.02, density_frac: float = 0.45,

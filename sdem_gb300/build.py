@@ -7,6 +7,8 @@ libsdem_surrogate.so (the learned surrogate, include/sdem_surrogate.h), one
 translation unit each, compiled in parallel with -fmad=false: the force law
 and the integrator must round exactly as the reference's Fortran (no FMA
 contraction), and the surrogate's graph features as its numpy statement.
+libsdem_bedgen.so (host C: the seeded random sequential placement of the
+synthetic beds) is compiled with gcc beside them.
 """
 from __future__ import annotations
 
@@ -25,6 +27,9 @@ LIB = os.path.join(HERE, "libsdem_gpu.so")
 SG_SRC = os.path.join(HERE, "csrc", "surrogate.cu")
 SG_DEPS = [SG_SRC, os.path.join(ROOT, "include", "sdem_surrogate.h")]
 SG_LIB = os.path.join(HERE, "libsdem_surrogate.so")
+BG_SRC = os.path.join(HERE, "csrc", "bedgen.c")
+BG_LIB = os.path.join(HERE, "libsdem_bedgen.so")
+BG_FLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
@@ -67,19 +72,27 @@ def up_to_date(lib: str, stamp: str) -> bool:
         return False
 
 
+def _cc() -> str:
+    return os.environ.get("CC") or shutil.which("gcc") or "cc"
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles libsdem_gpu.so and libsdem_surrogate.so next to this file
-    (those whose content stamp changed, in parallel); returns the path of
-    libsdem_gpu.so."""
+    """Compiles libsdem_gpu.so, libsdem_surrogate.so and libsdem_bedgen.so
+    next to this file (those whose content stamp changed, in parallel);
+    returns the path of libsdem_gpu.so."""
     exe = nvcc()
     version = _nvcc_version(exe)
+    cc = _cc()
+    specs = [(SRC, DEPS, LIB, [exe, *ARCH, *FLAGS], ["-lcudart"], ARCH + FLAGS, version),
+             (SG_SRC, SG_DEPS, SG_LIB, [exe, *ARCH, *FLAGS], ["-lcudart"], ARCH + FLAGS, version),
+             (BG_SRC, [BG_SRC], BG_LIB, [cc, *BG_FLAGS], ["-lm"], BG_FLAGS, _nvcc_version(cc))]
     jobs = []
-    for src, deps, lib in ((SRC, DEPS, LIB), (SG_SRC, SG_DEPS, SG_LIB)):
-        stamp = stamp_of(deps, ARCH + FLAGS, version)
+    for src, deps, lib, head, tail, flags, ver in specs:
+        stamp = stamp_of(deps, flags, ver)
         if not force and up_to_date(lib, stamp):
             continue
         tmp = f"{lib}.{os.getpid()}.tmp"
-        cmd = [exe, *ARCH, *FLAGS, "-o", tmp, src, "-lcudart"]
+        cmd = [*head, "-o", tmp, src, *tail]
         if verbose:
             print(" ".join(cmd), flush=True)
         jobs.append((subprocess.Popen(cmd), cmd, tmp, lib, stamp))
