@@ -6,15 +6,16 @@ Modules:
   geometry  plane walls (G_add_PlaneWall restated)
   beds      seeded synthetic beds (the workloads)
   restart   reader/writer of the reference's restart file layout
+  settle    gravity settling of a placed bed by the GPU path (the settled 1M bed)
   build     nvcc recipe of the native library
 """
 from . import beds, geometry, props  # noqa: F401
 
-__all__ = ["beds", "geometry", "props", "capi", "build"]
+__all__ = ["beds", "geometry", "props", "capi", "build", "restart", "settle"]
 
 
 def __getattr__(name):
-    if name in ("capi", "build", "restart"):
+    if name in ("capi", "build", "restart", "settle"):
         import importlib
         return importlib.import_module(f".{name}", __name__)
     raise AttributeError(name)
