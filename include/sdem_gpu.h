@@ -114,7 +114,9 @@ typedef struct sdem_cfg {
   int    wall_max_update_iter;  /* Wall_max_update_iter                              */
   int    periodic[3];           /* IsPeriodic; each periodic side > 2 search cells   */
   int    quirk_ab2_rot;         /* 1: AB2 rotation starts from linVel (Prtcl_Integration.f90:64) */
-  int    max_contacts_per_particle; /* GPU row capacity per particle, 0 = default (24), <= 64 */
+  int    max_contacts_per_particle; /* GPU row capacity per particle, 0 = default (24), <= 64; for
+                                       radii ratio q = rmax/rmin, 3.63*(1+q)^2 bounds the spheres
+                                       that can touch the largest one (59 at q = 3)           */
   double dt;                    /* dtDEM                                             */
   double gravity[3];
   double dom_min[3], dom_max[3];/* SimDomain_min/max (the whole domain on one rank)  */
@@ -273,6 +275,12 @@ const char* sdem_profile_phase_name(int i);
  * device; *mismatches receives the number of pairs whose results differ in
  * any bit (0 expected). */
 int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatches);
+
+/* Measures the FP64 pipe: a kernel of eight independent DFMA chains per
+ * thread (8 blocks of 256 threads per SM) runs `iters` iterations on the
+ * current device; *dfma_per_s receives the executed DFMA per second (one DFMA
+ * is two floating-point operations) and *ms the kernel's CUDA-event time. */
+int sdem_probe_fp64_peak(long long iters, double* dfma_per_s, double* ms);
 
 /* ---- allocation-free contact count (no counterpart in the reference) ------
  * For callers that cannot allocate device memory -- a host running inside

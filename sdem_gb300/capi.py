@@ -7,6 +7,7 @@ when the library is missing: there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 from typing import Optional
 
@@ -28,7 +29,7 @@ EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls
             "sdem_download_particles", "sdem_download_contacts", "sdem_check_restart_limit",
             "sdem_download_forces", "sdem_counters", "sdem_counters_lagged", "sdem_counter_sums",
             "sdem_launch_count", "sdem_profile_begin", "sdem_profile_end", "sdem_profile_phase_name",
-            "sdem_count_contacts_noalloc", "sdem_selftest_fp64",
+            "sdem_count_contacts_noalloc", "sdem_selftest_fp64", "sdem_probe_fp64_peak",
             "sdem_snapshot_begin", "sdem_snapshot_end", "sdem_snapshot_contacts", "sdem_set_fixed", "sdem_last_error",
             "sdem_destroy", "sdem_batch_create", "sdem_batch_step_async", "sdem_batch_sync", "sdem_batch_step",
             "sdem_batch_last_error", "sdem_batch_destroy")
@@ -64,6 +65,20 @@ class SdemError(RuntimeError):
         self.code = code
 
 
+def row_capacity_for(radius) -> int:
+    """Contacts per sphere the handle makes room for when a case leaves
+    max_contacts_per_particle at 0: the library's default of 24, or more when
+    the radii differ enough that a large sphere can touch more small ones.
+    A sphere of radius R touched by spheres of radius r holds at most about
+    4 pi (R + r)^2 / (2 sqrt(3) r^2) = 3.63 (1 + R/r)^2 of them (hexagonal
+    cover of the sphere their centres lie on); capped at the library's 64."""
+    r = np.asarray(radius, dtype=np.float64)
+    if r.size == 0 or not (r.min() > 0.0):
+        return 24
+    q = float(r.max() / r.min())
+    return int(min(64, max(24, math.ceil(3.63 * (1.0 + q) ** 2))))
+
+
 def cfg_from_case(case: Case, n_capacity: Optional[int] = None, max_gid: Optional[int] = None) -> SdemCfg:
     o = case.opts
     c = SdemCfg()
@@ -82,7 +97,7 @@ def cfg_from_case(case: Case, n_capacity: Optional[int] = None, max_gid: Optiona
         c.dom_min[k] = o.minpoint[k]
         c.dom_max[k] = o.maxpoint[k]
     c.quirk_ab2_rot = int(o.quirk_ab2_rot)
-    c.max_contacts_per_particle = int(o.max_contacts_per_particle)
+    c.max_contacts_per_particle = int(o.max_contacts_per_particle) or row_capacity_for(case.tables.radius)
     c.dt = o.dt
     c.cs_ratio = o.cs_ratio
     c.wall_neighbor_ratio = o.wall_neighbor_ratio
@@ -131,6 +146,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_profile_phase_name.restype = C.c_char_p
     lib.sdem_count_contacts_noalloc.argtypes = [C.POINTER(SdemCfg), C.c_double, C.c_int, P, P, P]
     lib.sdem_selftest_fp64.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
+    lib.sdem_probe_fp64_peak.argtypes = [C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.sdem_snapshot_begin.argtypes = [P, ip, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp, C.c_int]
     lib.sdem_snapshot_end.argtypes = [P, ip]
     lib.sdem_snapshot_contacts.argtypes = [P, C.c_int, ip, ip, ip, dp, dp]
@@ -170,6 +186,17 @@ def iptr(a: Optional[np.ndarray]):
 
 NOALLOC_MAX_PARTICLES = 65536
 NOALLOC_MAX_CELLS = 524288
+
+
+def probe_fp64_peak(iters: int = 20000) -> dict:
+    """sdem_probe_fp64_peak: DFMA chains on every SM; returns the measured
+    DFMA/s, FP64 TFLOP/s (2 per DFMA) and the kernel time."""
+    lib = load()
+    r, ms = C.c_double(), C.c_double()
+    rc = lib.sdem_probe_fp64_peak(int(iters), C.byref(r), C.byref(ms))
+    if rc:
+        raise SdemError(rc, "sdem_probe_fp64_peak failed")
+    return {"dfma_per_s": r.value, "tflops": 2.0 * r.value / 1e12, "ms": ms.value}
 
 
 def count_contacts_noalloc(cfg: SdemCfg, max_radius: float, n: int, d_posR: int, d_counts: int,

@@ -1485,6 +1485,20 @@ __global__ void k_selftest_fp64(long long n, unsigned long long seed, unsigned l
   if (nb) atomicAdd(bad, nb);
 }
 
+// FP64 pipe probe: eight independent DFMA chains per thread, so issue, not
+// latency, limits the rate.  The result is written only when it is zero
+// (never, for these operands), which keeps the chains alive.
+__global__ void __launch_bounds__(256) k_probe_dfma(long long iters, double b, double c, double* sink) {
+  double a0 = threadIdx.x * 1e-3 + 1.0, a1 = a0 + 0.1, a2 = a0 + 0.2, a3 = a0 + 0.3;
+  double a4 = a0 + 0.4, a5 = a0 + 0.5, a6 = a0 + 0.6, a7 = a0 + 0.7;
+  for (long long i = 0; i < iters; i++) {
+    a0 = __fma_rn(a0, b, c); a1 = __fma_rn(a1, b, c); a2 = __fma_rn(a2, b, c); a3 = __fma_rn(a3, b, c);
+    a4 = __fma_rn(a4, b, c); a5 = __fma_rn(a5, b, c); a6 = __fma_rn(a6, b, c); a7 = __fma_rn(a7, b, c);
+  }
+  const double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 0.0) sink[blockIdx.x] = s;
+}
+
 // Contact snapshot (asynchronous output): the records of the last step and
 // each particle's wall records, frozen so that later steps may run while the
 // copy travels to the host.
@@ -3495,6 +3509,39 @@ int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatch
   cudaFree(bad);
   if (e != cudaSuccess) return SDEM_E_CUDA;
   *mismatches = (long long)hb;
+  return 0;
+}
+
+int sdem_probe_fp64_peak(long long iters, double* dfma_per_s, double* ms) {
+  if (iters <= 0 || !dfma_per_s || !ms) return SDEM_E_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return SDEM_E_CUDA;
+  const int blocks = sms * 8, threads = 256;
+  double* sink = nullptr;
+  if (cudaMalloc(&sink, sizeof(double) * blocks) != cudaSuccess) {
+    cudaGetLastError();
+    return SDEM_E_NOMEM;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  float t = 0.f;
+  if (e == cudaSuccess) {
+    k_probe_dfma<<<blocks, threads>>>(iters / 8 + 1, 0.999999, 1e-7, sink);   // warm-up
+    cudaEventRecord(e0);
+    k_probe_dfma<<<blocks, threads>>>(iters, 0.999999, 1e-7, sink);
+    cudaEventRecord(e1);
+    e = cudaEventSynchronize(e1);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (e != cudaSuccess || !(t > 0.f)) return SDEM_E_CUDA;
+  *ms = t;
+  *dfma_per_s = 8.0 * (double)iters * blocks * threads / (t * 1e-3);
   return 0;
 }
 
