@@ -1,16 +1,23 @@
 #!/usr/bin/env python
-"""Throughput of the GB300 sDEM hot path: particle-steps/s on the 1M-sphere
-polydisperse Hertz bed.
+"""Throughput of the GB300 sDEM hot path: particle-steps/s.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+                  [--workload hertz_poly_1m | hertz_poly_1m_deposited | lsd_mono_20k | hopper_4m
+                              | sandboxes | surrogate]
+
+The headline workload (hertz_poly_1m) is the 1M-sphere polydisperse Hertz
+bed settled under gravity (seeded random sequential placement, settled by
+the GPU path itself and cached on disk; make_case below).
 
 Our arm: one DEMSystem per GPU (replicas: each rank advances its own
 independent bed, no collective on the data path), W untimed steps, then K
 timed steps (CUDA events on the library's stream, barrier + synchronize on both
-sides, max over ranks).  The bed (~300 MB of state) is larger than L2, so no
-flush is needed between steps.  e2e: the same metric through the C ABI with
-host buffers: upload of the state, K host-synchronous sdem_step(h,1) calls
-each followed by a counters read-back, download of the state.
+sides, max over ranks).  The 1M bed (~300 MB of state) is larger than L2, so
+no flush is needed between steps.  e2e: the same metric through the C ABI
+with host buffers: upload of the state, K sdem_step_async(h,1) calls each
+followed by a read-back of the step's counters, download of the state; once
+with page-locked host arrays (e2e) and once with ordinary ones
+(e2e_pageable).
 
 --impl reference: the CPU restatement of the reference's algorithm (the
 reference's Fortran+MPI build cannot be compiled here or on the GPU host: no
@@ -37,18 +44,72 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s, 1M Hertz spheres"
 UNIT = "particle-steps/s"
-WORKLOAD = "hertz_poly_1m"
-MEASURED_FP64_TFLOPS = 1.198   # DFMA-chain probe on GB300 (2 flops per DFMA)
-# From the ncu captures in profiles/k_force_search_gather_hertz_poly_500k.txt:
-FORCE_DRAM_BYTES_PER_CONTACT = 394.0     # dram__bytes_read.sum + dram__bytes_write.sum per contact
-FORCE_FP64_INST_PER_CONTACT = 133.8      # DADD + DMUL + DFMA thread instructions per contact
-FP64_INST_PER_SM_CLK = 2.0               # sm__sass_thread_inst_executed_op_dfma_pred_on peak per SM
+# From the ncu captures in profiles/ (each file gives its command):
+FORCE_DRAM_BYTES_PER_CONTACT = 394.0     # k_force: dram__bytes_read.sum + dram__bytes_write.sum per contact
+FP64_INST_PER_SM_CLK = 2.0               # DADD/DMUL/DFMA thread operations per SM per clock (FP64 pipe)
 NUM_SMS = 152
+# Executed DADD + DMUL + DFMA thread instructions of the step's kernels
+# (profiles/fp64_counts_hertz_poly_settled.txt), modelled per particle-particle
+# contact, per sphere and per wall contact.
+FP64_PER_CONTACT = {"k_force": 133.8, "k_gather": 24.0}
+FP64_PER_SPHERE = {"k_integrate": 57.0, "k_gather": 2.3, "k_bin": 6.0, "k_wall_detect": 0.6}
+FP64_PER_WALL_CONTACT = {"k_wall_force": 120.0}
+
+# name -> (metric, default particles, base seed)
+WORKLOADS = {
+    "hertz_poly_1m": (METRIC, 1_000_000, 2),
+    "hertz_poly_1m_deposited": ("particle-steps/s, 1M Hertz spheres (deposited bed)", 1_000_000, 2),
+    "lsd_mono_20k": ("particle-steps/s, 20k LSD spheres", 20_000, 1),
+    "hopper_4m": ("particle-steps/s, 4M bidisperse Hertz hopper", 4_000_000, 3),
+}
 
 
-def make_case(n: int, seed: int):
+def make_case(workload: str, n: int, seed: int):
+    """The bed of a workload and a description of it for the JSON line.
+
+    hertz_poly_1m: the 1M polydisperse Hertz configuration (d uniform in
+      [0.8, 1.2] mm as 41 types, E 5e7 Pa, restitution 0.8, friction 0.4,
+      dt 1e-6 s, AB2, 0.1 x 0.6 x 0.1 m box, five walls): seeded random
+      sequential placement settled under gravity on the GPU
+      (sdem_gb300.settle; cached on disk after the first run).
+    hertz_poly_1m_deposited: the same material on a geometric deposition
+      (sdem_gb300.beds.hertz_poly_case), about one resting contact per sphere.
+    lsd_mono_20k: 20,000 monodisperse LSD spheres (restitution 0.9, friction
+      0.3, dt 2e-6 s, AB2) from the seeded jittered lattice, after 10,000 GPU
+      steps of settling (half the configuration's 20,000).
+    hopper_4m: 4,000,000 bidisperse Hertz spheres (0.5 / 1.5 mm, 70:30,
+      friction 0.5, restitution 0.7, dt 5e-7 s) in a hopper of four 60-degree
+      finite planes over a 10 mm square outlet (0.26 m wide, a column above);
+      after 1,000 GPU steps of discharge."""
     from sdem_gb300 import beds
-    return beds.hertz_poly_case(n=n, seed=seed)
+    if workload == "hertz_poly_1m":
+        from sdem_gb300 import settle
+        case = settle.settled_hertz_poly_case(n=n, seed=seed)
+        log = json.loads(case.note)["settling"]
+        last = log[-1]
+        desc = {"bed": f"seeded random sequential placement (seed {seed}, solid fraction 0.25) settled under "
+                       f"gravity by the GPU path (sdem_gb300.settle: {sum(e['steps'] for e in log)} steps in "
+                       f"{len(log)} stages)",
+                "bed_height_m": last["height"], "bed_v_mean_mps": last["v_mean"], "bed_v_max_mps": last["v_max"]}
+        return case, desc
+    if workload == "hertz_poly_1m_deposited":
+        return beds.hertz_poly_case(n=n, seed=seed), {
+            "bed": f"seeded geometric deposition (seed {seed}, sdem_gb300.beds.hertz_poly_case)"}
+    from sdem_gb300.capi import DEMSystem
+    if workload == "lsd_mono_20k":
+        case0 = beds.lsd_mono_case(n=n, seed=seed)
+        prep = 10000
+        desc = {"bed": f"seeded jittered lattice (seed {seed}) after {prep} GPU steps of settling"}
+    elif workload == "hopper_4m":
+        case0 = beds.hopper_case(n, seed, width=0.26, outlet=10.0e-3)
+        prep = 1000
+        desc = {"bed": f"hopper filled on a jittered lattice (seed {seed}) after {prep} GPU steps of discharge"}
+    else:
+        raise ValueError(workload)
+    with DEMSystem(case0) as h:
+        h.step(prep)
+        case = beds.Case(case0.name, case0.opts, case0.tables, case0.walls, h.state(), contacts=h.contacts())
+    return case, desc
 
 
 # ---------------------------------------------------------------------------
@@ -192,18 +253,72 @@ def reference_arm(args):
     ws, rank, _ = dist_setup()
     if rank != 0:
         return
-    case = make_case(1_000_000, 2)
+    metric, n_def, seed = WORKLOADS[args.workload]
+    # the bed is the one our arm times (the settled bed is prepared on the GPU
+    # once and cached; the timed region below is CPU only)
+    case, desc = make_case(args.workload, args.n or n_def, seed)
     procs = os.cpu_count() or 1
     rate, cores, sample = cpu_leg(case, steps=args.steps, warm=args.warmup, procs=procs)
-    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+    line = {"impl": "reference", "metric": metric, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * case.particles.n / rate,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_particles": case.particles.n, "parallelism": f"{cores} processes"},
+            "config": {"workload": args.workload, "n_particles": case.particles.n, **desc,
+                       "parallelism": f"{cores} processes"},
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": "CPU restatement of the reference (oracle/sdem_oracle.c), not the reference "
                                        "itself: " + sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+STATE_FIELDS = ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta", "rotVel", "rotAcc")
+
+
+def e2e_run(case, K, pinned: bool, barrier):
+    """The metric through the C ABI with host buffers: upload of the state,
+    K x (sdem_step_async(h,1) + the step's counters read back), download of
+    the state.  pinned: page-locked host arrays; else ordinary (pageable)
+    numpy arrays, what a Fortran caller's arrays are unless it registers
+    them.  Returns (elapsed s, h2d bytes, d2h bytes)."""
+    import torch
+    from sdem_gb300 import beds
+    from sdem_gb300.capi import DEMSystem
+    sys2 = DEMSystem(case)
+    sys2.step(1)
+    st0 = sys2.state()
+    if pinned:
+        st = pinned_particles(st0)
+        out_buf = pinned_particles(st0, rows=sys2.cfg.n_capacity)
+    else:
+        st = st0
+        cap = sys2.cfg.n_capacity
+        out_buf = beds.Particles(*(np.zeros((cap,) + getattr(st0, f).shape[1:], dtype=getattr(st0, f).dtype)
+                                   for f in STATE_FIELDS))
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sys2.upload(st)
+    sys2.step_async(1)
+    for k in range(1, K + 1):
+        if k < K:
+            sys2.step_async(1)          # step k+1 is queued ...
+            sys2.counters_lagged()      # ... while step k's counters are read
+        else:
+            sys2.counters()
+    out = sys2.state(out=out_buf)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    h2d = sum(getattr(st, f).nbytes for f in STATE_FIELDS)
+    d2h = sum(getattr(out, f).nbytes for f in STATE_FIELDS) + K * 4 * 9
+    sys2.close()
+    return el, h2d, d2h
+
+
+def fp64_step_model(C: float, n: int, pw: float) -> float:
+    """Executed FP64 thread instructions of one step from the per-kernel
+    counts measured by ncu (the constants above)."""
+    return (C * sum(FP64_PER_CONTACT.values()) + n * sum(FP64_PER_SPHERE.values())
+            + pw * sum(FP64_PER_WALL_CONTACT.values()))
 
 
 def our_arm(args):
@@ -224,10 +339,12 @@ def our_arm(args):
 
     from sdem_gb300 import build
     build.build()
-    from sdem_gb300.capi import DEMSystem
-    seed = replicas.rank_seed(2, rank)
-    case = make_case(args.n, seed)
+    from sdem_gb300.capi import DEMSystem, probe_fp64_peak
+    metric, n_def, base_seed = WORKLOADS[args.workload]
+    seed = replicas.rank_seed(base_seed, rank)
+    case, desc = make_case(args.workload, args.n or n_def, seed)
     n = case.particles.n
+    fp64_peak = probe_fp64_peak()          # the FP64 pipe of this GPU, measured now (DFMA chains)
     sysm = DEMSystem(case)
     sysm.step(args.warmup)
     stream = torch.cuda.ExternalStream(sysm.stream())
@@ -273,51 +390,31 @@ def our_arm(args):
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     # DRAM bytes of k_force per contact from one ncu capture of the same kernel
-    # on the 500k-sphere bed (profiles/k_force_search_gather_hertz_poly_500k.txt),
-    # scaled to this launch by its contacts
+    # (profiles/), scaled to this launch by its contacts
     traffic = FORCE_DRAM_BYTES_PER_CONTACT * C
     # algorithmic FP64 operations of k_force per Hertz contact (force law + normal
     # vector; the two r*Moment scalings are the gather's): 121 add/sub/mul,
     # 8 sqrt, 7 divisions, each sqrt/div counted as one operation
     fp64_per_contact = 136
     t_step = ms / K * 1e-3
-    step_bytes = n * 352.0 + C * 80.0 + 4.0 * 0   # per-step algorithmic bytes of the whole path
+    step_bytes = n * 352.0 + C * 80.0   # per-step algorithmic bytes of the whole path
 
-    # e2e: through the C ABI with host buffers
-    e2e = None
+    e2e = e2e_pageable = None
     if args.e2e_steps < 0:
         args.e2e_steps = K      # the same number of steps as the device-timed run
     if args.e2e_steps > 0:
-        sys2 = DEMSystem(case)
-        sys2.step(1)
-        st = pinned_particles(sys2.state())                # the step's inputs, in pinned host memory
-        out_buf = pinned_particles(sys2.state(), rows=sys2.cfg.n_capacity)
         Ke = args.e2e_steps
-        barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        sys2.upload(st)
-        sys2.step_async(1)
-        for k in range(1, Ke + 1):
-            if k < Ke:
-                sys2.step_async(1)          # step k+1 is queued ...
-                sys2.counters_lagged()      # ... while step k's counters are read
-            else:
-                sys2.counters()
-        out = sys2.state(out=out_buf)
-        torch.cuda.synchronize()
-        el = time.perf_counter() - t0
-        _, el, _ = replicas.aggregate(el, n, Ke, device="cuda")
-        h2d = sum(getattr(st, f).nbytes for f in ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta",
-                                                  "rotVel", "rotAcc"))
-        d2h = sum(getattr(out, f).nbytes for f in ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta",
-                                                   "rotVel", "rotAcc")) + Ke * 32
-        e2e = {"value": n_all * Ke / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / Ke),
-               "d2h_bytes_per_step": int(d2h / Ke), "steps": Ke,
-               "note": "upload of the state from pinned host memory, K x (sdem_step_async(h,1) + the counters of "
-                       "each step read back: sdem_counters_lagged while the next step runs, sdem_counters after "
-                       "the last), download of the state into pinned host memory"}
-        sys2.close()
+        runs = {}
+        for pinned in (True, False):
+            el, h2d, d2h = e2e_run(case, Ke, pinned, barrier)
+            _, el, _ = replicas.aggregate(el, n, Ke, device="cuda")
+            runs[pinned] = {"value": n_all * Ke / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / Ke),
+                            "d2h_bytes_per_step": int(d2h / Ke), "steps": Ke}
+        e2e = dict(runs[True], note="upload of the state from page-locked host memory, K x (sdem_step_async(h,1) "
+                   "+ the counters of each step read back: sdem_counters_lagged while the next step runs, "
+                   "sdem_counters after the last), download of the state into page-locked host memory")
+        e2e_pageable = dict(runs[False], note="the same with ordinary (pageable) host arrays, as an unmodified "
+                            "Fortran caller passes them")
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -328,31 +425,43 @@ def our_arm(args):
     if rank == 0:
         clocks = clk.summary()
         clk_mhz = float(clocks.get("sm_mhz") or 2070.0)
+        pipe_peak = FP64_INST_PER_SM_CLK * NUM_SMS * clk_mhz * 1e6     # FP64 thread ops per second
+        step_ops = fp64_step_model(C, n, PW_avg)
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
+            "metric": metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
             "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_particles": n, "contact_model": "Hertz-Mindlin",
-                       "types": int(case.tables.n_types), "dt": case.opts.dt, "integrator": "AB2",
+            "config": {"workload": args.workload, "n_particles": n,
+                       "contact_model": "Hertz-Mindlin" if case.opts.cf_type == 2 else "linear spring-dashpot",
+                       "types": int(case.tables.n_types), "dt": case.opts.dt,
+                       "integrator": {1: "FE", 2: "AB2", 3: "AB3"}[case.opts.pi_method],
                        "pp_contacts_avg": C, "pw_contacts_avg": PW_avg, "contacts_per_particle": C / n,
-                       "pp_contacts_last": cnt["pp"],
-                       "bed": "seeded deposited packing (seed 2+rank), see sdem_gb300.beds.hertz_poly_case",
-                       "l2": "state > L2 (no flush)", "parallelism": f"replicas x{ws}"},
+                       "pp_contacts_last": cnt["pp"], **desc,
+                       "l2": "state > L2 (no flush)" if n >= 500_000 else "state < L2 (no flush)",
+                       "parallelism": f"replicas x{ws}"},
             "e2e": e2e,
+            "e2e_pageable": e2e_pageable,
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic,
                          "algorithmic_bytes": "80 B per contact x contacts per launch",
-                         "note": "k_force is FP64-ALU bound on GB300, see fp64 below"},
+                         "peak_note": "hbm_gbs of measured (MEASURED_PEAKS.json)",
+                         "note": "k_force is FP64-ALU bound on GB300, see fp64 and step_fp64"},
             "fp64": {"kernel": "k_force", "achieved_tflops": fp64_per_contact * C / t_force / 1e12,
-                     "peak_tflops": MEASURED_FP64_TFLOPS, "frac": fp64_per_contact * C / t_force / 1e12 /
-                     MEASURED_FP64_TFLOPS,
+                     "peak_tflops": fp64_peak["tflops"],
+                     "frac": fp64_per_contact * C / t_force / 1e12 / fp64_peak["tflops"],
                      "algorithmic_ops_per_contact": fp64_per_contact,
-                     "executed_inst_per_contact": FORCE_FP64_INST_PER_CONTACT,
-                     "pipe_frac": FORCE_FP64_INST_PER_CONTACT * C / t_force /
-                     (FP64_INST_PER_SM_CLK * NUM_SMS * clk_mhz * 1e6),
-                     "note": "pipe_frac: executed DADD/DMUL/DFMA per second over the pipe's peak "
-                             "(2 per SM per clock) at the sampled SM clock"},
+                     "executed_inst_per_contact": FP64_PER_CONTACT["k_force"],
+                     "pipe_frac": FP64_PER_CONTACT["k_force"] * C / t_force / pipe_peak,
+                     "note": "peak: DFMA chains measured in this run (sdem_probe_fp64_peak, 2 flops per DFMA); "
+                             "pipe_frac: executed DADD/DMUL/DFMA per second over the pipe's 2 per SM per clock "
+                             "at the sampled SM clock"},
+            "step_fp64": {"executed_per_step": step_ops, "achieved_per_s": step_ops / t_step,
+                          "pipe_peak_per_s": pipe_peak, "frac": step_ops / t_step / pipe_peak,
+                          "probe_dfma_per_s": fp64_peak["dfma_per_s"],
+                          "note": "executed DADD+DMUL+DFMA of every step kernel (ncu counts per contact, per "
+                                  "sphere and per wall contact, profiles/) over ms_per_step, against the FP64 "
+                                  "pipe's 2 per SM per clock x 152 SMs at the sampled SM clock"},
             "step_roofline": {"achieved": step_bytes / t_step / 1e9, "peak": hbm, "unit": "GB/s",
                               "frac": step_bytes / t_step / 1e9 / hbm,
                               "algorithmic_bytes": "352 B per particle + 80 B per contact per step"},
@@ -457,7 +566,7 @@ def surrogate_arm(args):
     t_train = time.perf_counter() - t0
     mse, mse_free = sg.evaluate(net, held)
 
-    case = make_case(args.n, 2)
+    case, _ = make_case("hertz_poly_1m_deposited", args.n or 1_000_000, 2)
     dem = DEMSystem(case)
     dem.step(args.warmup)
     dmax = 2.0 * float(case.tables.radius.max())
@@ -574,13 +683,14 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--n", type=int, default=0, help="particles (default: the workload's)")
     ap.add_argument("--e2e-steps", type=int, default=-1,
                     help="steps of the end-to-end run (default: --steps; 0 skips it)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="hertz_poly_1m", choices=["hertz_poly_1m", "sandboxes", "surrogate"],
-                    help="sandboxes: the batched workload; surrogate: the learned surrogate against the plain "
-                         "DEM (each its own line; not the headline)")
+    ap.add_argument("--workload", default="hertz_poly_1m", choices=[*WORKLOADS, "sandboxes", "surrogate"],
+                    help="hertz_poly_1m (the headline), hertz_poly_1m_deposited, lsd_mono_20k, hopper_4m; "
+                         "sandboxes: the batched workload; surrogate: the learned surrogate against the plain "
+                         "DEM (each its own line)")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--train-beds", type=int, default=3)
     ap.add_argument("--train-iters", type=int, default=300)

@@ -54,3 +54,41 @@ def compare_history(a: dict, b: dict, rtol: float, atol_tan: float = 1e-25):
 
 def force_scale(F: np.ndarray, floor: float) -> np.ndarray:
     return np.maximum(np.abs(F).max(axis=1), floor)
+
+
+def sorted_contacts(system):
+    """(keys, history) of the live contact list, keys = (listing id, partner
+    or wall id) packed in 64 bits, sorted; vectorised for millions of records."""
+    ids = system.state().id.astype(np.int64)
+    o, q, t, v = system.contacts()
+    key = (ids[o] << 32) | (np.asarray(q, np.int64) & 0xFFFFFFFF)
+    order = np.argsort(key, kind="stable")
+    hist = np.concatenate([np.asarray(t, float), np.asarray(v, float)[:, None]], axis=1)
+    return key[order], hist[order]
+
+
+def assert_step_matches(g, o, rtol: float = 1e-12, what: str = ""):
+    """After one step of a GPU system g and an oracle system o from identical
+    inputs: counters equal, contact sets equal, history, forces and torques
+    within rtol relative, ids equal, positions within 1e-13 relative."""
+    cg, co = g.counters(), o.counters()
+    for k in ("pp", "pw", "cnsv", "nlocal"):
+        assert cg[k] == co[k], f"{what}: counter {k}: gpu {cg[k]} oracle {co[k]}"
+    kg, hg = sorted_contacts(g)
+    ko, ho = sorted_contacts(o)
+    assert len(np.unique(kg)) == len(kg), f"{what}: a contact is listed twice"
+    np.testing.assert_array_equal(kg, ko, err_msg=f"{what}: contact sets")
+    sc = np.maximum(np.maximum(np.abs(hg[:, :3]).max(axis=1), np.abs(ho[:, :3]).max(axis=1)), 1e-25)
+    assert (np.abs(hg[:, :3] - ho[:, :3]).max(axis=1) <= rtol * sc).all(), f"{what}: tangential history"
+    sv = np.maximum(np.maximum(np.abs(hg[:, 3]), np.abs(ho[:, 3])), 1e-300)
+    assert (np.abs(hg[:, 3] - ho[:, 3]) <= rtol * sv).all(), f"{what}: VelRel_Init"
+    Fg, Tg = g.forces()
+    Fo, To = o.forces()
+    fs = force_scale(Fo, 1e-6 * max(np.abs(Fo).max(), 1e-30))
+    ts = force_scale(To, 1e-6 * max(np.abs(To).max(), 1e-30))
+    assert np.all(np.abs(Fg - Fo).max(axis=1) <= rtol * fs), f"{what}: force mismatch"
+    assert np.all(np.abs(Tg - To).max(axis=1) <= rtol * ts), f"{what}: torque mismatch"
+    sg, so = g.state(), o.state()
+    np.testing.assert_array_equal(sg.id, so.id)
+    np.testing.assert_allclose(sg.posR, so.posR, rtol=1e-13, atol=1e-18)
+    return {"pp": cg["pp"], "pw": cg["pw"], "contacts": len(kg)}
