@@ -499,15 +499,17 @@ int orc_upload_particles(orc* h, int n, const int* id, const int* ptype,
 }
 
 /* CL_Add_RestartCntctlink, Prtcl_CL_and_CF.f90:577-622, for one owner. */
+/* The partner's index is the first i with id(i) == gid2, as the reference's
+ * linear search finds it (Prtcl_CL_and_CF.f90:590-595); first_of[gid] holds
+ * that index (0: none), built once per upload so that a restart of millions
+ * of contacts does not search the particle list for each. */
 static int add_restart_links(orc* h, int pid1, int ncv, const int* CntctVec,
-                             const r3* tan, const double* vr) {
-  int nlocal = h->nlocal;
+                             const r3* tan, const double* vr, const int* first_of, int max_gid) {
   int gid1 = h->id[pid1];
   for (int j = 0; j < ncv; j++) {
     int pid2 = 0, gid2 = CntctVec[j];
     double dist = 0.0;
-    for (int i = 1; i <= nlocal; i++)
-      if (h->id[i] == gid2) { pid2 = i; break; }
+    if (gid2 >= 1 && gid2 <= max_gid) pid2 = first_of[gid2];
     if (pid2 > 0) {
       double dx = h->PosR[pid1].x - h->PosR[pid2].x;
       double dy = h->PosR[pid1].y - h->PosR[pid2].y;
@@ -537,6 +539,12 @@ static int add_restart_links(orc* h, int pid1, int ncv, const int* CntctVec,
 /* Records must be grouped by owner (consecutive), as PIO_RestartCL reads them. */
 int orc_upload_contacts(orc* h, int nc, const int* owner_idx, const int* partner_id,
                         const double* tandelta, const double* velrel) {
+  int max_gid = 0;
+  for (int i = 1; i <= h->nlocal; i++)
+    if (h->id[i] > max_gid) max_gid = h->id[i];
+  int* first_of = (int*)xcalloc((size_t)max_gid + 1, sizeof(int));
+  for (int i = h->nlocal; i >= 1; i--)
+    if (h->id[i] >= 1) first_of[h->id[i]] = i;
   int a = 0;
   while (a < nc) {
     int b = a;
@@ -551,12 +559,13 @@ int orc_upload_contacts(orc* h, int nc, const int* owner_idx, const int* partner
       vr[j] = velrel[a + j];
     }
     int pid1 = owner_idx[a] + 1;
-    int rc = (pid1 >= 1 && pid1 <= h->nlocal) ? add_restart_links(h, pid1, ncv, vec, tan, vr)
+    int rc = (pid1 >= 1 && pid1 <= h->nlocal) ? add_restart_links(h, pid1, ncv, vec, tan, vr, first_of, max_gid)
                                               : fail(h, SDEM_E_ARG, "orc_upload_contacts: bad owner index");
     free(vec); free(tan); free(vr);
-    if (rc) return rc;
+    if (rc) { free(first_of); return rc; }
     a = b;
   }
+  free(first_of);
   return 0;
 }
 
