@@ -820,6 +820,185 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
   if ((threadIdx.x & 31) == 0 && cand_x) atomicAdd(&d.counters[9], cand_x);
 }
 
+// ---------------------------------------------------------------------------
+// The same search on the one-level grid, warp-cooperative and staged through
+// shared memory.  A warp takes 32 consecutive target sort positions.  Targets
+// of one cell share their candidate list -- the cell itself (each target
+// uses the tail after its own position), then the reference's half shell in
+// its visit order -- so the warp stages that list once: the candidates'
+// single-precision records and their particle indices, each tagged with its
+// cell's corner offset.  Then, one target at a time, the lanes test 32
+// consecutive candidates of the list; a ballot over the hits gives every hit
+// its row slot in visit order, so rows, in-list keys and counters equal
+// those of the thread-per-target walk.  The tests are the same expressions as
+// k_search's (the prefilter, then the exact FP64 test inside its band).
+constexpr int kSearchWarps = 8;        // warps per block
+constexpr int kStage = 128;            // staged candidates per warp (longer lists go in pieces)
+
+__device__ __forceinline__ float corner_offset(int code, float cellf) {
+  return code == 1 ? cellf : (code == 2 ? -cellf : 0.f);
+}
+
+__global__ void __launch_bounds__(kSearchWarps * 32, 4) k_search_warp(Dev d, int s_begin, int s_end) {
+  __shared__ float4 st_q[kSearchWarps][kStage];
+  __shared__ int st_i[kSearchWarps][kStage];   // particle index | corner-offset code << 26
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int s0 = s_begin + (blockIdx.x * kSearchWarps + w) * 32;
+  if (s0 >= s_end) return;   // the whole warp
+  const int nt = *d.nt, nloc = *d.n;
+  const int K = d.K, Kin = d.Kin, ncap = d.ncap, nall = d.nall;
+  const float margin = d.pf_margin, cellf = d.cellf;
+  const int nx = d.nx, nz = d.nz;
+  const int* __restrict__ cs = d.cell_start;
+  const int s_me = s0 + lane;
+  const bool live = s_me < s_end && s_me < nt;
+  if (s_me < s_end && s_me >= nt) d.row_cnt[s_me] = 0;
+  int m_me = 0, cnt_me = 0;
+  int4 tc_me = make_int4(0, 0, 0, -1);
+  float4 pf_me = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (live) {
+    m_me = d.sorted[s_me];
+    tc_me = d.pcell[m_me];
+    pf_me = d.spos[s_me];
+  }
+  // live targets are a prefix of the warp's lanes (s < min(s_end, nt))
+  const int nlive = __popc(__ballot_sync(FULL, live));
+  unsigned long long cand = 0;
+  int j = 0;
+  while (j < nlive) {
+    // the group of targets in the cell of target j: consecutive lanes (the
+    // sort order is the cell order)
+    const int key = __shfl_sync(FULL, tc_me.w, j);
+    const unsigned same = __ballot_sync(FULL, live && tc_me.w == key);
+    const int j1 = 32 - __clz(same);
+    const int ix = __shfl_sync(FULL, tc_me.x, j), iy = __shfl_sync(FULL, tc_me.y, j),
+              iz = __shfl_sync(FULL, tc_me.z, j);
+    // the candidate list in visit order: six ranges of sort positions (own
+    // cell; cell (ix,iy,iz-1); columns (ix-1,iy), (ix-1..ix+1,iy-1), each of
+    // cells iz-1..iz+1, which are consecutive in the sort).  Corner offsets
+    // (target cell corner minus candidate cell corner) per axis as codes
+    // 0 -> 0, 1 -> +cell, 2 -> -cell, packed x | y << 2 | z << 4; a column's
+    // z code changes at its inner cell boundaries zb1, zb2.
+    int ra[6], rb[6], zb1[4], zb2[4];
+    const int a0 = cs[key];
+    ra[0] = a0; rb[0] = cs[key + 1];
+    ra[1] = iz > 0 ? cs[key - 1] : 0; rb[1] = iz > 0 ? a0 : 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const int cx = c == 0 ? ix - 1 : ix - 2 + c, cy = c == 0 ? iy : iy - 1;
+      int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+      if (!(cx < 0 || cx >= nx || cy < 0)) {
+        const int kb = (cy * nx + cx) * nz + iz;   // the grid holds fewer than 2^31 cells
+        b1 = cs[kb];
+        b2 = cs[kb + 1];
+        b0 = iz > 0 ? cs[kb - 1] : b1;
+        b3 = iz + 1 < nz ? cs[kb + 2] : b2;
+      }
+      ra[2 + c] = b0; rb[2 + c] = b3; zb1[c] = b1; zb2[c] = b2;
+    }
+    int pre[7];
+    pre[0] = 0;
+#pragma unroll
+    for (int r = 0; r < 6; r++) pre[r + 1] = pre[r] + (rb[r] - ra[r]);
+    const int M = pre[6];
+    for (int pb = 0; pb < M; pb += kStage) {
+      const int pe = min(M, pb + kStage);
+      // stage candidates [pb, pe) of the list
+      for (int i = pb + lane; i < pe; i += 32) {
+        int t = 0, cd = 0;
+#pragma unroll
+        for (int r = 0; r < 6; r++) {
+          if (i >= pre[r] && i < pre[r + 1]) {
+            t = ra[r] + (i - pre[r]);
+            if (r == 1) {
+              cd = 1 << 4;
+            } else if (r >= 2) {
+              const int c = r - 2;
+              const int xy = (c <= 1 ? 1 : (c == 2 ? 0 : 2)) | (c == 0 ? 0 : 1) << 2;
+              cd = xy | (t < zb1[c] ? 1 : (t < zb2[c] ? 0 : 2)) << 4;
+            }
+          }
+        }
+        st_q[w][i - pb] = d.spos[t];
+        st_i[w][i - pb] = (int)((unsigned)d.sorted[t] | (unsigned)cd << 26);   // indices < 2^26
+      }
+      __syncwarp();
+      for (int jj = j; jj < j1; jj++) {
+        const int s_t = s0 + jj;
+        const int m_t = __shfl_sync(FULL, m_me, jj);
+        const bool img = m_t >= nloc;
+        float4 Pf;
+        Pf.x = __shfl_sync(FULL, pf_me.x, jj);
+        Pf.y = __shfl_sync(FULL, pf_me.y, jj);
+        Pf.z = __shfl_sync(FULL, pf_me.z, jj);
+        Pf.w = __shfl_sync(FULL, pf_me.w, jj);
+        int cnt_t = __shfl_sync(FULL, cnt_me, jj);
+        const int first = max(s_t - a0 + 1, pb);   // the target's own-cell tail starts after it
+        for (int i0 = first; i0 < pe; i0 += 32) {
+          const int i = i0 + lane;
+          bool hit = false;
+          int q = 0;
+          if (i < pe) {
+            const float4 Qf = st_q[w][i - pb];
+            const int qi = st_i[w][i - pb];
+            q = qi & 0x3FFFFFF;
+            const int cd = (unsigned)qi >> 26;
+            if (!img || q < nloc) {   // an image or fixed target pairs with local particles only
+              cand++;
+              const float ox = corner_offset(cd & 3, cellf), oy = corner_offset((cd >> 2) & 3, cellf),
+                          oz = corner_offset((cd >> 4) & 3, cellf);
+              const float fx = (Pf.x - Qf.x) + ox, fy = (Pf.y - Qf.y) + oy, fz = (Pf.z - Qf.z) + oz;
+              const float d2f = fx * fx + fy * fy + fz * fz;
+              const float rs = Pf.w + Qf.w;
+              const float bhi = rs + margin;
+              if (!(d2f > bhi * bhi)) {
+                hit = true;
+                const float blo = rs - margin;
+                if (!(d2f < blo * blo)) {
+                  const dbl4 Pm = d.posr[m_t], Pq = d.posr[q];
+                  double dr = Pm.w + Pq.w;
+                  double dr2 = dr * dr;
+                  double dx = Pm.x - Pq.x;
+                  double d2sum = dx * dx;
+                  if (d2sum > dr2) hit = false;
+                  double dy = Pm.y - Pq.y;
+                  d2sum = dy * dy + d2sum;
+                  if (d2sum > dr2) hit = false;
+                  double dz = Pm.z - Pq.z;
+                  d2sum = dz * dz + d2sum;
+                  if (d2sum > dr2) hit = false;
+                }
+              }
+            }
+          }
+          const unsigned mask = __ballot_sync(FULL, hit);
+          if (hit) {
+            const int slot = cnt_t + __popc(mask & ((1u << lane) - 1u));
+            if (slot < K) {
+              d.row_partner[(size_t)slot * nall + s_t] = q;
+              if (q < nloc) {   // an image receives no force: it has no in-list
+                const int is = atomicAdd(&d.in_cnt[q], 1);
+                if (is < Kin) d.in_list[(size_t)is * ncap + q] = ((unsigned)s_t << 6) | (unsigned)slot;
+                else raise(d, SDEM_E_CL_FULL, q);
+              }
+            } else {
+              raise(d, SDEM_E_CL_FULL, m_t);
+            }
+          }
+          cnt_t += __popc(mask);
+        }
+        if (lane == jj) cnt_me = cnt_t;
+      }
+      __syncwarp();
+    }
+    j = j1;
+  }
+  if (live) d.row_cnt[s_me] = cnt_me < K ? cnt_me : K;
+  for (int o = 16; o > 0; o >>= 1) cand += __shfl_down_sync(FULL, cand, o);
+  if (lane == 0 && cand) atomicAdd(&d.counters[0], cand);
+}
+
 // Wall contacts of each particle: FindContactsPW (Prtcl_ContactSearchPW.f90:308-317)
 // walks the near-wall list front-first, i.e. the highest wall index first.
 // Slots j < kKw per particle keep that order; the compact list feeds k_wall_force.
@@ -2164,7 +2343,10 @@ int enqueue_step(sdem_h* h) {
   for (int k = 0; k < nchunk; k++) {
     const int a = cut(k), b = cut(k + 1);
     if (h->hier) k_search<true><<<grid_for(std::max(b - a, 1)), kThreads, 0, s2>>>(d, a, b);
-    else k_search<false><<<grid_for(std::max(b - a, 1)), kThreads, 0, s2>>>(d, a, b);
+    else {
+      const long long warps = (std::max(b - a, 1) + 31) / 32;
+      k_search_warp<<<(int)((warps + kSearchWarps - 1) / kSearchWarps), kSearchWarps * 32, 0, s2>>>(d, a, b);
+    }
     if (s2 != st) cudaEventRecord(h->ev_chunk[k], s2);
   }
   k_wall_detect<<<grid_for(n), kThreads, 0, s2>>>(d);
