@@ -822,26 +822,120 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
 
 // ---------------------------------------------------------------------------
 // The same search on the one-level grid, warp-cooperative and staged through
-// shared memory.  A warp takes 32 consecutive target sort positions.  Targets
-// of one cell share their candidate list -- the cell itself (each target
-// uses the tail after its own position), then the reference's half shell in
-// its visit order -- so the warp stages that list once: the candidates'
-// single-precision records and their particle indices, each tagged with its
-// cell's corner offset.  Then, one target at a time, the lanes test 32
-// consecutive candidates of the list; a ballot over the hits gives every hit
-// its row slot in visit order, so rows, in-list keys and counters equal
-// those of the thread-per-target walk.  The tests are the same expressions as
-// k_search's (the prefilter, then the exact FP64 test inside its band).
+// shared memory.  A warp takes 32 consecutive target sort positions; the
+// targets of one cell form a group and share one candidate list -- the cell
+// itself (each target uses the tail after its own position), then the
+// reference's half shell in its visit order.  Every lane first loads the
+// cell boundaries of its own target's list (the loads of all groups in
+// flight at once).  The warp then stages each group's list in shared memory
+// with asynchronous copies (cp.async: the candidates' single-precision
+// records and particle indices), one group ahead: group g+1's copies travel
+// while group g is tested.  One target at a time, the lanes test 32
+// consecutive candidates; a ballot over the hits gives every hit its row
+// slot in visit order, so rows, in-list keys and counters equal those of the
+// thread-per-target walk.  The tests are the same expressions as k_search's
+// (the prefilter, then the exact FP64 test inside its band).
 constexpr int kSearchWarps = 8;        // warps per block
-constexpr int kStage = 128;            // staged candidates per warp (longer lists go in pieces)
+constexpr int kStage = 96;             // staged candidates per warp and buffer (longer lists go in pieces)
+#ifndef SDEM_SEARCH_MIN_BLOCKS
+#define SDEM_SEARCH_MIN_BLOCKS 2       // resident blocks per SM the register budget allows
+#endif
+#ifndef SDEM_SEARCH_WARP
+#define SDEM_SEARCH_WARP 1             // 0: the thread-per-target walk also on the one-level grid
+#endif
 
 __device__ __forceinline__ float corner_offset(int code, float cellf) {
   return code == 1 ? cellf : (code == 2 ? -cellf : 0.f);
 }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-__global__ void __launch_bounds__(kSearchWarps * 32, 4) k_search_warp(Dev d, int s_begin, int s_end) {
-  __shared__ float4 st_q[kSearchWarps][kStage];
-  __shared__ int st_i[kSearchWarps][kStage];   // particle index | corner-offset code << 26
+// The candidate list of a target cell in visit order: six ranges of sort
+// positions (own cell; cell (ix,iy,iz-1); columns (ix-1,iy), (ix-1..ix+1,iy-1),
+// each of cells iz-1..iz+1, consecutive in the sort).  Corner offsets
+// (target cell corner minus candidate cell corner) per axis are codes
+// 0 -> 0, 1 -> +cell, 2 -> -cell, packed x | y << 2 | z << 4; a column's z
+// code changes at its inner cell boundaries zb1, zb2.
+struct CandList {
+  int ra[6], rb[6], zb1[4], zb2[4];
+};
+
+__device__ __forceinline__ void cand_list(const int* __restrict__ cs, int key, int ix, int iy, int iz, int nx, int nz,
+                                          CandList& L) {
+  const int a0 = cs[key];
+  L.ra[0] = a0; L.rb[0] = cs[key + 1];
+  L.ra[1] = iz > 0 ? cs[key - 1] : 0; L.rb[1] = iz > 0 ? a0 : 0;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const int cx = c == 0 ? ix - 1 : ix - 2 + c, cy = c == 0 ? iy : iy - 1;
+    int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+    if (!(cx < 0 || cx >= nx || cy < 0)) {
+      const int kb = (cy * nx + cx) * nz + iz;   // the grid holds fewer than 2^31 cells
+      b1 = cs[kb];
+      b2 = cs[kb + 1];
+      b0 = iz > 0 ? cs[kb - 1] : b1;
+      b3 = iz + 1 < nz ? cs[kb + 2] : b2;
+    }
+    L.ra[2 + c] = b0; L.rb[2 + c] = b3; L.zb1[c] = b1; L.zb2[c] = b2;
+  }
+}
+
+// the list of lane `src` (all lanes call)
+__device__ __forceinline__ void shfl_list(const CandList& mine, int src, CandList& L) {
+#pragma unroll
+  for (int r = 0; r < 6; r++) {
+    L.ra[r] = __shfl_sync(0xffffffffu, mine.ra[r], src);
+    L.rb[r] = __shfl_sync(0xffffffffu, mine.rb[r], src);
+  }
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    L.zb1[c] = __shfl_sync(0xffffffffu, mine.zb1[c], src);
+    L.zb2[c] = __shfl_sync(0xffffffffu, mine.zb2[c], src);
+  }
+}
+
+__device__ __forceinline__ int list_len(const CandList& L) {
+  int m = 0;
+#pragma unroll
+  for (int r = 0; r < 6; r++) m += L.rb[r] - L.ra[r];
+  return m;
+}
+
+// sort position and corner-offset code of entry i of the list
+__device__ __forceinline__ void list_entry(const CandList& L, int i, int& t, int& cd) {
+  t = 0;
+  cd = 0;
+  int base = 0;
+#pragma unroll
+  for (int r = 0; r < 6; r++) {
+    const int len = L.rb[r] - L.ra[r];
+    if (i >= base && i < base + len) {
+      t = L.ra[r] + (i - base);
+      if (r == 1) {
+        cd = 1 << 4;
+      } else if (r >= 2) {
+        const int c = r - 2;
+        const int xy = (c <= 1 ? 1 : (c == 2 ? 0 : 2)) | (c == 0 ? 0 : 1) << 2;
+        cd = xy | (t < L.zb1[c] ? 1 : (t < L.zb2[c] ? 0 : 2)) << 4;
+      }
+    }
+    base += len;
+  }
+}
+
+__global__ void __launch_bounds__(kSearchWarps * 32, SDEM_SEARCH_MIN_BLOCKS) k_search_warp(Dev d, int s_begin, int s_end) {
+  __shared__ float4 st_q[kSearchWarps][2][kStage];
+  __shared__ int st_i[kSearchWarps][2][kStage];
+  __shared__ unsigned char st_c[kSearchWarps][2][kStage];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int s0 = s_begin + (blockIdx.x * kSearchWarps + w) * 32;
@@ -849,150 +943,156 @@ __global__ void __launch_bounds__(kSearchWarps * 32, 4) k_search_warp(Dev d, int
   const int nt = *d.nt, nloc = *d.n;
   const int K = d.K, Kin = d.Kin, ncap = d.ncap, nall = d.nall;
   const float margin = d.pf_margin, cellf = d.cellf;
-  const int nx = d.nx, nz = d.nz;
   const int* __restrict__ cs = d.cell_start;
   const int s_me = s0 + lane;
   const bool live = s_me < s_end && s_me < nt;
   if (s_me < s_end && s_me >= nt) d.row_cnt[s_me] = 0;
-  int m_me = 0, cnt_me = 0;
-  int4 tc_me = make_int4(0, 0, 0, -1);
+  int m_me = 0, cnt_me = 0, key_me = -1;
   float4 pf_me = make_float4(0.f, 0.f, 0.f, 0.f);
+  CandList mine;
   if (live) {
     m_me = d.sorted[s_me];
-    tc_me = d.pcell[m_me];
+    const int4 tc = d.pcell[m_me];
+    key_me = tc.w;
     pf_me = d.spos[s_me];
+    cand_list(cs, tc.w, tc.x, tc.y, tc.z, d.nx, d.nz, mine);
+  } else {
+#pragma unroll
+    for (int r = 0; r < 6; r++) mine.ra[r] = mine.rb[r] = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) mine.zb1[c] = mine.zb2[c] = 0;
   }
-  // live targets are a prefix of the warp's lanes (s < min(s_end, nt))
+  // live targets are a prefix of the warp's lanes; a group starts where the
+  // cell changes (the sort order is the cell order)
   const int nlive = __popc(__ballot_sync(FULL, live));
+  const int key_prev = __shfl_up_sync(FULL, key_me, 1);
+  unsigned leaders = __ballot_sync(FULL, live && (lane == 0 || key_me != key_prev));
   unsigned long long cand = 0;
-  int j = 0;
-  while (j < nlive) {
-    // the group of targets in the cell of target j: consecutive lanes (the
-    // sort order is the cell order)
-    const int key = __shfl_sync(FULL, tc_me.w, j);
-    const unsigned same = __ballot_sync(FULL, live && tc_me.w == key);
-    const int j1 = 32 - __clz(same);
-    const int ix = __shfl_sync(FULL, tc_me.x, j), iy = __shfl_sync(FULL, tc_me.y, j),
-              iz = __shfl_sync(FULL, tc_me.z, j);
-    // the candidate list in visit order: six ranges of sort positions (own
-    // cell; cell (ix,iy,iz-1); columns (ix-1,iy), (ix-1..ix+1,iy-1), each of
-    // cells iz-1..iz+1, which are consecutive in the sort).  Corner offsets
-    // (target cell corner minus candidate cell corner) per axis as codes
-    // 0 -> 0, 1 -> +cell, 2 -> -cell, packed x | y << 2 | z << 4; a column's
-    // z code changes at its inner cell boundaries zb1, zb2.
-    int ra[6], rb[6], zb1[4], zb2[4];
-    const int a0 = cs[key];
-    ra[0] = a0; rb[0] = cs[key + 1];
-    ra[1] = iz > 0 ? cs[key - 1] : 0; rb[1] = iz > 0 ? a0 : 0;
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-      const int cx = c == 0 ? ix - 1 : ix - 2 + c, cy = c == 0 ? iy : iy - 1;
-      int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-      if (!(cx < 0 || cx >= nx || cy < 0)) {
-        const int kb = (cy * nx + cx) * nz + iz;   // the grid holds fewer than 2^31 cells
-        b1 = cs[kb];
-        b2 = cs[kb + 1];
-        b0 = iz > 0 ? cs[kb - 1] : b1;
-        b3 = iz + 1 < nz ? cs[kb + 2] : b2;
+
+  // stage the list of the group led by lane `lead` into buffer `buf` (copies
+  // only when it fits; one commit group either way)
+  auto stage = [&](int lead, int buf) -> int {
+    CandList L;
+    shfl_list(mine, lead, L);
+    const int M = list_len(L);
+    if (M <= kStage) {
+      for (int i = lane; i < M; i += 32) {
+        int t, cd;
+        list_entry(L, i, t, cd);
+        cp_async16(&st_q[w][buf][i], &d.spos[t]);
+        cp_async4(&st_i[w][buf][i], &d.sorted[t]);
+        st_c[w][buf][i] = (unsigned char)cd;
       }
-      ra[2 + c] = b0; rb[2 + c] = b3; zb1[c] = b1; zb2[c] = b2;
     }
-    int pre[7];
-    pre[0] = 0;
-#pragma unroll
-    for (int r = 0; r < 6; r++) pre[r + 1] = pre[r] + (rb[r] - ra[r]);
-    const int M = pre[6];
-    for (int pb = 0; pb < M; pb += kStage) {
-      const int pe = min(M, pb + kStage);
-      // stage candidates [pb, pe) of the list
-      for (int i = pb + lane; i < pe; i += 32) {
-        int t = 0, cd = 0;
-#pragma unroll
-        for (int r = 0; r < 6; r++) {
-          if (i >= pre[r] && i < pre[r + 1]) {
-            t = ra[r] + (i - pre[r]);
-            if (r == 1) {
-              cd = 1 << 4;
-            } else if (r >= 2) {
-              const int c = r - 2;
-              const int xy = (c <= 1 ? 1 : (c == 2 ? 0 : 2)) | (c == 0 ? 0 : 1) << 2;
-              cd = xy | (t < zb1[c] ? 1 : (t < zb2[c] ? 0 : 2)) << 4;
+    cp_async_commit();
+    return M;
+  };
+
+  // test candidates [lo, hi) of the buffer (entry i at i - base) for target lane jj
+  auto test_range = [&](int jj, int buf, int base, int lo, int hi) {
+    const int s_t = s0 + jj;
+    const int m_t = __shfl_sync(FULL, m_me, jj);
+    const bool img = m_t >= nloc;
+    float4 Pf;
+    Pf.x = __shfl_sync(FULL, pf_me.x, jj);
+    Pf.y = __shfl_sync(FULL, pf_me.y, jj);
+    Pf.z = __shfl_sync(FULL, pf_me.z, jj);
+    Pf.w = __shfl_sync(FULL, pf_me.w, jj);
+    int cnt_t = __shfl_sync(FULL, cnt_me, jj);
+    for (int i0 = lo; i0 < hi; i0 += 32) {
+      const int i = i0 + lane;
+      bool hit = false;
+      int q = 0;
+      if (i < hi) {
+        const float4 Qf = st_q[w][buf][i - base];
+        q = st_i[w][buf][i - base];
+        const int cd = st_c[w][buf][i - base];
+        if (!img || q < nloc) {   // an image or fixed target pairs with local particles only
+          cand++;
+          const float ox = corner_offset(cd & 3, cellf), oy = corner_offset((cd >> 2) & 3, cellf),
+                      oz = corner_offset((cd >> 4) & 3, cellf);
+          const float fx = (Pf.x - Qf.x) + ox, fy = (Pf.y - Qf.y) + oy, fz = (Pf.z - Qf.z) + oz;
+          const float d2f = fx * fx + fy * fy + fz * fz;
+          const float rs = Pf.w + Qf.w;
+          const float bhi = rs + margin;
+          if (!(d2f > bhi * bhi)) {
+            hit = true;
+            const float blo = rs - margin;
+            if (!(d2f < blo * blo)) {
+              const dbl4 Pm = d.posr[m_t], Pq = d.posr[q];
+              double dr = Pm.w + Pq.w;
+              double dr2 = dr * dr;
+              double dx = Pm.x - Pq.x;
+              double d2sum = dx * dx;
+              if (d2sum > dr2) hit = false;
+              double dy = Pm.y - Pq.y;
+              d2sum = dy * dy + d2sum;
+              if (d2sum > dr2) hit = false;
+              double dz = Pm.z - Pq.z;
+              d2sum = dz * dz + d2sum;
+              if (d2sum > dr2) hit = false;
             }
           }
         }
-        st_q[w][i - pb] = d.spos[t];
-        st_i[w][i - pb] = (int)((unsigned)d.sorted[t] | (unsigned)cd << 26);   // indices < 2^26
       }
-      __syncwarp();
-      for (int jj = j; jj < j1; jj++) {
-        const int s_t = s0 + jj;
-        const int m_t = __shfl_sync(FULL, m_me, jj);
-        const bool img = m_t >= nloc;
-        float4 Pf;
-        Pf.x = __shfl_sync(FULL, pf_me.x, jj);
-        Pf.y = __shfl_sync(FULL, pf_me.y, jj);
-        Pf.z = __shfl_sync(FULL, pf_me.z, jj);
-        Pf.w = __shfl_sync(FULL, pf_me.w, jj);
-        int cnt_t = __shfl_sync(FULL, cnt_me, jj);
-        const int first = max(s_t - a0 + 1, pb);   // the target's own-cell tail starts after it
-        for (int i0 = first; i0 < pe; i0 += 32) {
-          const int i = i0 + lane;
-          bool hit = false;
-          int q = 0;
-          if (i < pe) {
-            const float4 Qf = st_q[w][i - pb];
-            const int qi = st_i[w][i - pb];
-            q = qi & 0x3FFFFFF;
-            const int cd = (unsigned)qi >> 26;
-            if (!img || q < nloc) {   // an image or fixed target pairs with local particles only
-              cand++;
-              const float ox = corner_offset(cd & 3, cellf), oy = corner_offset((cd >> 2) & 3, cellf),
-                          oz = corner_offset((cd >> 4) & 3, cellf);
-              const float fx = (Pf.x - Qf.x) + ox, fy = (Pf.y - Qf.y) + oy, fz = (Pf.z - Qf.z) + oz;
-              const float d2f = fx * fx + fy * fy + fz * fz;
-              const float rs = Pf.w + Qf.w;
-              const float bhi = rs + margin;
-              if (!(d2f > bhi * bhi)) {
-                hit = true;
-                const float blo = rs - margin;
-                if (!(d2f < blo * blo)) {
-                  const dbl4 Pm = d.posr[m_t], Pq = d.posr[q];
-                  double dr = Pm.w + Pq.w;
-                  double dr2 = dr * dr;
-                  double dx = Pm.x - Pq.x;
-                  double d2sum = dx * dx;
-                  if (d2sum > dr2) hit = false;
-                  double dy = Pm.y - Pq.y;
-                  d2sum = dy * dy + d2sum;
-                  if (d2sum > dr2) hit = false;
-                  double dz = Pm.z - Pq.z;
-                  d2sum = dz * dz + d2sum;
-                  if (d2sum > dr2) hit = false;
-                }
-              }
-            }
+      const unsigned mask = __ballot_sync(FULL, hit);
+      if (hit) {
+        const int slot = cnt_t + __popc(mask & ((1u << lane) - 1u));
+        if (slot < K) {
+          d.row_partner[(size_t)slot * nall + s_t] = q;
+          if (q < nloc) {   // an image receives no force: it has no in-list
+            const int is = atomicAdd(&d.in_cnt[q], 1);
+            if (is < Kin) d.in_list[(size_t)is * ncap + q] = ((unsigned)s_t << 6) | (unsigned)slot;
+            else raise(d, SDEM_E_CL_FULL, q);
           }
-          const unsigned mask = __ballot_sync(FULL, hit);
-          if (hit) {
-            const int slot = cnt_t + __popc(mask & ((1u << lane) - 1u));
-            if (slot < K) {
-              d.row_partner[(size_t)slot * nall + s_t] = q;
-              if (q < nloc) {   // an image receives no force: it has no in-list
-                const int is = atomicAdd(&d.in_cnt[q], 1);
-                if (is < Kin) d.in_list[(size_t)is * ncap + q] = ((unsigned)s_t << 6) | (unsigned)slot;
-                else raise(d, SDEM_E_CL_FULL, q);
-              }
-            } else {
-              raise(d, SDEM_E_CL_FULL, m_t);
-            }
-          }
-          cnt_t += __popc(mask);
+        } else {
+          raise(d, SDEM_E_CL_FULL, m_t);
         }
-        if (lane == jj) cnt_me = cnt_t;
+      }
+      cnt_t += __popc(mask);
+    }
+    if (lane == jj) cnt_me = cnt_t;
+  };
+
+  if (nlive > 0) {
+    int lead = __ffs(leaders) - 1;
+    leaders &= leaders - 1;
+    int M = stage(lead, 0);
+    for (int g = 0; lead < nlive; g++) {
+      const int buf = g & 1;
+      const int next = leaders ? __ffs(leaders) - 1 : nlive;   // the next group's leader ends this group
+      int Mn = 0;
+      if (leaders) Mn = stage(next, buf ^ 1);
+      else cp_async_commit();
+      cp_async_wait_1();
+      __syncwarp();
+      const int a0 = __shfl_sync(FULL, mine.ra[0], lead);
+      if (M <= kStage) {
+        for (int jj = lead; jj < next; jj++) test_range(jj, buf, 0, s0 + jj - a0 + 1, M);
+      } else {
+        // a list longer than the buffer: pieces staged with plain loads
+        CandList L;
+        shfl_list(mine, lead, L);
+        for (int pb = 0; pb < M; pb += kStage) {
+          const int pe = min(M, pb + kStage);
+          for (int i = pb + lane; i < pe; i += 32) {
+            int t, cd;
+            list_entry(L, i, t, cd);
+            st_q[w][buf][i - pb] = d.spos[t];
+            st_i[w][buf][i - pb] = d.sorted[t];
+            st_c[w][buf][i - pb] = (unsigned char)cd;
+          }
+          __syncwarp();
+          for (int jj = lead; jj < next; jj++) test_range(jj, buf, pb, max(s0 + jj - a0 + 1, pb), pe);
+          __syncwarp();
+        }
       }
       __syncwarp();
+      lead = next;
+      if (leaders) leaders &= leaders - 1;
+      M = Mn;
     }
-    j = j1;
+    cp_async_wait_0();
   }
   if (live) d.row_cnt[s_me] = cnt_me < K ? cnt_me : K;
   for (int o = 16; o > 0; o >>= 1) cand += __shfl_down_sync(FULL, cand, o);
@@ -2343,6 +2443,7 @@ int enqueue_step(sdem_h* h) {
   for (int k = 0; k < nchunk; k++) {
     const int a = cut(k), b = cut(k + 1);
     if (h->hier) k_search<true><<<grid_for(std::max(b - a, 1)), kThreads, 0, s2>>>(d, a, b);
+    else if (!SDEM_SEARCH_WARP) k_search<false><<<grid_for(std::max(b - a, 1)), kThreads, 0, s2>>>(d, a, b);
     else {
       const long long warps = (std::max(b - a, 1) + 31) / 32;
       k_search_warp<<<(int)((warps + kSearchWarps - 1) / kSearchWarps), kSearchWarps * 32, 0, s2>>>(d, a, b);
