@@ -49,7 +49,7 @@ FORCE_DRAM_BYTES_PER_CONTACT = 394.0     # k_force: dram__bytes_read.sum + dram_
 FP64_INST_PER_SM_CLK = 2.0               # DADD/DMUL/DFMA thread operations per SM per clock (FP64 pipe)
 NUM_SMS = 152
 # Executed DADD + DMUL + DFMA thread instructions of the step's kernels
-# (profiles/fp64_counts_hertz_poly_settled.txt), modelled per particle-particle
+# (profiles/fp64_counts_hertz_poly_settled_1m.txt), modelled per particle-particle
 # contact, per sphere and per wall contact.
 FP64_PER_CONTACT = {"k_force": 133.8, "k_gather": 24.0}
 FP64_PER_SPHERE = {"k_integrate": 57.0, "k_gather": 2.3, "k_bin": 6.0, "k_wall_detect": 0.6}
