@@ -77,6 +77,9 @@ constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact r
 #define SDEM_PIPELINE_CHUNKS 2
 #endif
 constexpr int kChunks = SDEM_PIPELINE_CHUNKS;   // search/force pipeline chunks per step
+#ifndef SDEM_SEARCH_PREFETCH
+#define SDEM_SEARCH_PREFETCH 1     // k_search requests the next candidate's record before testing one
+#endif
 constexpr int kMaxLevels = 6;     // hierarchical search levels (Init_Munjiza_Hrchl caps at 6)
 
 // One level of the hierarchical search: a grid of cells 2^(mult-1) times
@@ -699,12 +702,11 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
       // only candidates inside the band run the FP64 test here.  FP64 work left
       // in this divergent loop would occupy the FP64 pipe with one or two lanes.
       // (ox, oy, oz): target cell corner minus candidate cell corner (0 or one cell)
-      auto test = [&](int t, float ox, float oy, float oz, unsigned long long& ctr) {
+      auto test = [&](int t, const float4 Qf, float ox, float oy, float oz, unsigned long long& ctr) {
         if (m_img) {
           if (d.sorted[t] >= nloc) return;   // image-image pairs are not searched
           ctr++;
         }
-        const float4 Qf = d.spos[t];
         const float fx = (Pf.x - Qf.x) + ox, fy = (Pf.y - Qf.y) + oy, fz = (Pf.z - Qf.z) + oz;
         const float d2f = fx * fx + fy * fy + fz * fz;
         const float rs = Pf.w + Qf.w;
@@ -738,6 +740,24 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
         }
         cnt++;
       };
+      // Candidates [a, b) of one range, in order; with SDEM_SEARCH_PREFETCH the
+      // next candidate's record is requested (read-only path) before the
+      // current one is tested.  In a column (cells iz-1, iz, iz+1 consecutive
+      // in the sort) the z offset changes at the inner boundaries z1, z2.
+      auto walk = [&](int a, int b, int z1, int z2, float ox, float oy, float oz0, float oz1, float oz2,
+                      unsigned long long& ctr) {
+#if SDEM_SEARCH_PREFETCH
+        if (a >= b) return;
+        float4 Qn = __ldg(&d.spos[a]);
+        for (int t = a; t < b; t++) {
+          const float4 Qf = Qn;
+          if (t + 1 < b) Qn = __ldg(&d.spos[t + 1]);
+          test(t, Qf, ox, oy, t < z1 ? oz0 : (t < z2 ? oz1 : oz2), ctr);
+        }
+#else
+        for (int t = a; t < b; t++) test(t, d.spos[t], ox, oy, t < z1 ? oz0 : (t < z2 ? oz1 : oz2), ctr);
+#endif
+      };
       // Cell boundaries of the whole half shell are loaded up front (they do
       // not depend on one another), then the candidates are walked in the
       // reference's order.  The three cells iz-1..iz+1 of one (ix, iy) column
@@ -762,18 +782,15 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
         }
       }
       // same cell, particles after the target in list order
-      for (int t = s + 1; t < tail_end; t++) test(t, 0.f, 0.f, 0.f, cand);
+      walk(s + 1, tail_end, tail_end, tail_end, 0.f, 0.f, 0.f, 0.f, 0.f, cand);
       // (ix, iy, iz-1)
-      for (int t = own_lo; t < own_hi; t++) test(t, 0.f, 0.f, cellf, cand);
+      walk(own_lo, own_hi, own_hi, own_hi, 0.f, 0.f, cellf, cellf, cellf, cand);
       if (!m_img) cand += (unsigned long long)((tail_end - s - 1) + (own_hi - own_lo));
       // columns (ix-1, iy), then (ix-1..ix+1, iy-1), cells iz-1, iz, iz+1
 #pragma unroll
       for (int c = 0; c < 4; c++) {
         const float ox = (float)(ix - ccx[c]) * cellf, oy = (float)(iy - ccy[c]) * cellf;
-        int t = cb[c][0];
-        for (; t < cb[c][1]; t++) test(t, ox, oy, cellf, cand);
-        for (; t < cb[c][2]; t++) test(t, ox, oy, 0.f, cand);
-        for (; t < cb[c][3]; t++) test(t, ox, oy, -cellf, cand);
+        walk(cb[c][0], cb[c][3], cb[c][1], cb[c][2], ox, oy, cellf, 0.f, -cellf, cand);
         if (!m_img) cand += (unsigned long long)(cb[c][3] - cb[c][0]);
       }
       // Hierarchical search: then the 27 cells around the target's cell in
@@ -801,7 +818,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
                 if (cz < 0 || cz >= X.nz) continue;
                 const int a = csx[kc + cz], b = csx[kc + cz + 1];
                 const float oz = (float)(iz - cz * coe) * cellf;
-                for (int t = a; t < b; t++) test(t, ox, oy, oz, cand_x);
+                walk(a, b, b, b, ox, oy, oz, oz, oz, cand_x);
                 if (!m_img) cand_x += (unsigned long long)(b - a);
               }
             }
@@ -841,7 +858,7 @@ constexpr int kStage = 96;             // staged candidates per warp and buffer 
 #define SDEM_SEARCH_MIN_BLOCKS 2       // resident blocks per SM the register budget allows
 #endif
 #ifndef SDEM_SEARCH_WARP
-#define SDEM_SEARCH_WARP 1             // 0: the thread-per-target walk also on the one-level grid
+#define SDEM_SEARCH_WARP 0             // 1: the warp-cooperative search on the one-level grid
 #endif
 
 __device__ __forceinline__ float corner_offset(int code, float cellf) {

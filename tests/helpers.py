@@ -79,9 +79,15 @@ def assert_step_matches(g, o, rtol: float = 1e-12, what: str = ""):
     assert len(np.unique(kg)) == len(kg), f"{what}: a contact is listed twice"
     np.testing.assert_array_equal(kg, ko, err_msg=f"{what}: contact sets")
     sc = np.maximum(np.maximum(np.abs(hg[:, :3]).max(axis=1), np.abs(ho[:, :3]).max(axis=1)), 1e-25)
-    assert (np.abs(hg[:, :3] - ho[:, :3]).max(axis=1) <= rtol * sc).all(), f"{what}: tangential history"
+    bad = np.nonzero(np.abs(hg[:, :3] - ho[:, :3]).max(axis=1) > rtol * sc)[0]
+    assert len(bad) == 0, (f"{what}: tangential history of {len(bad)} contacts; first "
+                           + "; ".join(f"key ({kg[b] >> 32}, {kg[b] & 0xFFFFFFFF}) gpu {hg[b].tolist()} "
+                                       f"oracle {ho[b].tolist()}" for b in bad[:3]))
     sv = np.maximum(np.maximum(np.abs(hg[:, 3]), np.abs(ho[:, 3])), 1e-300)
-    assert (np.abs(hg[:, 3] - ho[:, 3]) <= rtol * sv).all(), f"{what}: VelRel_Init"
+    bad = np.nonzero(np.abs(hg[:, 3] - ho[:, 3]) > rtol * sv)[0]
+    assert len(bad) == 0, (f"{what}: VelRel_Init of {len(bad)} contacts; first "
+                           + "; ".join(f"key ({kg[b] >> 32}, {kg[b] & 0xFFFFFFFF}) gpu {hg[b].tolist()} "
+                                       f"oracle {ho[b].tolist()}" for b in bad[:3]))
     Fg, Tg = g.forces()
     Fo, To = o.forces()
     fs = force_scale(Fo, 1e-6 * max(np.abs(Fo).max(), 1e-30))
