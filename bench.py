@@ -480,29 +480,62 @@ def our_arm(args):
 
 
 def sandboxes_arm(args):
-    """The batched workload (not the headline line): `--instances` sandboxes
-    of 2,000-50,000 spheres with their own materials, contact models and
-    boxes (sdem_gb300.beds.sandbox_case, parameters from seed 4), advanced
-    (a) as one batch (sdem_batch_step: one graph per two steps for all of
-    them), (b) one instance after another (each instance's steps, then the
-    next instance), (c) every instance on its own stream from one host
-    thread.  Host wall-clock around synchronised runs; particle-steps/s of
-    the whole set."""
+    """The batched workload (its own line): `--instances` sandboxes of
+    2,000-50,000 spheres with their own materials, contact models and boxes
+    (sdem_gb300.beds.sandbox_case, parameters from seed 4).  They first fall
+    into contact (`--contact-steps` batch steps: the lattices collapse onto
+    their floors), then the autotuner (sdem_gb300.tune) picks each size
+    class's launch shape and the batch's group size.  Timed, from that state:
+    (a) the tuned batch, (b) the batch with the default shapes, (c) one
+    instance after another (each instance's steps, then the next: one launch
+    sequence per instance), (d) every instance on its own stream from one host
+    thread.  Host wall-clock around synchronised runs; particle-steps/s of the
+    whole set."""
     import torch
-    from sdem_gb300 import beds
+    from sdem_gb300 import beds, tune
     from sdem_gb300.capi import DEMBatch, DEMSystem
     torch.cuda.set_device(0)
     rng = np.random.default_rng(4)
     cases = [beds.sandbox_case(rng, i) for i in range(args.instances)]
     total = sum(c.particles.n for c in cases)
     members = [DEMSystem(c) for c in cases]
-    batch = DEMBatch(members)
-    K = args.steps + args.steps % 2          # whole graph replays
-    batch.step(2 * ((args.warmup + 1) // 2))   # even: the captured parities hold
     t0 = time.perf_counter()
-    batch.step(K)
-    t_batch = time.perf_counter() - t0
+    pre = DEMBatch(members)
+    pre.step(args.contact_steps + args.contact_steps % 2)
+    pre.close()
+    t_contact = time.perf_counter() - t0
     contacts = sum(m.counters()["pp"] + m.counters()["pw"] for m in members)
+    # tuning: one representative (its state and contacts now) per size class
+    t0 = time.perf_counter()
+    classes = {}
+    for m in members:
+        classes.setdefault(tune.size_class(m.case), []).append(m)
+    shapes = {}
+    for key, ms_ in classes.items():
+        rep = ms_[len(ms_) // 2]
+        rc = beds.Case(rep.case.name, rep.case.opts, rep.case.tables, rep.case.walls, rep.state(),
+                       contacts=rep.contacts())
+        shapes[key] = tune.tune_handle(rc, steps=6)
+    default_shape = [m.get_launch() for m in members]
+    for m in members:
+        tune.apply(m, shapes[tune.size_class(m.case)])
+    group = tune.tune_batch(members, steps=4)
+    t_tune = time.perf_counter() - t0
+    K = args.steps + args.steps % 2          # whole graph replays
+
+    def run_batch(gs):
+        b = DEMBatch(members, group_size=gs)
+        b.step(2 * ((args.warmup + 1) // 2))   # even: the captured parities hold
+        t = time.perf_counter()
+        b.step(K)
+        el = time.perf_counter() - t
+        b.close()
+        return el
+
+    t_tuned = run_batch(group["group_size"])
+    for m, (c, f) in zip(members, default_shape):
+        m.set_launch(c, f)
+    t_default = run_batch(0)
     for m in members:                        # each instance's own graphs, captured before timing
         m.step(4)
     t0 = time.perf_counter()
@@ -515,19 +548,25 @@ def sandboxes_arm(args):
     for m in members:
         m.counters()
     t_streams = time.perf_counter() - t0
-    line = {"metric": "particle-steps/s, %d sandboxes" % args.instances, "value": total * K / t_batch,
-            "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": t_batch / K * 1e3,
+    line = {"metric": "particle-steps/s, %d sandboxes" % args.instances, "value": total * K / t_tuned,
+            "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": t_tuned / K * 1e3,
             "higher_is_better": True, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "sandboxes", "instances": args.instances, "particles": total,
-                       "contacts_last": contacts, "models": {
+                       "contact_steps": args.contact_steps, "contacts_at_start": contacts,
+                       "contacts_per_particle": contacts / total, "models": {
                            "hertz": sum(1 for c in cases if c.opts.cf_type == props_cft_nlin()),
                            "lsd": sum(1 for c in cases if c.opts.cf_type != props_cft_nlin())}},
+            "batch_default_shapes": total * K / t_default,
             "one_instance_after_another": total * K / t_seq,
             "instances_on_own_streams": total * K / t_streams,
-            "note": "host wall clock around synchronised runs of the same sandboxes, in this order: batch, "
-                    "one instance after another, every instance on its own stream"}
+            "tuning": {"group_size": group["group_size"], "group_sizes_ms": group["tried"],
+                       "shapes": {k: {"pipeline_chunks": v["pipeline_chunks"],
+                                      "force_blocks_per_sm": v["force_blocks_per_sm"]} for k, v in shapes.items()},
+                       "seconds": t_tune, "contact_seconds": t_contact},
+            "note": "host wall clock around synchronised runs of the same sandboxes in contact, in this order: "
+                    "tuned batch, batch with default shapes, one instance after another, every instance on its "
+                    "own stream"}
     print(json.dumps(line), flush=True)
-    batch.close()
     for m in members:
         m.close()
 
@@ -692,6 +731,8 @@ def main():
                          "sandboxes: the batched workload; surrogate: the learned surrogate against the plain "
                          "DEM (each its own line)")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--contact-steps", type=int, default=4000,
+                    help="sandboxes: batch steps before timing, so that the beds are in contact")
     ap.add_argument("--train-beds", type=int, default=3)
     ap.add_argument("--train-iters", type=int, default=300)
     ap.add_argument("--strides", type=int, default=5)

@@ -276,6 +276,16 @@ const char* sdem_profile_phase_name(int i);
  * any bit (0 expected). */
 int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatches);
 
+/* ---- launch shape (no counterpart in the reference) -------------------------
+ * The step's search/force pipeline runs in pipeline_chunks chunks of target
+ * sort positions (1..4; default 2) and the force kernel with
+ * force_blocks_per_sm blocks per SM in it (1..8; default 3).  Results are
+ * bit-identical for every value (every order that matters is fixed by sort
+ * positions); only the speed changes, which sdem_gb300/tune.py measures.  0
+ * keeps a value; a change makes the next step capture its graphs again. */
+int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm);
+int sdem_get_launch(sdem_h* h, int* pipeline_chunks, int* force_blocks_per_sm);
+
 /* Measures the FP64 pipe: a kernel of eight independent DFMA chains per
  * thread (8 blocks of 256 threads per SM) runs `iters` iterations on the
  * current device; *dfma_per_s receives the executed DFMA per second (one DFMA
@@ -330,6 +340,9 @@ void sdem_destroy(sdem_h* h);
  * outlive it; sdem_batch_destroy does not destroy the members. */
 typedef struct sdem_batch sdem_batch;
 int sdem_batch_create(int n, sdem_h* const* members, sdem_batch** out);
+/* The same with groups of at most group_size members (0: the default of 64):
+ * one graph and one stream per group. */
+int sdem_batch_create_grouped(int n, sdem_h* const* members, int group_size, sdem_batch** out);
 /* nsteps steps of every member, without a final synchronisation */
 int sdem_batch_step_async(sdem_batch* b, int nsteps);
 /* waits for the batch and reports the first member error (SDEM_E_*) */

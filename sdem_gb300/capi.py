@@ -30,6 +30,7 @@ EXPORTED = ("sdem_default_cfg", "sdem_create", "sdem_set_types", "sdem_set_walls
             "sdem_download_forces", "sdem_counters", "sdem_counters_lagged", "sdem_counter_sums",
             "sdem_launch_count", "sdem_profile_begin", "sdem_profile_end", "sdem_profile_phase_name",
             "sdem_count_contacts_noalloc", "sdem_selftest_fp64", "sdem_probe_fp64_peak",
+            "sdem_set_launch", "sdem_get_launch", "sdem_batch_create_grouped",
             "sdem_snapshot_begin", "sdem_snapshot_end", "sdem_snapshot_contacts", "sdem_set_fixed", "sdem_last_error",
             "sdem_destroy", "sdem_batch_create", "sdem_batch_step_async", "sdem_batch_sync", "sdem_batch_step",
             "sdem_batch_last_error", "sdem_batch_destroy")
@@ -147,6 +148,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_count_contacts_noalloc.argtypes = [C.POINTER(SdemCfg), C.c_double, C.c_int, P, P, P]
     lib.sdem_selftest_fp64.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
     lib.sdem_probe_fp64_peak.argtypes = [C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.sdem_set_launch.argtypes = [P, C.c_int, C.c_int]
+    lib.sdem_get_launch.argtypes = [P, ip, ip]
+    lib.sdem_batch_create_grouped.argtypes = [C.c_int, C.POINTER(P), C.c_int, C.POINTER(P)]
     lib.sdem_snapshot_begin.argtypes = [P, ip, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp, C.c_int]
     lib.sdem_snapshot_end.argtypes = [P, ip]
     lib.sdem_snapshot_contacts.argtypes = [P, C.c_int, ip, ip, ip, dp, dp]
@@ -364,6 +368,15 @@ class DEMSystem:
         self._check(self.lib.sdem_counter_sums(self.h, out))
         return {"pp": out[0], "pw": out[1], "steps": out[2]}
 
+    def set_launch(self, pipeline_chunks: int = 0, force_blocks_per_sm: int = 0) -> None:
+        """sdem_set_launch: the step's launch shape (results do not depend on it)."""
+        self._check(self.lib.sdem_set_launch(self.h, int(pipeline_chunks), int(force_blocks_per_sm)))
+
+    def get_launch(self) -> tuple:
+        a, b = C.c_int(), C.c_int()
+        self._check(self.lib.sdem_get_launch(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def launch_count(self) -> int:
         n = C.c_longlong()
         self._check(self.lib.sdem_launch_count(self.h, C.byref(n)))
@@ -419,12 +432,12 @@ class DEMBatch:
     per batch step holds every member's step.  The members stay usable for
     downloads and single steps; they must outlive the batch."""
 
-    def __init__(self, members):
+    def __init__(self, members, group_size: int = 0):
         self.lib = load()
         self.members = list(members)
         arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
         self.b = C.c_void_p()
-        rc = self.lib.sdem_batch_create(len(self.members), arr, C.byref(self.b))
+        rc = self.lib.sdem_batch_create_grouped(len(self.members), arr, int(group_size), C.byref(self.b))
         if rc:
             msg = self.lib.sdem_batch_last_error(self.b).decode() if self.b else ""
             self.lib.sdem_batch_destroy(self.b)

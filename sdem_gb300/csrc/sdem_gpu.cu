@@ -76,7 +76,9 @@ constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact r
 #ifndef SDEM_PIPELINE_CHUNKS
 #define SDEM_PIPELINE_CHUNKS 2
 #endif
-constexpr int kChunks = SDEM_PIPELINE_CHUNKS;   // search/force pipeline chunks per step
+constexpr int kChunks = SDEM_PIPELINE_CHUNKS;   // search/force pipeline chunks per step (default)
+constexpr int kMaxChunks = 4;                   // most chunks sdem_set_launch accepts
+constexpr int kForceBlocksPerSM = 3;            // k_force blocks per SM in the pipeline (default)
 #ifndef SDEM_SEARCH_PREFETCH
 #define SDEM_SEARCH_PREFETCH 1     // k_search requests the next candidate's record before testing one
 #endif
@@ -2136,7 +2138,9 @@ struct sdem_h {
   GRec* gorder = nullptr;
   // second stream and events of the chunked search/force pipeline
   cudaStream_t stream2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chunk[kChunks] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chunk[kMaxChunks] = {};
+  int nchunk = kChunks;                  // launch shape (sdem_set_launch); results do not depend on it
+  int force_bps = kForceBlocksPerSM;
   int cur = 0;  // buffer written by the next step
   // device scalars
   int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
@@ -2446,7 +2450,7 @@ int enqueue_step(sdem_h* h) {
   // the previous chunk's total), contact rows and forces run on the main
   // stream as soon as its search is done.  Profiling runs one chunk on one
   // stream, so that every phase has its own events.
-  const int nchunk = ev ? 1 : kChunks;
+  const int nchunk = ev ? 1 : h->nchunk;
   cudaStream_t s2 = ev ? st : h->stream2;
   // chunk boundaries on scan tiles, so that each chunk's row scan moves whole
   // aligned tiles
@@ -2486,8 +2490,8 @@ int enqueue_step(sdem_h* h) {
       cudaStreamWaitEvent(st, h->ev_chunk[k], 0);
       scan(h, h->row_cnt + a, b - a, h->row_off + a, k ? h->row_off + a : nullptr);
       k_row_fill<<<grid_for(std::max(b - a, 1)), kThreads, 0, st>>>(d, a, b);
-      if (h->gcap > 0 || h->nfix > 0) k_force<true><<<h->num_sms * 3, kThreads, 0, st>>>(d, a, b);
-      else k_force<false><<<h->num_sms * 3, kThreads, 0, st>>>(d, a, b);
+      if (h->gcap > 0 || h->nfix > 0) k_force<true><<<h->num_sms * h->force_bps, kThreads, 0, st>>>(d, a, b);
+      else k_force<false><<<h->num_sms * h->force_bps, kThreads, 0, st>>>(d, a, b);
     }
     cudaStreamWaitEvent(st, h->ev_join, 0);
   }
@@ -2647,7 +2651,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   CK(cudaEventCreateWithFlags(&h->ev_snap_done, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
-  for (int k = 0; k < kChunks; k++) CK(cudaEventCreateWithFlags(&h->ev_chunk[k], cudaEventDisableTiming));
+  for (int k = 0; k < kMaxChunks; k++) CK(cudaEventCreateWithFlags(&h->ev_chunk[k], cudaEventDisableTiming));
   int N = c.n_capacity;
   if (c.n_fixed_capacity < 0) return bad("n_fixed_capacity must be >= 0");
   if (c.n_fixed_capacity > 0 && nper > 0) {
@@ -3812,6 +3816,28 @@ int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatch
   return 0;
 }
 
+int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm) {
+  if (!h) return SDEM_E_ARG;
+  if (pipeline_chunks < 0 || pipeline_chunks > kMaxChunks || force_blocks_per_sm < 0 || force_blocks_per_sm > 8)
+    return set_err(h, SDEM_E_ARG, "sdem_set_launch: pipeline_chunks in 1..4, force_blocks_per_sm in 1..8 (0 keeps)");
+  const int nc = pipeline_chunks ? pipeline_chunks : h->nchunk;
+  const int fb = force_blocks_per_sm ? force_blocks_per_sm : h->force_bps;
+  if (nc != h->nchunk || fb != h->force_bps) {
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graph(h);   // the next step captures the new shape
+    h->nchunk = nc;
+    h->force_bps = fb;
+  }
+  return 0;
+}
+
+int sdem_get_launch(sdem_h* h, int* pipeline_chunks, int* force_blocks_per_sm) {
+  if (!h || !pipeline_chunks || !force_blocks_per_sm) return SDEM_E_ARG;
+  *pipeline_chunks = h->nchunk;
+  *force_blocks_per_sm = h->force_bps;
+  return 0;
+}
+
 int sdem_probe_fp64_peak(long long iters, double* dfma_per_s, double* ms) {
   if (iters <= 0 || !dfma_per_s || !ms) return SDEM_E_ARG;
   int dev = 0, sms = 0;
@@ -3868,7 +3894,7 @@ void sdem_destroy(sdem_h* h) {
   for (int b = 0; b < 2; b++)
     if (h->ev_step[b]) cudaEventDestroy(h->ev_step[b]);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
-  for (int k = 0; k < kChunks; k++)
+  for (int k = 0; k < kMaxChunks; k++)
     if (h->ev_chunk[k]) cudaEventDestroy(h->ev_chunk[k]);
   if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -3983,9 +4009,14 @@ int batch_capture(sdem_batch* b, sdem_batch::Group& G) {
 extern "C" {
 
 int sdem_batch_create(int n, sdem_h* const* members, sdem_batch** out) {
+  return sdem_batch_create_grouped(n, members, 0, out);
+}
+
+int sdem_batch_create_grouped(int n, sdem_h* const* members, int group_size, sdem_batch** out) {
   if (!out) return SDEM_E_ARG;
   *out = nullptr;
-  if (n < 1 || !members) return SDEM_E_ARG;
+  if (n < 1 || !members || group_size < 0) return SDEM_E_ARG;
+  const int gsz = group_size ? group_size : SDEM_BATCH_GROUP;
   for (int k = 0; k < n; k++)
     if (!members[k]) return SDEM_E_ARG;
   {
@@ -3996,7 +4027,7 @@ int sdem_batch_create(int n, sdem_h* const* members, sdem_batch** out) {
   sdem_batch* b = new sdem_batch();
   *out = b;
   b->m.assign(members, members + n);
-  const int ng = (n + SDEM_BATCH_GROUP - 1) / SDEM_BATCH_GROUP;
+  const int ng = (n + gsz - 1) / gsz;
   b->g.resize(ng);
   for (int q = 0; q < ng; q++) {
     sdem_batch::Group& G = b->g[q];

@@ -4,7 +4,7 @@
 ! Compiled with the reference's sources when it is built with -DSDEM_GPU
 ! (before Prtcl_DEMSystem.o) and linked with -lsdem_gpu -lcudart.  It depends
 ! on no module of the reference: the driver code that packs the reference's
-! arrays into these calls is sdem_gpu_dems_iterate.inc (next to this file).
+! arrays into these calls is Prtcl_GPU_Driver.f90 (next to this file).
 !
 ! Conventions (those of sdem_gpu.h):
 !   - a handle (sdem_h*, sdem_batch*) and a device or stream address (void*,
@@ -220,6 +220,18 @@ module Prtcl_GPU
       real(c_double), intent(out) :: dfma_per_s, ms
     end function sdem_probe_fp64_peak
 
+    integer(c_int) function sdem_set_launch(h, pipeline_chunks, force_blocks_per_sm) bind(C, name="sdem_set_launch")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), value :: pipeline_chunks, force_blocks_per_sm
+    end function sdem_set_launch
+
+    integer(c_int) function sdem_get_launch(h, pipeline_chunks, force_blocks_per_sm) bind(C, name="sdem_get_launch")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), intent(out) :: pipeline_chunks, force_blocks_per_sm
+    end function sdem_get_launch
+
     integer(c_int) function sdem_count_contacts_noalloc(cfg, max_radius, n, d_posR, d_counts, stream) &
         bind(C, name="sdem_count_contacts_noalloc")
       import :: c_int, c_ptr, c_double, sdem_cfg
@@ -245,6 +257,15 @@ module Prtcl_GPU
       type(c_ptr), intent(in) :: members(*)
       type(c_ptr), intent(out) :: b
     end function sdem_batch_create
+
+    integer(c_int) function sdem_batch_create_grouped(n, members, group_size, b) &
+        bind(C, name="sdem_batch_create_grouped")
+      import :: c_int, c_ptr
+      integer(c_int), value :: n
+      type(c_ptr), intent(in) :: members(*)
+      integer(c_int), value :: group_size
+      type(c_ptr), intent(out) :: b
+    end function sdem_batch_create_grouped
 
     integer(c_int) function sdem_batch_step_async(b, nsteps) bind(C, name="sdem_batch_step_async")
       import :: c_int, c_ptr
