@@ -80,7 +80,7 @@ constexpr int kChunks = SDEM_PIPELINE_CHUNKS;   // search/force pipeline chunks 
 constexpr int kMaxChunks = 4;                   // most chunks sdem_set_launch accepts
 constexpr int kForceBlocksPerSM = 3;            // k_force blocks per SM in the pipeline (default)
 #ifndef SDEM_SEARCH_PREFETCH
-#define SDEM_SEARCH_PREFETCH 1     // k_search requests the next candidate's record before testing one
+#define SDEM_SEARCH_PREFETCH 0     // 1: k_search requests the next candidate's record before testing one
 #endif
 constexpr int kMaxLevels = 6;     // hierarchical search levels (Init_Munjiza_Hrchl caps at 6)
 

@@ -73,7 +73,7 @@ def test_contact_sets_over_1000_steps_resynchronised(settled_1m):
         g.step(1)                      # step k of the free run ...
         o.step(1)                      # ... and the oracle's step from the same inputs
         done = k
-        seen.append((k, assert_step_matches(g, o, what=f"step {k}")))
+        seen.append((k, assert_step_matches(g, o, what=f"step {k}", pre=st, case=case)))
         o.close()
     g.close()
     print("resynchronised checkpoints:", seen)
