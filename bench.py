@@ -45,15 +45,15 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s, 1M Hertz spheres"
 UNIT = "particle-steps/s"
 # From the ncu captures in profiles/ (each file gives its command):
-FORCE_DRAM_BYTES_PER_CONTACT = 394.0     # k_force: dram__bytes_read.sum + dram__bytes_write.sum per contact
+# profiles/kernels_hertz_poly_settled_1m.txt, one step of the settled 1M bed.
+FORCE_DRAM_BYTES_PER_CONTACT = 418.9     # k_force: dram__bytes_read.sum + dram__bytes_write.sum per contact
 FP64_INST_PER_SM_CLK = 2.0               # DADD/DMUL/DFMA thread operations per SM per clock (FP64 pipe)
 NUM_SMS = 152
-# Executed DADD + DMUL + DFMA thread instructions of the step's kernels
-# (profiles/fp64_counts_hertz_poly_settled_1m.txt), modelled per particle-particle
-# contact, per sphere and per wall contact.
-FP64_PER_CONTACT = {"k_force": 133.8, "k_gather": 24.0}
-FP64_PER_SPHERE = {"k_integrate": 57.0, "k_gather": 2.3, "k_bin": 6.0, "k_wall_detect": 0.6}
-FP64_PER_WALL_CONTACT = {"k_wall_force": 120.0}
+# Executed DADD + DMUL + DFMA thread instructions of the step's kernels,
+# modelled per particle-particle contact, per sphere and per wall contact.
+FP64_PER_CONTACT = {"k_force": 136.1, "k_gather": 24.2}
+FP64_PER_SPHERE = {"k_integrate": 51.0, "k_bin": 3.0, "k_wall_detect": 0.74}
+FP64_PER_WALL_CONTACT = {"k_wall_force": 123.3, "k_gather": 12.0}
 
 # name -> (metric, default particles, base seed)
 WORKLOADS = {
