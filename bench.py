@@ -482,9 +482,9 @@ def our_arm(args):
 def sandboxes_arm(args):
     """The batched workload (its own line): `--instances` sandboxes of
     2,000-50,000 spheres with their own materials, contact models and boxes
-    (sdem_gb300.beds.sandbox_case, parameters from seed 4).  They first fall
-    into contact (`--contact-steps` batch steps: the lattices collapse onto
-    their floors), then the autotuner (sdem_gb300.tune) picks each size
+    (sdem_gb300.beds.sandbox_case, parameters from seed 4), deposited as
+    beds in contact (`--sandbox-layout lattice`: the configuration's falling
+    lattice), stepped `--contact-steps` batch steps, then the autotuner (sdem_gb300.tune) picks each size
     class's launch shape and the batch's group size.  Timed, from that state:
     (a) the tuned batch, (b) the batch with the default shapes, (c) one
     instance after another (each instance's steps, then the next: one launch
@@ -496,7 +496,7 @@ def sandboxes_arm(args):
     from sdem_gb300.capi import DEMBatch, DEMSystem
     torch.cuda.set_device(0)
     rng = np.random.default_rng(4)
-    cases = [beds.sandbox_case(rng, i) for i in range(args.instances)]
+    cases = [beds.sandbox_case(rng, i, layout=args.sandbox_layout) for i in range(args.instances)]
     total = sum(c.particles.n for c in cases)
     members = [DEMSystem(c) for c in cases]
     t0 = time.perf_counter()
@@ -552,7 +552,8 @@ def sandboxes_arm(args):
             "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": t_tuned / K * 1e3,
             "higher_is_better": True, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "sandboxes", "instances": args.instances, "particles": total,
-                       "contact_steps": args.contact_steps, "contacts_at_start": contacts,
+                       "layout": args.sandbox_layout, "contact_steps": args.contact_steps,
+                       "contacts_at_start": contacts,
                        "contacts_per_particle": contacts / total, "models": {
                            "hertz": sum(1 for c in cases if c.opts.cf_type == props_cft_nlin()),
                            "lsd": sum(1 for c in cases if c.opts.cf_type != props_cft_nlin())}},
@@ -731,8 +732,10 @@ def main():
                          "sandboxes: the batched workload; surrogate: the learned surrogate against the plain "
                          "DEM (each its own line)")
     ap.add_argument("--instances", type=int, default=512)
-    ap.add_argument("--contact-steps", type=int, default=4000,
-                    help="sandboxes: batch steps before timing, so that the beds are in contact")
+    ap.add_argument("--contact-steps", type=int, default=1000,
+                    help="sandboxes: batch steps before timing")
+    ap.add_argument("--sandbox-layout", default="deposited", choices=["deposited", "lattice"],
+                    help="sandboxes: deposited beds in contact (default) or the falling lattice")
     ap.add_argument("--train-beds", type=int, default=3)
     ap.add_argument("--train-iters", type=int, default=300)
     ap.add_argument("--strides", type=int, default=5)

@@ -677,14 +677,19 @@ def fixed_floor_case(n: int, seed: int, **kw) -> Case:
     return Case(f"fixedfloor_{n}_{seed}", opts, case.tables, walls, parts, fixed=fixed)
 
 
-def sandbox_case(rng: np.random.Generator, index: int, n_lo: int = 2000, n_hi: int = 50000) -> Case:
+def sandbox_case(rng: np.random.Generator, index: int, n_lo: int = 2000, n_hi: int = 50000,
+                 layout: str = "lattice") -> Case:
     """One sandbox of the batched workload: n ~ U{n_lo..n_hi} spheres with d
     uniform in [0.8, 1.2] mm (five types, density 2500 kg/m^3), sliding
     friction U(0.1, 0.5), restitution U(0.5, 0.95), linear spring-dashpot or
     Hertz-Mindlin by a coin flip, dt = 2e-6 s, AB2; a jittered simple-cubic
     lattice (pitch 1.3 d_max) filling a box of aspect ratios x:y:z = a:1:b with
     a, b ~ U(0.5, 2), five infinite walls, velocities U(-0.05, 0.05) m/s.  The
-    parameters are drawn from `rng` in a fixed order."""
+    parameters are drawn from `rng` in a fixed order.  layout="deposited"
+    puts the same spheres, on the same footprint, as a bed already in
+    contact: deposited_positions (column grid spacing 1.1 d_max, jitter
+    0.04 d_max), each sphere resting on its support without overlap, at
+    rest."""
     n = int(rng.integers(n_lo, n_hi + 1))
     mu = float(rng.uniform(0.1, 0.5))
     e_n = float(rng.uniform(0.5, 0.95))
@@ -713,6 +718,14 @@ def sandbox_case(rng: np.random.Generator, index: int, n_lo: int = 2000, n_hi: i
     box = (nx * pitch + 0.4e-3, (ny + 2) * pitch + 0.4e-3, nz * pitch + 0.4e-3)
     ptype = r.integers(1, ntypes + 1, size=n).astype(np.int32)
     vel = r.uniform(-0.05, 0.05, size=(n, 3))
+    if layout == "deposited":
+        dmax = float(diam[-1])
+        tall = (box[0], 1.0e3, box[2])
+        pos = deposited_positions(r, diam[ptype - 1], tall, 0.0, 0.0, 1.1 * dmax, 0.04 * dmax)
+        box = (box[0], float(pos[:, 1].max()) + 3.0 * dmax, box[2])
+        vel = np.zeros((n, 3))
+    elif layout != "lattice":
+        raise ValueError(f"sandbox_case: unknown layout {layout!r}")
     opts = Options(dt=2.0e-6, minpoint=(0.0, 0.0, 0.0), maxpoint=box, cf_type=cf, pi_method=2, pri_method=2)
     parts = new_particles(pos, ptype, tables.radius, vel, opts.tsize, opts.rsize)
     walls = box_walls(opts.minpoint, opts.maxpoint, infinite=True, base_wall_id=opts.base_wall_id, skip_axes=())
