@@ -274,7 +274,7 @@ def reference_arm(args):
 STATE_FIELDS = ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta", "rotVel", "rotAcc")
 
 
-def e2e_run(case, K, pinned: bool, barrier):
+def e2e_run(case, K, pinned: bool, barrier, shape=None):
     """The metric through the C ABI with host buffers: upload of the state,
     K x (sdem_step_async(h,1) + the step's counters read back), download of
     the state.  pinned: page-locked host arrays; else ordinary (pageable)
@@ -284,6 +284,9 @@ def e2e_run(case, K, pinned: bool, barrier):
     from sdem_gb300 import beds
     from sdem_gb300.capi import DEMSystem
     sys2 = DEMSystem(case)
+    if shape:
+        from sdem_gb300 import tune
+        tune.apply(sys2, shape)
     sys2.step(1)
     st0 = sys2.state()
     if pinned:
@@ -345,7 +348,12 @@ def our_arm(args):
     case, desc = make_case(args.workload, args.n or n_def, seed)
     n = case.particles.n
     fp64_peak = probe_fp64_peak()          # the FP64 pipe of this GPU, measured now (DFMA chains)
+    # launch shape by the autotuner (results do not depend on it; cached per size class)
+    from sdem_gb300 import tune
+    shape = tune.tune_handle(case) if not args.no_tune else None
     sysm = DEMSystem(case)
+    if shape:
+        tune.apply(sysm, shape)
     sysm.step(args.warmup)
     stream = torch.cuda.ExternalStream(sysm.stream())
     K = args.steps
@@ -406,7 +414,7 @@ def our_arm(args):
         Ke = args.e2e_steps
         runs = {}
         for pinned in (True, False):
-            el, h2d, d2h = e2e_run(case, Ke, pinned, barrier)
+            el, h2d, d2h = e2e_run(case, Ke, pinned, barrier, shape)
             _, el, _ = replicas.aggregate(el, n, Ke, device="cuda")
             runs[pinned] = {"value": n_all * Ke / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / Ke),
                             "d2h_bytes_per_step": int(d2h / Ke), "steps": Ke}
@@ -442,6 +450,10 @@ def our_arm(args):
             "e2e": e2e,
             "e2e_pageable": e2e_pageable,
             "gpu_launches": launches,
+            "tuning": ({"pipeline_chunks": shape["pipeline_chunks"],
+                        "force_blocks_per_sm": shape["force_blocks_per_sm"],
+                        "ms_per_step_tried": shape["tried"], "note": "sdem_gb300.tune.tune_handle, cached by size "
+                        "class; results are bit-identical for every launch shape"} if shape else None),
             "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic,
                          "algorithmic_bytes": "80 B per contact x contacts per launch",
@@ -727,6 +739,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=-1,
                     help="steps of the end-to-end run (default: --steps; 0 skips it)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shape")
     ap.add_argument("--workload", default="hertz_poly_1m", choices=[*WORKLOADS, "sandboxes", "surrogate"],
                     help="hertz_poly_1m (the headline), hertz_poly_1m_deposited, lsd_mono_20k, hopper_4m; "
                          "sandboxes: the batched workload; surrogate: the learned surrogate against the plain "
