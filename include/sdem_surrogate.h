@@ -115,6 +115,14 @@ typedef struct sdem_sg_epilogue {
 int sdem_sg_gemm(int I, int J, int R, const sdem_sg_operand* a, const sdem_sg_operand* b,
                  const sdem_sg_epilogue* ep, int splits, float* partial, void* stream);
 
+/* Which tensor-core kernel sdem_sg_gemm uses for the forms without
+ * transposed operands or split reductions: 1 (default) the tcgen05/TMEM
+ * kernel, 0 the warp-level mma.sync kernel (kept for the other forms). */
+int sdem_sg_set_tensor_path(int use_tcgen05);
+/* Number of tcgen05 GEMM blocks whose bounded mbarrier wait expired (0
+ * expected; such a block writes zeros instead of its products). */
+int sdem_sg_tensor_timeouts(unsigned int* count);
+
 /* out[i] (J floats) = (accumulate ? out[i] : 0) + sum over e in row_off[i] ..
  * row_off[i+1] of x[perm ? perm[e] : e]; out_bf = bf16(out) when given.
  * Rows are summed in list order (deterministic). */

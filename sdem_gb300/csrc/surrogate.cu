@@ -278,6 +278,173 @@ __global__ void __launch_bounds__(GT) k_gemm(int I, int J, int R, Operand A, Ope
                 }
 }
 
+// ------------------------------------------------------ tcgen05 GEMM
+// The same C = A . B^T with the fused epilogue on the 5th-generation tensor
+// cores, for the forms without transposed operands or split reductions (the
+// forward layers and the input gradients): one CTA of 128 threads per
+// 128 x 128 output tile.  The threads stage 32-deep slices of A and B
+// (row-gathered, segmented, as k_gemm) in shared memory in the UMMA K-major
+// layout without swizzle -- core matrices of 8 rows x 16 bytes, (m-group,
+// k-group) at k-group * 2048 + m-group * 128 bytes, so the descriptor's
+// leading (K) byte offset is 2048 and its stride (M/N) byte offset 128.  One
+// thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> fp32, M = N = 128,
+// K = 16, two per slice) into a 128-column fp32 accumulator in tensor memory;
+// tcgen05.commit arrives on the slice buffer's mbarrier, so the next slice is
+// staged into the other buffer while the tensor cores work (double
+// buffering).  After the last slice each warp reads its 32 accumulator rows
+// with tcgen05.ld and applies the epilogue.  Every mbarrier wait is bounded:
+// on expiry the CTA counts a timeout (sdem_sg_tensor_timeouts) and finishes.
+constexpr int TC_M = 128, TC_N = 128, TC_K = 32, TC_T = 128;
+constexpr int TC_TILE = TC_M * TC_K * 2;          // bytes of one staged operand slice (8 KB)
+// A0 A1 B0 B1 take 32 KB; the allocation is 64 KB so that every address a
+// descriptor of this layout can reach, under either reading of its two byte
+// offsets, stays inside the CTA's shared memory.
+constexpr int TC_SMEM = 64 * 1024;
+constexpr long long TC_WAIT_LIMIT = 1ll << 26;
+constexpr uint32_t TC_IDESC = (1u << 4)                        // D: fp32
+                              | (1u << 7) | (1u << 10)         // A, B: bf16
+                              | ((uint32_t)(TC_N >> 3) << 17)  // N / 8
+                              | ((uint32_t)(TC_M >> 4) << 24); // M / 16; both operands K-major
+__device__ unsigned int g_tc_timeouts = 0;
+int g_tc_enabled = 1;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+    const uint64_t lbo = 2048, sbo = 128;
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (long long it = 0; it < TC_WAIT_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.u32 %0, 1, 0, P;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// rows d0.. (128) x reduction r0..r0+31 of an operand into the core-matrix layout
+__device__ __forceinline__ void tc_stage(uint8_t* S, const Operand& op, int d0, int ndim, int r0, int rend) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int c = threadIdx.x + q * TC_T;   // 512 chunks of 8 elements
+        const int d = c >> 2, kg = c & 3;
+        const int gd = d0 + d, gr = r0 + kg * 8;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (gd < ndim && gr < rend) v = __ldg(chunk_addr(op, gd, gr));
+        *reinterpret_cast<uint4*>(S + kg * 2048 + (d >> 3) * 128 + (d & 7) * 16) = v;
+    }
+}
+
+__global__ void __launch_bounds__(TC_T, 1) k_gemm_tc(int I, int J, int R, Operand A, Operand B,
+                                                      sdem_sg_epilogue ep) {
+    extern __shared__ __align__(1024) uint8_t tc_smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_slot;
+    uint8_t* As0 = tc_smem;
+    uint8_t* Bs0 = tc_smem + 2 * TC_TILE;
+    const int i0 = blockIdx.x * TC_M, j0 = blockIdx.y * TC_N;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(TC_N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const int nch = (R + TC_K - 1) / TC_K;
+    bool ok = true;
+    if (nch > 0) {
+        tc_stage(As0, A, i0, I, 0, R);
+        tc_stage(Bs0, B, j0, J, 0, R);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+    }
+    for (int c = 0; c < nch; ++c) {
+        const int b = c & 1;
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t a_base = smem_u32(As0 + b * TC_TILE), b_base = smem_u32(Bs0 + b * TC_TILE);
+#pragma unroll
+            for (int kk = 0; kk < TC_K / 16; ++kk) {
+                const uint64_t ad = umma_desc(a_base + kk * 2 * 2048), bd = umma_desc(b_base + kk * 2 * 2048);
+                const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(TC_IDESC), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&mbar[b]))
+                         : "memory");
+        }
+        if (c + 1 < nch) {
+            // the other buffer was read by slice c-1's MMAs: wait for them
+            if (c >= 1 && ok) ok = mbar_wait(smem_u32(&mbar[b ^ 1]), ((c - 1) >> 1) & 1);
+            tc_stage(As0 + (b ^ 1) * TC_TILE, A, i0, I, (c + 1) * TC_K, R);
+            tc_stage(Bs0 + (b ^ 1) * TC_TILE, B, j0, J, (c + 1) * TC_K, R);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        }
+        __syncthreads();
+    }
+    if (nch > 0 && ok) ok = mbar_wait(smem_u32(&mbar[(nch - 1) & 1]), ((nch - 1) >> 1) & 1);
+    if (!ok && lane == 0) atomicAdd(&g_tc_timeouts, 1u);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const int gi = i0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int cc = 0; cc < TC_N / 32; ++cc) {
+        uint32_t r[32];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (gi >= I) continue;
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+            const int gj = j0 + cc * 32 + q;
+            if (gj >= J) continue;
+            float v = (nch > 0 && ok) ? __uint_as_float(r[q]) : 0.f;
+            if (ep.bias) v += ep.bias[gj];
+            if (ep.relu) v = fmaxf(v, 0.f);
+            if (ep.mask && !bf16_positive(ep.mask[(size_t)gi * ep.ld_mask + gj])) v = 0.f;
+            if (ep.out) {
+                float* o = ep.out + (size_t)gi * ep.ld_out + gj;
+                *o = ep.accumulate ? *o + v : v;
+            }
+            if (ep.out_bf) ep.out_bf[(size_t)gi * ep.ld_out_bf + gj] = bf16_bits(v);
+            if (ep.resid) {
+                const float w = ep.resid[(size_t)gi * ep.ld_resid + gj] + v;
+                if (ep.res_out) ep.res_out[(size_t)gi * ep.ld_res_out + gj] = w;
+                if (ep.res_out_bf) ep.res_out_bf[(size_t)gi * ep.ld_res_out_bf + gj] = bf16_bits(w);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_N) : "memory");
+}
+
 __global__ void k_split_reduce(int I, int J, int splits, const float* __restrict__ partial, float* __restrict__ out,
                                int ld_out, int accumulate) {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -514,6 +681,18 @@ int sdem_sg_gemm(int I, int J, int R, const sdem_sg_operand* a, const sdem_sg_op
     const int nsplit = R > 0 ? (int)((R + rchunk - 1) / rchunk) : 1;
     const dim3 grid(blocks(I, BM), blocks(J, BN), nsplit);
     if (grid.y > 65535 || grid.z > 65535) return SDEM_SG_E_ARG;
+    if (nsplit == 1 && g_tc_enabled && !A.trans && !B.trans) {
+        static bool attr = false;
+        if (!attr) {
+            if (cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) != cudaSuccess)
+                return SDEM_SG_E_CUDA;
+            attr = true;
+        }
+        const dim3 tgrid(blocks(I, TC_M), blocks(J, TC_N));
+        if (tgrid.y > 65535) return SDEM_SG_E_ARG;
+        k_gemm_tc<<<tgrid, TC_T, TC_SMEM, st(stream)>>>(I, J, R, A, B, *ep);
+        return launched();
+    }
     if (nsplit == 1) {
         k_gemm<<<grid, GT, 0, st(stream)>>>(I, J, R, A, B, *ep, (int)rchunk, nullptr);
         return launched();
@@ -524,6 +703,18 @@ int sdem_sg_gemm(int I, int J, int R, const sdem_sg_operand* a, const sdem_sg_op
     k_split_reduce<<<blocks((long long)I * J, 256), 256, 0, st(stream)>>>(I, J, nsplit, partial, ep->out, ep->ld_out,
                                                                        ep->accumulate);
     return launched();
+}
+
+int sdem_sg_set_tensor_path(int use_tcgen05) {
+    if (use_tcgen05 != 0 && use_tcgen05 != 1) return SDEM_SG_E_ARG;
+    g_tc_enabled = use_tcgen05;
+    return SDEM_SG_OK;
+}
+
+int sdem_sg_tensor_timeouts(unsigned int* count) {
+    if (!count) return SDEM_SG_E_ARG;
+    return cudaMemcpyFromSymbol(count, g_tc_timeouts, sizeof(unsigned int)) == cudaSuccess ? SDEM_SG_OK
+                                                                                         : SDEM_SG_E_CUDA;
 }
 
 int sdem_sg_segsum(int nrows, int J, const int* row_off, const int* perm, const float* x, int ldx, float* out,

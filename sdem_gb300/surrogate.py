@@ -53,7 +53,8 @@ OVERLAP_GAIN = 100.0
 
 EXPORTED = ("sdem_sg_cells", "sdem_sg_edge_count", "sdem_sg_edge_fill", "sdem_sg_node_features", "sdem_sg_gemm",
             "sdem_sg_segsum", "sdem_sg_gather_add", "sdem_sg_colsum_blocks", "sdem_sg_colsum", "sdem_sg_mse",
-            "sdem_sg_adam", "sdem_sg_to_bf16", "sdem_sg_advance")
+            "sdem_sg_adam", "sdem_sg_to_bf16", "sdem_sg_advance", "sdem_sg_set_tensor_path",
+            "sdem_sg_tensor_timeouts")
 
 
 class SgGrid(C.Structure):
@@ -106,6 +107,8 @@ def load(path: str = LIB_PATH):
         "sdem_sg_adam": [LL, P, P, P, P, P, F, F, F, F, F, I, P],
         "sdem_sg_to_bf16": [LL, P, P, P],
         "sdem_sg_advance": [I, P, I, D, D, D, D, D, C.POINTER(SgBox), P, P, P, P],
+        "sdem_sg_set_tensor_path": [I],
+        "sdem_sg_tensor_timeouts": [C.POINTER(C.c_uint)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -159,6 +159,45 @@ def test_gemm_operand_forms(sg_lib):
     _close(_np(o16), _np(d16).T @ _np(z), np.abs(_np(d16)).T @ np.abs(_np(z)))
 
 
+def test_gemm_tcgen05_and_mma_sync_paths(sg_lib):
+    """The forward forms on both tensor paths: the tcgen05/TMEM kernel and
+    the warp-level mma.sync kernel, each against float64 products of the same
+    bf16 values within the fp32 accumulation bound, over ragged shapes (rows
+    not a multiple of the 128-row tile, 16 and 136 output columns, reductions
+    of 48 and 384 in up to three gathered segments); no bounded wait of the
+    tcgen05 kernel expires."""
+    rng = np.random.default_rng(7)
+    lib = sg.load()
+    shapes = [(1001, 136, 384, 3), (129, 16, 48, 1), (4096, 128, 256, 2), (77, 128, 128, 1)]
+    try:
+        for path in (1, 0):
+            assert lib.sdem_sg_set_tensor_path(path) == 0
+            for M, J, R, nseg in shapes:
+                rows = 300
+                w_seg = R // nseg
+                segs, parts = [], []
+                for k in range(nseg):
+                    src = _bf16(rng, (rows, w_seg))
+                    idx = torch.from_numpy(rng.integers(0, rows, M).astype(np.int32)).to(DEV)
+                    segs.append((src, 0, w_seg, w_seg, idx))
+                    parts.append(_np(src)[idx.cpu().numpy()])
+                A = sg._Op(0, *segs)
+                W = _bf16(rng, (J, R), 0.05)
+                bias = torch.from_numpy(rng.normal(size=J).astype(np.float32)).to(DEV)
+                out = torch.empty((M, J), dtype=torch.float32, device=DEV)
+                rc = lib.sdem_sg_gemm(M, J, R, ctypes.byref(A.o), ctypes.byref(sg._Op(0, (W, 0, R, R, None)).o),
+                                      ctypes.byref(sg._ep(bias=bias, out=out, ld_out=J)), 1, None, sg._stream())
+                assert rc == 0
+                x = np.concatenate(parts, axis=1)
+                w = _np(W)
+                want = x @ w.T + _np(bias)[None, :]
+                _close(_np(out), want, np.abs(x) @ np.abs(w).T + np.abs(_np(bias))[None, :])
+        cnt = ctypes.c_uint(99)
+        assert lib.sdem_sg_tensor_timeouts(ctypes.byref(cnt)) == 0 and cnt.value == 0
+    finally:
+        lib.sdem_sg_set_tensor_path(1)
+
+
 def _graph_sample(n, index, steps, seed):
     case, s = settled_sandbox(n, index, steps)
     st = s.state()
