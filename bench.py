@@ -628,6 +628,10 @@ def surrogate_arm(args):
     start = (runner.posR.clone(), runner.vel.clone(), runner.omega.clone())
     runner._surrogate_stride(runner.posR, runner.vel, runner.omega)     # warm-up
     phases, E = surrogate_phases(runner, net, sg, torch)
+    # the same forward on the warp-level mma.sync kernel, for comparison
+    assert net.lib.sdem_sg_set_tensor_path(0) == 0
+    phases_mma, _ = surrogate_phases(runner, net, sg, torch)
+    assert net.lib.sdem_sg_set_tensor_path(1) == 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(K):
@@ -657,7 +661,11 @@ def surrogate_arm(args):
             "surrogate_phases_ms": phases,
             "forward_tensor": {"flop": surrogate_forward_flop(case.particles.n, E),
                                "achieved_tflops": surrogate_forward_flop(case.particles.n, E) / phases["forward"] / 1e9,
-                               "peak_tflops": measured_bf16_tflops(), "peak_note": "bf16 dense, burst, of measured"},
+                               "peak_tflops": measured_bf16_tflops(), "peak_note": "bf16 dense, burst, of measured",
+                               "gemm": "tcgen05 (k_gemm_tc) for the forward layers",
+                               "mma_sync_forward_ms": phases_mma["forward"],
+                               "mma_sync_achieved_tflops": surrogate_forward_flop(case.particles.n, E)
+                               / phases_mma["forward"] / 1e9},
             "with_judge": {"strides": 2 * args.judge_every, "sim_s_per_s": run_strides * h / t_run,
                            "rewound_strides": stats["rewound_strides"],
                            "judged": stats["judged"], "fallbacks": stats["fallbacks"],
@@ -675,6 +683,77 @@ def surrogate_arm(args):
                     "stride-mean accelerations (semi-implicit Euler over the stride)"}
     print(json.dumps(line), flush=True)
     dem.close()
+
+
+def surrogate_gemm_arm(args):
+    """The surrogate's GEMM alone (its own line): the first edge layer of the
+    network's forward -- E rows gathered from node latents twice plus the
+    edge latents (three 128-wide segments, R = 384) times a 128 x 384 weight,
+    bias, ReLU, bf16 output -- and the second edge layer (R = 128), on the
+    tcgen05 kernel and on the mma.sync kernel.  E = --n rows (default 2^22),
+    node rows E / 24.  CUDA events on the current stream, median of 5 after 3
+    warm-ups; FLOP = 2 E R J."""
+    import ctypes
+    import torch
+    from sdem_gb300 import build, surrogate as sg
+    build.build()
+    torch.cuda.set_device(0)
+    lib = sg.load()
+    E = args.n or (1 << 22)
+    nodes = max(E // 24, 1)
+    L = 128
+    g = torch.Generator(device="cuda").manual_seed(11)
+    h = (torch.randn((nodes, L), device="cuda", generator=g) * 0.5).to(torch.bfloat16)
+    e = (torch.randn((E, L), device="cuda", generator=g) * 0.5).to(torch.bfloat16)
+    dst = torch.randint(0, nodes, (E,), device="cuda", generator=g, dtype=torch.int32)
+    src = torch.randint(0, nodes, (E,), device="cuda", generator=g, dtype=torch.int32)
+    W1 = (torch.randn((L, 3 * L), device="cuda", generator=g) * 0.05).to(torch.bfloat16)
+    W2 = (torch.randn((L, L), device="cuda", generator=g) * 0.05).to(torch.bfloat16)
+    bias = torch.zeros(L, device="cuda")
+    z = torch.empty((E, L), dtype=torch.bfloat16, device="cuda")
+    out = torch.empty((E, L), dtype=torch.float32, device="cuda")
+    A1 = sg._Op(0, (h, 0, L, L, dst), (h, 0, L, L, src), (e, 0, L, L, None))
+    B1 = sg._Op(0, (W1, 0, 3 * L, 3 * L, None))
+    A2 = sg._Op(0, (z, 0, L, L, None))
+    B2 = sg._Op(0, (W2, 0, L, L, None))
+    ep1 = sg._ep(bias=bias, relu=1, out_bf=z, ld_out_bf=L)
+    ep2 = sg._ep(out=out, ld_out=L)
+
+    def timed(A, B, R, ep):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ts = []
+        for k in range(8):
+            ev[0].record()
+            assert lib.sdem_sg_gemm(E, L, R, ctypes.byref(A.o), ctypes.byref(B.o), ctypes.byref(ep), 1, None,
+                                    sg._stream()) == 0
+            ev[1].record()
+            torch.cuda.synchronize()
+            if k >= 3:
+                ts.append(ev[0].elapsed_time(ev[1]))
+        return statistics.median(ts)
+
+    res = {}
+    for path, name in ((1, "tcgen05"), (0, "mma_sync")):
+        assert lib.sdem_sg_set_tensor_path(path) == 0
+        t1 = timed(A1, B1, 3 * L, ep1)
+        t2 = timed(A2, B2, L, ep2)
+        res[name] = {"edge_w1_ms": t1, "edge_w1_tflops": 2.0 * E * 3 * L * L / t1 / 1e9,
+                     "edge_w2_ms": t2, "edge_w2_tflops": 2.0 * E * L * L / t2 / 1e9}
+    assert lib.sdem_sg_set_tensor_path(1) == 0
+    cnt = ctypes.c_uint(0)
+    lib.sdem_sg_tensor_timeouts(ctypes.byref(cnt))
+    peak = measured_bf16_tflops()
+    tc = res["tcgen05"]
+    line = {"metric": "TFLOP/s, surrogate edge-layer GEMM (bf16 in, fp32 accumulate)",
+            "value": tc["edge_w1_tflops"], "unit": "TFLOP/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": "surrogate_gemm", "rows": E, "node_rows": nodes, "J": L,
+                       "R": [3 * L, L], "gather": "rows of two 128-wide segments gathered by edge index"},
+            "roofline": {"bound": "tensor", "kernel": "k_gemm_tc", "achieved": tc["edge_w1_tflops"], "peak": peak,
+                         "unit": "TFLOP/s", "frac": tc["edge_w1_tflops"] / peak,
+                         "peak_note": "bf16 dense, burst, of measured (MEASURED_PEAKS.json)"},
+            "paths": res, "tcgen05_wait_timeouts": cnt.value}
+    print(json.dumps(line), flush=True)
 
 
 def surrogate_forward_flop(n: int, E: int, latent: int = 128, layers: int = 6) -> float:
@@ -740,7 +819,8 @@ def main():
                     help="steps of the end-to-end run (default: --steps; 0 skips it)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shape")
-    ap.add_argument("--workload", default="hertz_poly_1m", choices=[*WORKLOADS, "sandboxes", "surrogate"],
+    ap.add_argument("--workload", default="hertz_poly_1m",
+                    choices=[*WORKLOADS, "sandboxes", "surrogate", "surrogate_gemm"],
                     help="hertz_poly_1m (the headline), hertz_poly_1m_deposited, lsd_mono_20k, hopper_4m; "
                          "sandboxes: the batched workload; surrogate: the learned surrogate against the plain "
                          "DEM (each its own line)")
@@ -758,6 +838,8 @@ def main():
         args.warmup = 3
     if args.workload == "sandboxes":
         sandboxes_arm(args)
+    elif args.workload == "surrogate_gemm":
+        surrogate_gemm_arm(args)
     elif args.workload == "surrogate":
         surrogate_arm(args)
     elif args.impl == "reference":
