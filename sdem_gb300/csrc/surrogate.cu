@@ -281,25 +281,27 @@ __global__ void __launch_bounds__(GT) k_gemm(int I, int J, int R, Operand A, Ope
 // ------------------------------------------------------ tcgen05 GEMM
 // The same C = A . B^T with the fused epilogue on the 5th-generation tensor
 // cores, for the forms without transposed operands or split reductions (the
-// forward layers and the input gradients): one CTA of 128 threads per
-// 128 x 128 output tile.  The threads stage 32-deep slices of A and B
-// (row-gathered, segmented, as k_gemm) in shared memory in the UMMA K-major
-// layout without swizzle -- core matrices of 8 rows x 16 bytes, (m-group,
-// k-group) at k-group * 2048 + m-group * 128 bytes, so the descriptor's
-// leading (K) byte offset is 2048 and its stride (M/N) byte offset 128.  One
-// thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> fp32, M = N = 128,
-// K = 16, two per slice) into a 128-column fp32 accumulator in tensor memory;
-// tcgen05.commit arrives on the slice buffer's mbarrier, so the next slice is
-// staged into the other buffer while the tensor cores work (double
-// buffering).  After the last slice each warp reads its 32 accumulator rows
-// with tcgen05.ld and applies the epilogue.  Every mbarrier wait is bounded:
-// on expiry the CTA counts a timeout (sdem_sg_tensor_timeouts) and finishes.
-constexpr int TC_M = 128, TC_N = 128, TC_K = 32, TC_T = 128;
-constexpr int TC_TILE = TC_M * TC_K * 2;          // bytes of one staged operand slice (8 KB)
-// A0 A1 B0 B1 take 32 KB; the allocation is 64 KB so that every address a
-// descriptor of this layout can reach, under either reading of its two byte
-// offsets, stays inside the CTA's shared memory.
-constexpr int TC_SMEM = 64 * 1024;
+// forward layers): one CTA of 256 threads per 128 x 128 output tile.
+//
+// Operand slices (128 rows x 32 reduction elements of A and of B) are
+// copied from global memory into shared memory with cp.async -- each 16-byte
+// chunk from its own row, so gathered rows and column segments need no
+// staging pass -- into the UMMA K-major layout without swizzle: core
+// matrices of 8 rows x 16 bytes, (row group, k group) at
+// k group * 2048 + row group * 128 bytes, i.e. the descriptor's leading (K)
+// byte offset 2048 and stride (M/N) byte offset 128.  Four slice buffers
+// form a ring: while the tensor cores work on slice c, the copies of slices
+// c+1..c+3 are in flight.  One thread issues tcgen05.mma (kind::f16, bf16 x
+// bf16 -> fp32, M = N = 128, K = 16, two per slice) into a 128-column fp32
+// accumulator in tensor memory, and tcgen05.commit arrives on the slice
+// buffer's mbarrier, which gates the buffer's next copy.  After the last
+// slice, warp w reads accumulator rows 32 (w mod 4).. and columns
+// 64 (w / 4).. with tcgen05.ld and applies the epilogue.  Every mbarrier wait
+// is bounded: on expiry the CTA counts a timeout (sdem_sg_tensor_timeouts)
+// and writes zeros.
+constexpr int TC_M = 128, TC_N = 128, TC_K = 32, TC_T = 256, TC_STAGES = 4;
+constexpr int TC_TILE = TC_M * TC_K * 2;          // bytes of one operand slice (8 KB)
+constexpr int TC_SMEM = TC_STAGES * 2 * TC_TILE;  // 64 KB: A and B slices of every stage
 constexpr long long TC_WAIT_LIMIT = 1ll << 26;
 constexpr uint32_t TC_IDESC = (1u << 4)                        // D: fp32
                               | (1u << 7) | (1u << 10)         // A, B: bf16
@@ -328,26 +330,30 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
+// cp.async of 16 bytes; src_bytes = 0 fills the chunk with zeros (nothing is read)
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+
 // rows d0.. (128) x reduction r0..r0+31 of an operand into the core-matrix layout
-__device__ __forceinline__ void tc_stage(uint8_t* S, const Operand& op, int d0, int ndim, int r0, int rend) {
+__device__ __forceinline__ void tc_copy(uint32_t S, const Operand& op, int d0, int ndim, int r0, int rend) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 2; ++q) {
         const int c = threadIdx.x + q * TC_T;   // 512 chunks of 8 elements
         const int d = c >> 2, kg = c & 3;
         const int gd = d0 + d, gr = r0 + kg * 8;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gd < ndim && gr < rend) v = __ldg(chunk_addr(op, gd, gr));
-        *reinterpret_cast<uint4*>(S + kg * 2048 + (d >> 3) * 128 + (d & 7) * 16) = v;
+        const bool in = gd < ndim && gr < rend;
+        const void* src = in ? (const void*)chunk_addr(op, gd, gr) : (const void*)op.ptr[0];
+        cp16(S + kg * 2048 + (d >> 3) * 128 + (d & 7) * 16, src, in ? 16u : 0u);
     }
 }
 
 __global__ void __launch_bounds__(TC_T, 1) k_gemm_tc(int I, int J, int R, Operand A, Operand B,
                                                       sdem_sg_epilogue ep) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t mbar[TC_STAGES];
     __shared__ uint32_t tmem_slot;
-    uint8_t* As0 = tc_smem;
-    uint8_t* Bs0 = tc_smem + 2 * TC_TILE;
+    const uint32_t As0 = smem_u32(tc_smem), Bs0 = As0 + TC_STAGES * TC_TILE;
     const int i0 = blockIdx.x * TC_M, j0 = blockIdx.y * TC_N;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) {
@@ -357,8 +363,8 @@ __global__ void __launch_bounds__(TC_T, 1) k_gemm_tc(int I, int J, int R, Operan
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])) : "memory");
+        for (int k = 0; k < TC_STAGES; ++k)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[k])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -367,20 +373,28 @@ __global__ void __launch_bounds__(TC_T, 1) k_gemm_tc(int I, int J, int R, Operan
     const uint32_t tmem = tmem_slot;
     const int nch = (R + TC_K - 1) / TC_K;
     bool ok = true;
-    if (nch > 0) {
-        tc_stage(As0, A, i0, I, 0, R);
-        tc_stage(Bs0, B, j0, J, 0, R);
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        __syncthreads();
+    // prologue: slices 0 .. STAGES-2 in flight (one commit group each, empty past the end)
+#pragma unroll
+    for (int k = 0; k < TC_STAGES - 1; ++k) {
+        if (k < nch) {
+            tc_copy(As0 + k * TC_TILE, A, i0, I, k * TC_K, R);
+            tc_copy(Bs0 + k * TC_TILE, B, j0, J, k * TC_K, R);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
     for (int c = 0; c < nch; ++c) {
-        const int b = c & 1;
+        const int b = c % TC_STAGES;
+        // this thread's copies of slice c have landed; make every thread's
+        // visible to the tensor cores
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(TC_STAGES - 2) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t a_base = smem_u32(As0 + b * TC_TILE), b_base = smem_u32(Bs0 + b * TC_TILE);
 #pragma unroll
             for (int kk = 0; kk < TC_K / 16; ++kk) {
-                const uint64_t ad = umma_desc(a_base + kk * 2 * 2048), bd = umma_desc(b_base + kk * 2 * 2048);
+                const uint64_t ad = umma_desc(As0 + b * TC_TILE + kk * 2 * 2048);
+                const uint64_t bd = umma_desc(Bs0 + b * TC_TILE + kk * 2 * 2048);
                 const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -392,23 +406,28 @@ __global__ void __launch_bounds__(TC_T, 1) k_gemm_tc(int I, int J, int R, Operan
                              smem_u32(&mbar[b]))
                          : "memory");
         }
-        if (c + 1 < nch) {
-            // the other buffer was read by slice c-1's MMAs: wait for them
-            if (c >= 1 && ok) ok = mbar_wait(smem_u32(&mbar[b ^ 1]), ((c - 1) >> 1) & 1);
-            tc_stage(As0 + (b ^ 1) * TC_TILE, A, i0, I, (c + 1) * TC_K, R);
-            tc_stage(Bs0 + (b ^ 1) * TC_TILE, B, j0, J, (c + 1) * TC_K, R);
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        // slice c + STAGES - 1 goes into the buffer slice c - 1 used: wait
+        // for that slice's MMAs first
+        const int nx = c + TC_STAGES - 1;
+        if (nx < nch) {
+            const int bx = nx % TC_STAGES;
+            if (c >= 1 && ok) ok = mbar_wait(smem_u32(&mbar[bx]), ((c - 1) / TC_STAGES) & 1);
+            tc_copy(As0 + bx * TC_TILE, A, i0, I, nx * TC_K, R);
+            tc_copy(Bs0 + bx * TC_TILE, B, j0, J, nx * TC_K, R);
         }
-        __syncthreads();
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
-    if (nch > 0 && ok) ok = mbar_wait(smem_u32(&mbar[(nch - 1) & 1]), ((nch - 1) >> 1) & 1);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    if (nch > 0 && ok) ok = mbar_wait(smem_u32(&mbar[(nch - 1) % TC_STAGES]), ((nch - 1) / TC_STAGES) & 1);
     if (!ok && lane == 0) atomicAdd(&g_tc_timeouts, 1u);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const int gi = i0 + warp * 32 + lane;
+    const int quarter = warp & 3, half = warp >> 2;
+    const int gi = i0 + quarter * 32 + lane;
 #pragma unroll 1
-    for (int cc = 0; cc < TC_N / 32; ++cc) {
+    for (int cc = 0; cc < 2; ++cc) {
+        const int col = half * 64 + cc * 32;
         uint32_t r[32];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32);
+        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)col;
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
@@ -421,7 +440,7 @@ __global__ void __launch_bounds__(TC_T, 1) k_gemm_tc(int I, int J, int R, Operan
         if (gi >= I) continue;
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
-            const int gj = j0 + cc * 32 + q;
+            const int gj = j0 + col + q;
             if (gj >= J) continue;
             float v = (nch > 0 && ok) ? __uint_as_float(r[q]) : 0.f;
             if (ep.bias) v += ep.bias[gj];
