@@ -295,8 +295,8 @@ __global__ void __launch_bounds__(GT) k_gemm(int I, int J, int R, Operand A, Ope
 // bf16 -> fp32, M = N = 128, K = 16, two per slice) into a 128-column fp32
 // accumulator in tensor memory, and tcgen05.commit arrives on the slice
 // buffer's mbarrier, which gates the buffer's next copy.  After the last
-// slice, warp w reads accumulator rows 32 (w mod 4).. and columns
-// 64 (w / 4).. with tcgen05.ld and applies the epilogue.  Every mbarrier wait
+// slice the accumulator goes through shared memory (tcgen05.ld by lane
+// quarter, then whole rows per warp) to a coalesced epilogue.  Every mbarrier wait
 // is bounded: on expiry the CTA counts a timeout (sdem_sg_tensor_timeouts)
 // and writes zeros.
 constexpr int TC_M = 128, TC_N = 128, TC_K = 32, TC_T = 256, TC_STAGES = 4;
@@ -421,11 +421,17 @@ __global__ void __launch_bounds__(TC_T, 1) k_gemm_tc(int I, int J, int R, Operan
     if (nch > 0 && ok) ok = mbar_wait(smem_u32(&mbar[(nch - 1) % TC_STAGES]), ((nch - 1) / TC_STAGES) & 1);
     if (!ok && lane == 0) atomicAdd(&g_tc_timeouts, 1u);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const int quarter = warp & 3, half = warp >> 2;
-    const int gi = i0 + quarter * 32 + lane;
+    // Epilogue in two column halves through shared memory (the slice buffers
+    // are free now): warp w moves accumulator rows 32 (w mod 4).. and columns
+    // 32 (w / 4).. of the half from tensor memory into a padded row-major
+    // tile, then every warp writes whole rows, so that the epilogue's global
+    // loads and stores are coalesced along j.
+    float* T = reinterpret_cast<float*>(tc_smem);   // 128 rows x 65 floats (33 KB)
+    const int quarter = warp & 3, sub = warp >> 2;
+    const bool valid = nch > 0 && ok;
 #pragma unroll 1
-    for (int cc = 0; cc < 2; ++cc) {
-        const int col = half * 64 + cc * 32;
+    for (int half = 0; half < 2; ++half) {
+        const int col = half * 64 + sub * 32;
         uint32_t r[32];
         const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)col;
         asm volatile(
@@ -437,26 +443,37 @@ __global__ void __launch_bounds__(TC_T, 1) k_gemm_tc(int I, int J, int R, Operan
               "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        if (gi >= I) continue;
+        const int row = quarter * 32 + lane;
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
-            const int gj = j0 + col + q;
-            if (gj >= J) continue;
-            float v = (nch > 0 && ok) ? __uint_as_float(r[q]) : 0.f;
-            if (ep.bias) v += ep.bias[gj];
-            if (ep.relu) v = fmaxf(v, 0.f);
-            if (ep.mask && !bf16_positive(ep.mask[(size_t)gi * ep.ld_mask + gj])) v = 0.f;
-            if (ep.out) {
-                float* o = ep.out + (size_t)gi * ep.ld_out + gj;
-                *o = ep.accumulate ? *o + v : v;
-            }
-            if (ep.out_bf) ep.out_bf[(size_t)gi * ep.ld_out_bf + gj] = bf16_bits(v);
-            if (ep.resid) {
-                const float w = ep.resid[(size_t)gi * ep.ld_resid + gj] + v;
-                if (ep.res_out) ep.res_out[(size_t)gi * ep.ld_res_out + gj] = w;
-                if (ep.res_out_bf) ep.res_out_bf[(size_t)gi * ep.ld_res_out_bf + gj] = bf16_bits(w);
+        for (int q = 0; q < 32; ++q) T[row * 65 + sub * 32 + q] = valid ? __uint_as_float(r[q]) : 0.f;
+        __syncthreads();
+        // 128 rows x 64 columns: warp w writes rows w, w+8, ...; lane l columns l and l+32
+#pragma unroll 1
+        for (int rr = warp; rr < TC_M; rr += TC_T / 32) {
+            const int gi = i0 + rr;
+            if (gi >= I) break;
+#pragma unroll
+            for (int h2 = 0; h2 < 2; ++h2) {
+                const int cj = h2 * 32 + lane;
+                const int gj = j0 + half * 64 + cj;
+                if (gj >= J) continue;
+                float v = T[rr * 65 + cj];
+                if (ep.bias) v += ep.bias[gj];
+                if (ep.relu) v = fmaxf(v, 0.f);
+                if (ep.mask && !bf16_positive(ep.mask[(size_t)gi * ep.ld_mask + gj])) v = 0.f;
+                if (ep.out) {
+                    float* o = ep.out + (size_t)gi * ep.ld_out + gj;
+                    *o = ep.accumulate ? *o + v : v;
+                }
+                if (ep.out_bf) ep.out_bf[(size_t)gi * ep.ld_out_bf + gj] = bf16_bits(v);
+                if (ep.resid) {
+                    const float w = ep.resid[(size_t)gi * ep.ld_resid + gj] + v;
+                    if (ep.res_out) ep.res_out[(size_t)gi * ep.ld_res_out + gj] = w;
+                    if (ep.res_out_bf) ep.res_out_bf[(size_t)gi * ep.ld_res_out_bf + gj] = bf16_bits(w);
+                }
             }
         }
+        __syncthreads();
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
