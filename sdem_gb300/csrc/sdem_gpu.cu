@@ -79,6 +79,9 @@ constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact r
 constexpr int kChunks = SDEM_PIPELINE_CHUNKS;   // search/force pipeline chunks per step (default)
 constexpr int kMaxChunks = 4;                   // most chunks sdem_set_launch accepts
 constexpr int kForceBlocksPerSM = 3;            // k_force blocks per SM in the pipeline (default)
+#ifndef SDEM_FORCE_MIN_BLOCKS
+#define SDEM_FORCE_MIN_BLOCKS 3    // k_force blocks of 256 threads per SM its register budget allows
+#endif
 #ifndef SDEM_SEARCH_PREFETCH
 #define SDEM_SEARCH_PREFETCH 0     // 1: k_search requests the next candidate's record before testing one
 #endif
@@ -1249,7 +1252,7 @@ __global__ void k_row_fill(Dev d, int s_begin, int s_end) {
 // Contacts of the rows [s_begin, s_end).  kOneSided: the search holds periodic
 // images or fixed spheres (pairs whose force goes to one sphere only).
 template <bool kOneSided>
-__global__ void __launch_bounds__(kThreads, 3) k_force(Dev d, int s_begin, int s_end) {
+__global__ void __launch_bounds__(kThreads, SDEM_FORCE_MIN_BLOCKS) k_force(Dev d, int s_begin, int s_end) {
   const int nloc = *d.n;
   const int c0 = d.row_off[s_begin], C = d.row_off[s_end];
   if (C > d.ccap) {
