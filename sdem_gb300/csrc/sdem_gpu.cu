@@ -119,6 +119,14 @@ struct __align__(32) GRec {
 };
 
 // ---------------------------------------------------------------------------
+// The force kernel's record of one contact for the gather, 96 bytes in one
+// place (the gather reads all three of a contact together).
+struct __align__(32) ContactRec {
+  dbl4 S;    // Fnij + Ftij, signed for the row's target
+  dbl4 M;    // Moment = Norm_v x Ftij (each side's gather scales it by its own radius)
+  dbl4 Mr;   // Mrij, signed for the row's target
+};
+
 // Device view of one handle, passed by value to every kernel.
 struct Dev {
   int ncap, n_launch;
@@ -180,7 +188,7 @@ struct Dev {
   const int* c_pgid_prev;
   dbl4* c_hist;
   const dbl4* c_hist_prev;
-  dbl4 *c_S, *c_M, *c_Mr;   // Fnij+Ftij and Mrij signed for the row's target; Moment = n x Ftij
+  struct ContactRec* c_rec;   // per contact: S = Fnij+Ftij and Mr = Mrij signed for the row's target, M = n x Ftij
   // contact history by the reference's bucket owner (Find_insert's bkt_id):
   // the lower id for particle-particle pairs, the local particle for a pair
   // with a periodic image; own_c lists this step's contacts of each owner id
@@ -737,7 +745,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
           d.row_partner[(size_t)cnt * nall + s] = q;
           if (q < nloc) {   // an image receives no force: it has no in-list
             int slot = atomicAdd(&d.in_cnt[q], 1);
-            if (slot < Kin) d.in_list[(size_t)slot * ncap + q] = ((unsigned)s << 6) | (unsigned)cnt;
+            if (slot < Kin) d.in_list[(size_t)q * Kin + slot] = ((unsigned)s << 6) | (unsigned)cnt;
             else raise(d, SDEM_E_CL_FULL, q);
           }
         } else {
@@ -1064,7 +1072,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32, SDEM_SEARCH_MIN_BLOCKS) k_s
           d.row_partner[(size_t)slot * nall + s_t] = q;
           if (q < nloc) {   // an image receives no force: it has no in-list
             const int is = atomicAdd(&d.in_cnt[q], 1);
-            if (is < Kin) d.in_list[(size_t)is * ncap + q] = ((unsigned)s_t << 6) | (unsigned)slot;
+            if (is < Kin) d.in_list[(size_t)q * Kin + is] = ((unsigned)s_t << 6) | (unsigned)slot;
             else raise(d, SDEM_E_CL_FULL, q);
           }
         } else {
@@ -1325,9 +1333,10 @@ __global__ void __launch_bounds__(kThreads, SDEM_FORCE_MIN_BLOCKS) k_force(Dev d
     // bits); the partner adds their negations
     const uint64_t sg = m_lo ? 0ull : fpi::kSign;
     auto flip = [sg](double v) { return fpi::from_bits(fpi::bits(v) ^ sg); };
-    d.c_S[c] = make_dbl4(flip(S.x), flip(S.y), flip(S.z), 0.0);
-    d.c_M[c] = sdem::d4(M, 0.0);   // Moment: each side's gather scales it by its own radius
-    d.c_Mr[c] = make_dbl4(flip(Mr.x), flip(Mr.y), flip(Mr.z), 0.0);
+    ContactRec& rec = d.c_rec[c];
+    rec.S = make_dbl4(flip(S.x), flip(S.y), flip(S.z), 0.0);
+    rec.M = sdem::d4(M, 0.0);   // Moment: each side's gather scales it by its own radius
+    rec.Mr = make_dbl4(flip(Mr.x), flip(Mr.y), flip(Mr.z), 0.0);
     const int os = atomicAdd(&d.own_cnt[owner], 1);
     if (os < d.Ko) d.own_c[(size_t)owner * d.Ko + os] = make_int2(c, partner);
     else raise(d, SDEM_E_CL_FULL, owner);
@@ -1403,7 +1412,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   if (nin <= 8) {
     unsigned u[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) u[k] = k < nin ? d.in_list[(size_t)k * ncap + p] : 0xffffffffu;
+    for (int k = 0; k < 8; k++) u[k] = k < nin ? d.in_list[(size_t)p * d.Kin + k] : 0xffffffffu;
     sort_net<8>(u);
 #pragma unroll
     for (int k = 0; k < 8; k++)
@@ -1415,7 +1424,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   } else if (nin <= 16) {
     unsigned u[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) u[k] = k < nin ? d.in_list[(size_t)k * ncap + p] : 0xffffffffu;
+    for (int k = 0; k < 16; k++) u[k] = k < nin ? d.in_list[(size_t)p * d.Kin + k] : 0xffffffffu;
     sort_net<16>(u);
 #pragma unroll
     for (int k = 0; k < 16; k++)
@@ -1427,7 +1436,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
   } else {
     unsigned e[kMaxK];
     for (int k = 0; k < nin; k++) {
-      unsigned v = d.in_list[(size_t)k * ncap + p];
+      unsigned v = d.in_list[(size_t)p * d.Kin + k];
       int j = k - 1;
       while (j >= 0 && e[j] > v) { e[j + 1] = e[j]; j--; }
       e[j + 1] = v;
@@ -1445,9 +1454,10 @@ __global__ void __launch_bounds__(kThreads) k_gather(Dev d) {
     const bool tgt = e < 0 || (e & 1);   // a wall record or p's own row: as stored
     dbl4 S, Ms, Mr;
     if (c >= 0) {
-      S = d.c_S[c];
-      Ms = d.c_M[c];
-      Mr = d.c_Mr[c];
+      const ContactRec& rec = d.c_rec[c];
+      S = rec.S;
+      Ms = rec.M;
+      Mr = rec.Mr;
     } else {
       const size_t at = (size_t)(-c - 1) * ncap + p;
       S = d.w_S[at];
@@ -2128,7 +2138,8 @@ struct sdem_h {
   // owner id, partner id, listed under the partner too
   struct UpRec { int owner, partner; bool both; dbl4 hist; };
   std::vector<UpRec> h_up;
-  dbl4 *c_hist[2] = {}, *c_S = nullptr, *c_M = nullptr, *c_Mr = nullptr;
+  dbl4* c_hist[2] = {};
+  ContactRec* c_rec = nullptr;
   int *wh_cnt[2] = {}, *wh_wall[2] = {};
   dbl4* wh_hist[2] = {};
   int *w_cnt = nullptr, *w_wall = nullptr, *wl = nullptr;
@@ -2368,9 +2379,7 @@ Dev make_dev(sdem_h* h) {
   d.c_pgid_prev = h->c_pgid[pv];
   d.c_hist = h->c_hist[cu];
   d.c_hist_prev = h->c_hist[pv];
-  d.c_S = h->c_S;
-  d.c_M = h->c_M;
-  d.c_Mr = h->c_Mr;
+  d.c_rec = h->c_rec;
   d.Ko = h->K;
   d.c_row = h->c_row;
   d.own_cnt = h->own_cnt[cu];
@@ -2721,9 +2730,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   h->ccap = std::max(1, c.cntct_list_size) * N;
   rc |= dalloc(h, &h->c_ogid, h->ccap);
   rc |= dalloc(h, &h->c_row, h->ccap);
-  rc |= dalloc(h, &h->c_S, h->ccap);
-  rc |= dalloc(h, &h->c_M, h->ccap);
-  rc |= dalloc(h, &h->c_Mr, h->ccap);
+  rc |= dalloc(h, &h->c_rec, h->ccap);
   size_t G = (size_t)c.max_gid + 1;
   for (int b = 0; b < 2; b++) {
     rc |= dalloc(h, &h->c_pgid[b], h->ccap);
