@@ -452,6 +452,7 @@ def our_arm(args):
             "gpu_launches": launches,
             "tuning": ({"pipeline_chunks": shape["pipeline_chunks"],
                         "force_blocks_per_sm": shape["force_blocks_per_sm"],
+                        "first_chunk_percent": shape["first_chunk_percent"],
                         "ms_per_step_tried": shape["tried"], "note": "sdem_gb300.tune.tune_handle, cached by size "
                         "class; results are bit-identical for every launch shape"} if shape else None),
             "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -545,8 +546,8 @@ def sandboxes_arm(args):
         return el
 
     t_tuned = run_batch(group["group_size"])
-    for m, (c, f) in zip(members, default_shape):
-        m.set_launch(c, f)
+    for m, (c, f, p) in zip(members, default_shape):
+        m.set_launch(c, f, p or -1)
     t_default = run_batch(0)
     for m in members:                        # each instance's own graphs, captured before timing
         m.step(4)
@@ -574,7 +575,8 @@ def sandboxes_arm(args):
             "instances_on_own_streams": total * K / t_streams,
             "tuning": {"group_size": group["group_size"], "group_sizes_ms": group["tried"],
                        "shapes": {k: {"pipeline_chunks": v["pipeline_chunks"],
-                                      "force_blocks_per_sm": v["force_blocks_per_sm"]} for k, v in shapes.items()},
+                                      "force_blocks_per_sm": v["force_blocks_per_sm"],
+                                      "first_chunk_percent": v["first_chunk_percent"]} for k, v in shapes.items()},
                        "seconds": t_tune, "contact_seconds": t_contact},
             "note": "host wall clock around synchronised runs of the same sandboxes in contact, in this order: "
                     "tuned batch, batch with default shapes, one instance after another, every instance on its "

@@ -278,13 +278,15 @@ int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatch
 
 /* ---- launch shape (no counterpart in the reference) -------------------------
  * The step's search/force pipeline runs in pipeline_chunks chunks of target
- * sort positions (1..4; default 2) and the force kernel with
- * force_blocks_per_sm blocks per SM in it (1..8; default 3).  Results are
- * bit-identical for every value (every order that matters is fixed by sort
- * positions); only the speed changes, which sdem_gb300/tune.py measures.  0
- * keeps a value; a change makes the next step capture its graphs again. */
-int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm);
-int sdem_get_launch(sdem_h* h, int* pipeline_chunks, int* force_blocks_per_sm);
+ * sort positions (1..4; default 2), the first of them holding
+ * first_chunk_percent percent of the targets (10..90; -1: even chunks, the
+ * default), and the force kernel with force_blocks_per_sm blocks per SM in
+ * it (1..8; default 3).  Results are bit-identical for every value (every
+ * order that matters is fixed by sort positions); only the speed changes,
+ * which sdem_gb300/tune.py measures.  0 keeps a value; a change makes the
+ * next step capture its graphs again. */
+int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm, int first_chunk_percent);
+int sdem_get_launch(sdem_h* h, int* pipeline_chunks, int* force_blocks_per_sm, int* first_chunk_percent);
 
 /* Measures the FP64 pipe: a kernel of eight independent DFMA chains per
  * thread (8 blocks of 256 threads per SM) runs `iters` iterations on the

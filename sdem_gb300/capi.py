@@ -148,8 +148,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sdem_count_contacts_noalloc.argtypes = [C.POINTER(SdemCfg), C.c_double, C.c_int, P, P, P]
     lib.sdem_selftest_fp64.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
     lib.sdem_probe_fp64_peak.argtypes = [C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double)]
-    lib.sdem_set_launch.argtypes = [P, C.c_int, C.c_int]
-    lib.sdem_get_launch.argtypes = [P, ip, ip]
+    lib.sdem_set_launch.argtypes = [P, C.c_int, C.c_int, C.c_int]
+    lib.sdem_get_launch.argtypes = [P, ip, ip, ip]
     lib.sdem_batch_create_grouped.argtypes = [C.c_int, C.POINTER(P), C.c_int, C.POINTER(P)]
     lib.sdem_snapshot_begin.argtypes = [P, ip, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp, C.c_int]
     lib.sdem_snapshot_end.argtypes = [P, ip]
@@ -368,14 +368,17 @@ class DEMSystem:
         self._check(self.lib.sdem_counter_sums(self.h, out))
         return {"pp": out[0], "pw": out[1], "steps": out[2]}
 
-    def set_launch(self, pipeline_chunks: int = 0, force_blocks_per_sm: int = 0) -> None:
-        """sdem_set_launch: the step's launch shape (results do not depend on it)."""
-        self._check(self.lib.sdem_set_launch(self.h, int(pipeline_chunks), int(force_blocks_per_sm)))
+    def set_launch(self, pipeline_chunks: int = 0, force_blocks_per_sm: int = 0, first_chunk_percent: int = 0) -> None:
+        """sdem_set_launch: the step's launch shape (results do not depend on
+        it); first_chunk_percent -1 restores even chunks, 0 keeps a value."""
+        self._check(self.lib.sdem_set_launch(self.h, int(pipeline_chunks), int(force_blocks_per_sm),
+                                             int(first_chunk_percent)))
 
     def get_launch(self) -> tuple:
-        a, b = C.c_int(), C.c_int()
-        self._check(self.lib.sdem_get_launch(self.h, C.byref(a), C.byref(b)))
-        return a.value, b.value
+        """(pipeline_chunks, force_blocks_per_sm, first_chunk_percent; 0 = even)."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.lib.sdem_get_launch(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def launch_count(self) -> int:
         n = C.c_longlong()

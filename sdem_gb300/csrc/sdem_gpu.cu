@@ -2155,6 +2155,7 @@ struct sdem_h {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chunk[kMaxChunks] = {};
   int nchunk = kChunks;                  // launch shape (sdem_set_launch); results do not depend on it
   int force_bps = kForceBlocksPerSM;
+  int first_pct = 0;                     // percent of the targets in the first chunk (0: even chunks)
   int cur = 0;  // buffer written by the next step
   // device scalars
   int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
@@ -2466,8 +2467,14 @@ int enqueue_step(sdem_h* h) {
   cudaStream_t s2 = ev ? st : h->stream2;
   // chunk boundaries on scan tiles, so that each chunk's row scan moves whole
   // aligned tiles
+  // (the first chunk may take first_pct percent of the targets, the others
+  // share the rest evenly: a short first search starts the forces sooner)
+  const long long first = (nchunk > 1 && h->first_pct > 0) ? (long long)na * h->first_pct / 100 : -1;
   auto cut = [&](int k) {
-    return k == nchunk ? na : (int)(((long long)na * k / nchunk) & ~(long long)(kScanTile - 1));
+    if (k == 0) return 0;
+    if (k == nchunk) return na;
+    const long long c = first < 0 ? (long long)na * k / nchunk : first + (na - first) * (k - 1) / (nchunk - 1);
+    return (int)(c & ~(long long)(kScanTile - 1));
   };
   if (s2 != st) {
     cudaEventRecord(h->ev_fork, st);
@@ -3826,25 +3833,30 @@ int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatch
   return 0;
 }
 
-int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm) {
+int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm, int first_chunk_percent) {
   if (!h) return SDEM_E_ARG;
-  if (pipeline_chunks < 0 || pipeline_chunks > kMaxChunks || force_blocks_per_sm < 0 || force_blocks_per_sm > 8)
-    return set_err(h, SDEM_E_ARG, "sdem_set_launch: pipeline_chunks in 1..4, force_blocks_per_sm in 1..8 (0 keeps)");
+  if (pipeline_chunks < 0 || pipeline_chunks > kMaxChunks || force_blocks_per_sm < 0 || force_blocks_per_sm > 8 ||
+      first_chunk_percent < -1 || first_chunk_percent > 90 || (first_chunk_percent > 0 && first_chunk_percent < 10))
+    return set_err(h, SDEM_E_ARG, "sdem_set_launch: pipeline_chunks in 1..4, force_blocks_per_sm in 1..8, "
+                                  "first_chunk_percent in 10..90 or -1 for even chunks (0 keeps)");
   const int nc = pipeline_chunks ? pipeline_chunks : h->nchunk;
   const int fb = force_blocks_per_sm ? force_blocks_per_sm : h->force_bps;
-  if (nc != h->nchunk || fb != h->force_bps) {
+  const int fp = first_chunk_percent == 0 ? h->first_pct : (first_chunk_percent < 0 ? 0 : first_chunk_percent);
+  if (nc != h->nchunk || fb != h->force_bps || fp != h->first_pct) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);   // the next step captures the new shape
     h->nchunk = nc;
     h->force_bps = fb;
+    h->first_pct = fp;
   }
   return 0;
 }
 
-int sdem_get_launch(sdem_h* h, int* pipeline_chunks, int* force_blocks_per_sm) {
-  if (!h || !pipeline_chunks || !force_blocks_per_sm) return SDEM_E_ARG;
+int sdem_get_launch(sdem_h* h, int* pipeline_chunks, int* force_blocks_per_sm, int* first_chunk_percent) {
+  if (!h || !pipeline_chunks || !force_blocks_per_sm || !first_chunk_percent) return SDEM_E_ARG;
   *pipeline_chunks = h->nchunk;
   *force_blocks_per_sm = h->force_bps;
+  *first_chunk_percent = h->first_pct;
   return 0;
 }
 

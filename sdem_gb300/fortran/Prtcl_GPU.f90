@@ -220,16 +220,18 @@ module Prtcl_GPU
       real(c_double), intent(out) :: dfma_per_s, ms
     end function sdem_probe_fp64_peak
 
-    integer(c_int) function sdem_set_launch(h, pipeline_chunks, force_blocks_per_sm) bind(C, name="sdem_set_launch")
+    integer(c_int) function sdem_set_launch(h, pipeline_chunks, force_blocks_per_sm, first_chunk_percent) &
+        bind(C, name="sdem_set_launch")
       import :: c_int, c_ptr
       type(c_ptr), value :: h
-      integer(c_int), value :: pipeline_chunks, force_blocks_per_sm
+      integer(c_int), value :: pipeline_chunks, force_blocks_per_sm, first_chunk_percent
     end function sdem_set_launch
 
-    integer(c_int) function sdem_get_launch(h, pipeline_chunks, force_blocks_per_sm) bind(C, name="sdem_get_launch")
+    integer(c_int) function sdem_get_launch(h, pipeline_chunks, force_blocks_per_sm, first_chunk_percent) &
+        bind(C, name="sdem_get_launch")
       import :: c_int, c_ptr
       type(c_ptr), value :: h
-      integer(c_int), intent(out) :: pipeline_chunks, force_blocks_per_sm
+      integer(c_int), intent(out) :: pipeline_chunks, force_blocks_per_sm, first_chunk_percent
     end function sdem_get_launch
 
     integer(c_int) function sdem_count_contacts_noalloc(cfg, max_radius, n, d_posR, d_counts, stream) &

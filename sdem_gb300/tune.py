@@ -3,9 +3,10 @@ and group size).
 
 What it may change, and why results stay exact:
 
-- pipeline chunks (1..4) and force blocks per SM (1..8) of one handle's step
-  (sdem_set_launch): every order that matters is fixed by sort positions, so
-  the results are bit-identical for every value;
+- pipeline chunks (1..4), the first chunk's share of the targets and force
+  blocks per SM (1..8) of one handle's step (sdem_set_launch): every order
+  that matters is fixed by sort positions, so the results are bit-identical
+  for every value;
 - the batch's group size (members per captured graph and stream,
   sdem_batch_create_grouped): members are independent, so results are
   bit-identical;
@@ -40,6 +41,7 @@ CACHE_DIR = os.path.join(os.path.dirname(HERE), ".tunecache")
 
 CHUNKS = (1, 2, 3, 4)
 FORCE_BLOCKS = (2, 3, 4)
+FIRST_CHUNK = (-1, 25, 35)        # percent of the targets in the first chunk (-1: even chunks)
 CELL_FACTORS = (1.0, 1.25, 1.5)
 GROUP_SIZES = (16, 32, 64, 128)
 
@@ -109,9 +111,10 @@ def best_of(candidates: Iterable, measure: Callable[[object], float]):
 
 def tune_handle(case, allow_cell_factor: bool = False, steps: int = 10, cache: bool = True,
                 timer: Optional[Callable] = None) -> Dict:
-    """The fastest (pipeline_chunks, force_blocks_per_sm[, cs_ratio]) for a
-    case's size class.  Returns {"pipeline_chunks", "force_blocks_per_sm",
-    "cs_ratio", "ms_per_step", "tried"}."""
+    """The fastest (pipeline_chunks, force_blocks_per_sm, first_chunk_percent
+    [, cs_ratio]) for a case's size class.  Returns {"pipeline_chunks",
+    "force_blocks_per_sm", "first_chunk_percent", "cs_ratio", "ms_per_step",
+    "tried"}."""
     from .capi import DEMSystem
     key = size_class(case) + ("_cell" if allow_cell_factor else "")
     table = _load("handle") if cache else {}
@@ -120,15 +123,19 @@ def tune_handle(case, allow_cell_factor: bool = False, steps: int = 10, cache: b
     factors = CELL_FACTORS if allow_cell_factor else (case.opts.cs_ratio,)
 
     def measure(c):
-        chunks, fb, cf = c
+        chunks, fb, fp, cf = c
         trial = case if cf == case.opts.cs_ratio else replace(case, opts=replace(case.opts, cs_ratio=cf))
         with DEMSystem(trial) as h:
-            h.set_launch(chunks, fb)
+            h.set_launch(chunks, fb, fp)
             return (timer or time_steps)(h, steps)
 
-    best, times = best_of(itertools.product(CHUNKS, FORCE_BLOCKS, factors), measure)
-    out = {"pipeline_chunks": best[0], "force_blocks_per_sm": best[1], "cs_ratio": best[2],
-           "ms_per_step": times[best], "tried": {f"{c[0]}x{c[1]}@{c[2]}": t for c, t in times.items()}}
+    # the first chunk's share only matters with more than one chunk
+    cands = [(c, f, p, x) for c, f, p, x in itertools.product(CHUNKS, FORCE_BLOCKS, FIRST_CHUNK, factors)
+             if c > 1 or p == -1]
+    best, times = best_of(cands, measure)
+    out = {"pipeline_chunks": best[0], "force_blocks_per_sm": best[1], "first_chunk_percent": best[2],
+           "cs_ratio": best[3], "ms_per_step": times[best],
+           "tried": {f"{c[0]}x{c[1]}/{c[2]}@{c[3]}": t for c, t in times.items()}}
     if cache:
         table[key] = out
         _store("handle", table)
@@ -174,4 +181,4 @@ def tune_batch(systems: Sequence, steps: int = 4, cache: bool = True, key_extra:
 def apply(system, choice: Dict) -> None:
     """Sets a handle's launch shape to a tune_handle choice (the cell factor
     is a creation option: build the handle's case with choice["cs_ratio"])."""
-    system.set_launch(choice["pipeline_chunks"], choice["force_blocks_per_sm"])
+    system.set_launch(choice["pipeline_chunks"], choice["force_blocks_per_sm"], choice.get("first_chunk_percent", -1))

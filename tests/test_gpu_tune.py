@@ -34,12 +34,12 @@ def assert_identical(a, b):
 def test_launch_shapes_bit_identical(gpu_lib):
     case = beds.hertz_poly_case(n=200_000, seed=5)
     ref = None
-    for chunks, fb in ((2, 3), (1, 2), (3, 4), (4, 8)):
+    for chunks, fb, fp in ((2, 3, -1), (1, 2, -1), (3, 4, 30), (4, 8, -1), (2, 3, 20)):
         with DEMSystem(case) as s:
-            s.set_launch(chunks, fb)
-            assert s.get_launch() == (chunks, fb)
+            s.set_launch(chunks, fb, fp)
+            assert s.get_launch() == (chunks, fb, max(fp, 0))
             s.step(7)
-            s.set_launch(1 if chunks > 1 else 2, 0)   # a change between steps recaptures the graphs
+            s.set_launch(1 if chunks > 1 else 2, 0, 0)   # a change between steps recaptures the graphs
             s.step(5)
             snap = snapshot(s)
         if ref is None:
@@ -70,8 +70,10 @@ def test_tuner_returns_a_candidate(gpu_lib, tmp_path, monkeypatch):
     case = beds.lattice_cloud_case(3000, seed=9)
     choice = tune.tune_handle(case, steps=3)
     assert choice["pipeline_chunks"] in tune.CHUNKS and choice["force_blocks_per_sm"] in tune.FORCE_BLOCKS
-    assert choice["cs_ratio"] == case.opts.cs_ratio and len(choice["tried"]) == len(tune.CHUNKS) * len(tune.FORCE_BLOCKS)
+    n_cands = len(tune.FORCE_BLOCKS) * (1 + (len(tune.CHUNKS) - 1) * len(tune.FIRST_CHUNK))
+    assert choice["cs_ratio"] == case.opts.cs_ratio and len(choice["tried"]) == n_cands
     assert tune.tune_handle(case, steps=3) == choice        # cached
     with DEMSystem(case) as s:
         tune.apply(s, choice)
-        assert s.get_launch() == (choice["pipeline_chunks"], choice["force_blocks_per_sm"])
+        assert s.get_launch() == (choice["pipeline_chunks"], choice["force_blocks_per_sm"],
+                                  max(choice["first_chunk_percent"], 0))
