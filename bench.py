@@ -46,12 +46,12 @@ METRIC = "particle-steps/s, 1M Hertz spheres"
 UNIT = "particle-steps/s"
 # From the ncu captures in profiles/ (each file gives its command):
 # profiles/kernels_hertz_poly_settled_1m.txt, one step of the settled 1M bed.
-FORCE_DRAM_BYTES_PER_CONTACT = 413.4     # k_force: dram__bytes_read.sum + dram__bytes_write.sum per contact
+FORCE_DRAM_BYTES_PER_CONTACT = 401.4     # k_force: dram__bytes_read.sum + dram__bytes_write.sum per contact
 FP64_INST_PER_SM_CLK = 2.0               # DADD/DMUL/DFMA thread operations per SM per clock (FP64 pipe)
 NUM_SMS = 152
 # Executed DADD + DMUL + DFMA thread instructions of the step's kernels,
 # modelled per particle-particle contact, per sphere and per wall contact.
-FP64_PER_CONTACT = {"k_force": 136.1, "k_gather": 24.2}
+FP64_PER_CONTACT = {"k_force": 120.1, "k_gather": 24.2}
 FP64_PER_SPHERE = {"k_integrate": 51.0, "k_bin": 3.0, "k_wall_detect": 0.74}
 FP64_PER_WALL_CONTACT = {"k_wall_force": 123.3, "k_gather": 12.0}
 

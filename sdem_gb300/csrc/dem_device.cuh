@@ -51,12 +51,6 @@ __device__ __forceinline__ r3 cross3(r3 u, r3 v) {
   return mk3(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
 }
 __device__ __forceinline__ double norm3(r3 p) { return fpi::sqrt_rn(p.x * p.x + p.y * p.y + p.z * p.z); }
-// The same norm with the hardware square root (same bits).  The force law uses
-// it for the two spring norms: their operand arrives last (the history
-// lookup), and there the shorter latency of the FP64-pipe sequence measured
-// faster than the integer one (0.49 against 0.52 ms per step on the 1M bed);
-// every other sqrt and division measured faster on the integer pipes.
-__device__ __forceinline__ double norm3_hw(r3 p) { return sqrt(p.x * p.x + p.y * p.y + p.z * p.z); }
 // real4_nv / real3_nv: s/|s| with the 1e-10 guard
 __device__ __forceinline__ r3 nv3(r3 s) {
   double n = norm3(s);
@@ -182,9 +176,9 @@ __device__ __forceinline__ void force_law(const LawCfg& L, const double* P, r3 V
   r3 Vij_t = sub3(Vrij, Vij_n);
 
   r3 Ovlp_t = mk3(hist.x, hist.y, hist.z);
-  double normTan1 = norm3_hw(Ovlp_t);
+  double normTan1 = norm3(Ovlp_t);
   Ovlp_t = sub3(Ovlp_t, scale3(Norm_v, dot3(Ovlp_t, Norm_v)));
-  double normTan2 = norm3_hw(Ovlp_t);
+  double normTan2 = norm3(Ovlp_t);
   if (fpi::gt(normTan2, 1.0E-10)) Ovlp_t = scale3(Ovlp_t, fpi::div_rn(normTan1, normTan2));
   else Ovlp_t = mk3(0.0, 0.0, 0.0);
   Ovlp_t = add3(scale3(Vij_t, L.dt), Ovlp_t);

@@ -708,7 +708,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int 
       const float4 Pf = d.spos[s];
       const float margin = d.pf_margin;
       int cnt = 0;
-      const int K = d.K, Kin = d.Kin, ncap = d.ncap, nall = d.nall;
+      const int K = d.K, Kin = d.Kin, nall = d.nall;
       // The single-precision distance is within pf_margin of the exact one, so
       // outside the band |d - (ri+rj)| < pf_margin the FP32 test decides the
       // reference's FP64 test (NBSM_FineSearch2, Prtcl_NBS_Munjiza.f90:514-522);
@@ -971,7 +971,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32, SDEM_SEARCH_MIN_BLOCKS) k_s
   const int s0 = s_begin + (blockIdx.x * kSearchWarps + w) * 32;
   if (s0 >= s_end) return;   // the whole warp
   const int nt = *d.nt, nloc = *d.n;
-  const int K = d.K, Kin = d.Kin, ncap = d.ncap, nall = d.nall;
+  const int K = d.K, Kin = d.Kin, nall = d.nall;
   const float margin = d.pf_margin, cellf = d.cellf;
   const int* __restrict__ cs = d.cell_start;
   const int s_me = s0 + lane;

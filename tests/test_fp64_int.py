@@ -1,9 +1,10 @@
 """The integer-pipe binary64 arithmetic of sdem_gb300/csrc/fp64_int.cuh
-(add, sub, mul, exact multiplication by -1/2) is bit-identical to IEEE
+(square root, division, comparisons, exact multiplication by -1/2, the grid
+floor and the floor of a quotient) is bit-identical to IEEE
 round-to-nearest-even: compiled for the host and compared with the host's own
 double arithmetic on random and adversarial operand pairs (every exponent,
-close exponents, cancellations, near-ties, overflow and underflow edges,
-zeros, subnormals, infinities, NaN)."""
+close exponents, exact squares and quotients, near-ties, overflow and
+underflow edges, zeros, subnormals, infinities, NaN)."""
 import os
 import shutil
 import subprocess
