@@ -593,9 +593,9 @@ def surrogate_arm(args):
     stride of 100 steps apart) for `--train-iters` Adam steps, then on the 1M
     Hertz bed: K surrogate strides (graph build, features, forward, stride
     update) against K x 100 plain DEM steps, and a run of the runner with the
-    plain-DEM judge every `--judge-every` strides (bound: 2% relative bed
-    height).  Simulated seconds per wall second, host clock around
-    synchronised runs."""
+    plain-DEM judge every `--judge-every` strides (bounds: 2% relative bed
+    height, 5% mean relative wall pressure).  Simulated seconds per wall
+    second, host clock around synchronised runs."""
     import torch
     from sdem_gb300 import beds, surrogate as sg
     from sdem_gb300.capi import DEMSystem
@@ -625,7 +625,7 @@ def surrogate_arm(args):
     dem.step(args.warmup)
     dmax = 2.0 * float(case.tables.radius.max())
     runner = sg.SurrogateRunner(net, dem, case, S, dmax, vscale, judge_every=args.judge_every, bound=0.02,
-                                fallback_strides=args.judge_every)
+                                fallback_strides=args.judge_every, pressure_bound=0.05)
     K = max(1, args.strides)
     start = (runner.posR.clone(), runner.vel.clone(), runner.omega.clone())
     runner._surrogate_stride(runner.posR, runner.vel, runner.omega)     # warm-up
@@ -672,7 +672,9 @@ def surrogate_arm(args):
                            "rewound_strides": stats["rewound_strides"],
                            "judged": stats["judged"], "fallbacks": stats["fallbacks"],
                            "diverged": stats["diverged"],
-                           "bed_height_rel_err": stats["errors"]},
+                           "bed_height_rel_err": stats["errors"],
+                           "wall_pressure_rel_err": stats["pressure_errors"],
+                           "bounds": {"bed_height": runner.bound, "wall_pressure": runner.pressure_bound}},
             "training": {"beds": args.train_beds, "samples": len(train), "iters": args.train_iters,
                          "loss_first10": float(np.mean(losses[:10])), "loss_last10": float(np.mean(losses[-10:])),
                          "heldout_mse": mse, "heldout_mse_free_flight": mse_free, "data_s": t_data,

@@ -23,9 +23,10 @@ no CPU fallback: loading fails loudly when the library is missing.
 SurrogateRunner advances a bed by surrogate strides and, every `judge_every`
 strides, re-advances one stride with the plain FP64 DEM (include/sdem_gpu.h)
 from the surrogate's state as the error judge; when the relative bed-height
-difference exceeds the bound, when the plain DEM rejects the state, or when
-the neighbour graph outgrows its limit, the plain DEM takes over for the next
-strides (from its last own state where the surrogate's was rejected).
+difference or the mean relative wall-pressure difference exceeds its bound,
+when the plain DEM rejects the state, or when the neighbour graph outgrows its
+limit, the plain DEM takes over for the next strides (from its last own state
+where the surrogate's was rejected).
 """
 from __future__ import annotations
 
@@ -646,6 +647,60 @@ def evaluate(net: Network, samples: List[DeviceSample]) -> Tuple[float, float]:
     return num / den, base / den
 
 
+# ----------------------------------------------------------- wall pressure
+
+def wall_pressure(posR: np.ndarray, ptype: np.ndarray, case) -> np.ndarray:
+    """Pressure on each plane wall of `case` from the elastic normal forces of
+    the spheres that overlap it (the state's static load): for a sphere at
+    signed distance s = n.x + d from the wall's plane (|s| for a two-sided
+    wall), overlap delta = r - s >= 0 and, for a finite wall, the foot of the
+    perpendicular inside the wall's bounding box; the force is
+    Kn delta^1.5 (Hertz) or Kn 0.01^0.4 delta (the reference's LSD stiffness
+    at its lowest contact speed), Kn of the (wall type, sphere type) pair
+    (Prtcl_Property.f90:200-247), and the pressure their sum over the wall's
+    area |(p2 - p1) x (p4 - p1)|.  (nw,) float64 in Pa."""
+    from . import props
+    walls, flags = case.walls.arrays()
+    nw = case.walls.n
+    out = np.zeros(nw)
+    if nw == 0 or len(posR) == 0:
+        return out
+    W = walls.reshape(nw, -1)
+    F = flags.reshape(nw, -1)
+    nT = case.tables.n_types
+    bpw = case.tables.bpw.reshape(-1, nT, props.BP_SIZE)
+    x, r = posR[:, :3], posR[:, 3]
+    for k in range(nw):
+        n, d = W[k, 12:15], W[k, 15]
+        s = x @ n + d
+        if F[k, 0]:
+            s = np.abs(s)
+        delta = r - s
+        on = (delta >= 0.0) & (s >= 0.0)
+        if not F[k, 1]:   # finite wall: the foot of the perpendicular inside its box
+            foot = x - s[:, None] * n[None, :]
+            lo, hi = W[k, 19:22] - 1e-12, W[k, 22:25] + 1e-12
+            on &= np.all((foot >= lo) & (foot <= hi), axis=1)
+        if not on.any():
+            continue
+        kn = np.abs(bpw[F[k, 3] - 1, ptype[on] - 1, 2])
+        dl = delta[on]
+        f = kn * (dl * np.sqrt(dl) if case.opts.cf_type == props.CFT_NLIN else 0.01 ** 0.4 * dl)
+        p1, p2, p4 = W[k, 0:3], W[k, 3:6], W[k, 9:12]
+        area = float(np.linalg.norm(np.cross(p2 - p1, p4 - p1)))
+        out[k] = float(f.sum()) / area
+    return out
+
+
+def pressure_error(p: np.ndarray, ref: np.ndarray) -> float:
+    """Mean over the walls that carry load in `ref` of |p - ref| / ref (0 when
+    no wall carries load)."""
+    loaded = ref > 0.0
+    if not loaded.any():
+        return 0.0
+    return float(np.mean(np.abs(p[loaded] - ref[loaded]) / ref[loaded]))
+
+
 # --------------------------------------------------------------- rollout
 
 class Diverged(RuntimeError):
@@ -657,11 +712,13 @@ class SurrogateRunner:
     """Advances a bed by surrogate strides with a plain-DEM judge.
 
     Every `judge_every` surrogate strides the plain DEM re-advances one
-    stride from the surrogate's state; the relative bed-height difference
-    (mean sphere height above the floor, over the spheres both keep) between
-    that stride and the surrogate's own stride from the same state is the
-    error.  Within the bound the run continues from the plain DEM's state;
-    above it, or when the plain stride fails (a state the DEM rejects), the
+    stride from the surrogate's state; between that stride and the
+    surrogate's own stride from the same state, the relative bed-height
+    difference (mean sphere height above the floor, over the spheres both
+    keep) and the mean relative wall-pressure difference (wall_pressure of
+    either end state, over the walls the plain state loads) are the errors.
+    Within both bounds the run continues from the plain DEM's state; above
+    either, or when the plain stride fails (a state the DEM rejects), the
     last state the plain DEM produced is restored (simulated time rewinds to
     it) and the plain DEM advances the next `fallback_strides` strides
     itself.  Spheres the plain DEM deletes (out of the domain) leave the
@@ -673,12 +730,14 @@ class SurrogateRunner:
     without bound)."""
 
     def __init__(self, net: Network, system, case, stride: int, d_max: float, vscale: float,
-                 judge_every: int = 20, bound: float = 0.02, fallback_strides: int = 20, edge_growth: float = 3.0):
+                 judge_every: int = 20, bound: float = 0.02, fallback_strides: int = 20, edge_growth: float = 3.0,
+                 pressure_bound: float = 0.05):
         self.net, self.sys, self.case = net, system, case
         self.edge_growth = edge_growth
         self.edge_ref = None
         self.stride, self.d_max, self.vscale = stride, d_max, vscale
         self.judge_every, self.bound, self.fallback = judge_every, bound, fallback_strides
+        self.pressure_bound = pressure_bound
         self.h = stride * case.opts.dt
         self.grid = make_grid(case.opts.minpoint, case.opts.maxpoint, d_max)
         self.planes = torch.from_numpy(planes_of(case.walls)).to(net.device)
@@ -687,7 +746,7 @@ class SurrogateRunner:
         self.t = 0                    # strides of simulated time since the start
         self.since_judge = 0
         self.stats = {"surrogate_strides": 0, "dem_strides": 0, "judged": 0, "fallbacks": 0, "rewound_strides": 0,
-                      "diverged": 0, "errors": []}
+                      "diverged": 0, "errors": [], "pressure_errors": []}
         self._seed_from_dem()
 
     def _dem_stride(self) -> None:
@@ -769,14 +828,18 @@ class SurrogateRunner:
         self.stats["judged"] += 1
         self.stats["surrogate_strides"] += 1
         if st is None:
-            err = math.inf
+            err = perr = math.inf
         else:
+            p_sur = p2.cpu().numpy()
             keep = np.isin(ids, st.id)
-            h_sur = float((p2[:, 1].cpu().numpy()[keep] - self.floor).mean())
+            h_sur = float((p_sur[keep, 1] - self.floor).mean())
             h_dem = float((st.posR[:, 1] - self.floor).mean())
             err = abs(h_sur - h_dem) / max(abs(h_dem), 1e-300)
+            perr = pressure_error(wall_pressure(p_sur, self.parts.ptype, self.case),
+                                  wall_pressure(st.posR, st.ptype, self.case))
         self.stats["errors"].append(err)
-        if err > self.bound:
+        self.stats["pressure_errors"].append(perr)
+        if err > self.bound or perr > self.pressure_bound:
             self._fall_back(rewind=st is None)
         else:
             v = st.linVel[:, 0, :]

@@ -290,11 +290,12 @@ def test_runner_judges_and_falls_back(sg_lib):
                                fallback_strides=3)
         st = r.run(12)
         assert r.t >= 14 and st["judged"] >= 1
-        errs = st["errors"]
-        assert len(errs) == st["judged"] and all(e >= 0.0 for e in errs)
-        # a fallback exactly when a judged error exceeds the bound or the
+        errs, perrs = st["errors"], st["pressure_errors"]
+        assert len(errs) == len(perrs) == st["judged"] and all(e >= 0.0 for e in errs + perrs)
+        # a fallback exactly when a judged error exceeds its bound or the
         # graph outgrows its limit
-        assert st["fallbacks"] == sum(1 for e in errs if e > bound) + st["diverged"]
+        assert st["fallbacks"] == sum(1 for e, pe in zip(errs, perrs)
+                                      if e > bound or pe > r.pressure_bound) + st["diverged"]
         if bound == 0.0:
             assert st["fallbacks"] >= 1
         assert torch.isfinite(r.posR).all() and r.posR.shape[0] == s.counters()["nlocal"]

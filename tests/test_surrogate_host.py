@@ -168,12 +168,49 @@ def test_runner_over_the_oracle(mock, bound, growth):
     t0 = r.t
     st = r.run(9)
     assert r.t >= t0 + 9
-    assert st["fallbacks"] == sum(1 for e in st["errors"] if e > bound) + st["diverged"]
+    assert len(st["pressure_errors"]) == len(st["errors"]) == st["judged"]
+    assert st["fallbacks"] == sum(1 for e, pe in zip(st["errors"], st["pressure_errors"])
+                                  if e > bound or pe > r.pressure_bound) + st["diverged"]
     if bound == 0.0:
         assert st["fallbacks"] >= 1 and st["diverged"] == 0
     if growth < 1.0:
         assert st["diverged"] >= 1 and st["rewound_strides"] >= 1
     assert r.posR.shape[0] == dem.counters()["nlocal"] and torch.isfinite(r.posR).all()
+
+
+def test_wall_pressure_known_answers():
+    # one Hertz sphere pressed into the floor of a 0.1 x 0.6 x 0.1 m box, one
+    # touching a side wall, one free: the pressure on each wall is
+    # |Kn| delta^1.5 over the wall's area; LSD scales the overlap linearly
+    from sdem_gb300 import beds, props
+    case = beds.sandbox_case(np.random.default_rng(3), 0, n_lo=200, n_hi=200)
+    nT = case.tables.n_types
+    bpw = case.tables.bpw.reshape(-1, nT, props.BP_SIZE)
+    lo, hi = np.asarray(case.opts.minpoint), np.asarray(case.opts.maxpoint)
+    r = 1e-3
+    mid = (lo + hi) / 2
+    posR = np.array([[mid[0], lo[1] + r - 2e-5, mid[2], r],        # floor, delta 2e-5
+                     [lo[0] + r - 1e-5, mid[1], mid[2], r],        # wall x = min, delta 1e-5
+                     [mid[0], mid[1], mid[2], r]])                 # free
+    ptype = np.array([1, 2, 1], dtype=np.int32)
+    walls, flags = case.walls.arrays()
+    W, F = walls.reshape(case.walls.n, -1), flags.reshape(case.walls.n, -1)
+    p = sg.wall_pressure(posR, ptype, case)
+    assert p.shape == (case.walls.n,)
+    for k in range(case.walls.n):
+        n = W[k, 12:15]
+        area = float(np.linalg.norm(np.cross(W[k, 3:6] - W[k, 0:3], W[k, 9:12] - W[k, 0:3])))
+        want = 0.0
+        for (x, t) in ((posR[0], 1), (posR[1], 2)):
+            delta = r - (x[:3] @ n + W[k, 15])
+            if delta >= 0:
+                kn = abs(bpw[F[k, 3] - 1, t - 1, 2])
+                want += kn * delta ** 1.5 if case.opts.cf_type == props.CFT_NLIN else kn * 0.01 ** 0.4 * delta
+        np.testing.assert_allclose(p[k], want / area, rtol=1e-12)
+    assert np.count_nonzero(p) == 2
+    # the relative error over the loaded walls only
+    assert sg.pressure_error(p * 1.1, p) == pytest.approx(0.1)
+    assert sg.pressure_error(p, np.zeros_like(p)) == 0.0
 
 
 def test_graph_without_edges(mock):
