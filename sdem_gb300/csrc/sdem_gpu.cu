@@ -2169,6 +2169,7 @@ struct sdem_h {
   // mapped host copy of the device scalars, written by every step's last
   // kernel; valid while no host write to the scalars came after the last step
   int* h_mirror = nullptr;   // 2 slots of S_SIZE ints, by iteration parity
+  int* h_chk = nullptr;      // page-locked: the upload's id/type check (status, detail)
   int* d_mirror = nullptr;
   bool mirror_ok = false;
   long long iter_host = 0;   // device iteration number after the last enqueued step
@@ -2180,6 +2181,7 @@ struct sdem_h {
   // downloaded on the I/O stream while later steps run
   cudaStream_t stream_io = nullptr;
   cudaEvent_t ev_snap = nullptr, ev_snap_done = nullptr;
+  cudaEvent_t ev_xfer[6] = {};   // upload/download: one staged field copied / packed
   bool snap_busy = false, snap_done = false, snap_contacts = false, snap_stepped = false;
   double* sn_state = nullptr;    // device: posR, 3-vector fields, F, T (host layouts)
   int* sn_ints = nullptr;        // device: id, ptype, usrmark, n
@@ -2670,6 +2672,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   CK(cudaEventCreateWithFlags(&h->ev_snap_done, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+  for (int k = 0; k < 6; k++) CK(cudaEventCreateWithFlags(&h->ev_xfer[k], cudaEventDisableTiming));
   for (int k = 0; k < kMaxChunks; k++) CK(cudaEventCreateWithFlags(&h->ev_chunk[k], cudaEventDisableTiming));
   int N = c.n_capacity;
   if (c.n_fixed_capacity < 0) return bad("n_fixed_capacity must be >= 0");
@@ -2759,6 +2762,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   if (rc) return SDEM_E_NOMEM;
   CK(cudaMallocHost(&h->h_counters, sizeof(int) * SDEM_CNT_SIZE));
   CK(cudaHostAlloc((void**)&h->h_mirror, sizeof(int) * 2 * S_SIZE, cudaHostAllocMapped));
+  CK(cudaHostAlloc((void**)&h->h_chk, sizeof(int) * 2, cudaHostAllocDefault));
   std::memset(h->h_mirror, 0, sizeof(int) * 2 * S_SIZE);
   for (int b = 0; b < 2; b++) CK(cudaEventCreateWithFlags(&h->ev_step[b], cudaEventDisableTiming));
   CK(cudaHostGetDevicePointer((void**)&h->d_mirror, h->h_mirror, 0));
@@ -2961,35 +2965,25 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   if (n < 0 || n > c.n_capacity) return set_err(h, SDEM_E_CAPACITY, "sdem_upload_particles: n exceeds n_capacity");
   if (n > 0 && (!id || !ptype || !posR || !linVel)) return set_err(h, SDEM_E_ARG, "sdem_upload_particles: null arrays");
   // Stream-ordered copies: a step still in flight finishes before the state
-  // is replaced, and the call returns after the last copy has landed.
-  cudaStream_t st = h->stream;
+  // is replaced, and the call returns after the last copy has landed.  The
+  // copies follow one another on the handle's stream; each staged field is
+  // unpacked on the second stream once its copy has landed, beside the next
+  // copy.  The device's check of ids and types is read back at the end.
+  cudaStream_t st = h->stream, s2 = h->stream2;
   CK(cudaStreamSynchronize(st));
   h->mirror_ok = false;   // the device scalars are rewritten below
+  int chk[2] = {0, 0};
+  int* scal = h->scal;
   if (n > 0) {
     CK(cudaMemcpyAsync(h->gid, id, sizeof(int) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(h->ptype, ptype, sizeof(int) * n, cudaMemcpyHostToDevice, st));
     // ids and types are checked on the device (the owner table of buffer 0,
     // cleared again below, holds the per-id flags)
-    int* scal = h->scal;
     CK(cudaMemsetAsync(h->own_cnt[0], 0, sizeof(int) * ((size_t)c.max_gid + 1), st));
     CK(cudaMemsetAsync(scal + S_STATUS, 0, 2 * sizeof(int), st));
     k_check_upload<<<grid_for(n), kThreads, 0, st>>>(h->gid, h->ptype, n, c.max_gid, h->nT, h->own_cnt[0],
                                                      scal + S_STATUS);
-    int chk[2] = {0, 0};
-    CK(cudaMemcpyAsync(chk, scal + S_STATUS, sizeof chk, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (chk[0] != 0) {
-      h->n_host = 0;   // the handle holds no valid particle set now
-      h->stepped = false;
-      drop_graph(h);
-      int z[2] = {0, 0};
-      CK(cudaMemcpyAsync(scal + S_STATUS, z, sizeof z, cudaMemcpyHostToDevice, st));
-      CK(cudaStreamSynchronize(st));
-      const std::string at = " (particle index " + std::to_string(chk[1]) + ")";
-      if (chk[0] == SDEM_E_BAD_ID) return set_err(h, SDEM_E_BAD_ID, "particle id outside 1..max_gid" + at);
-      if (chk[0] == SDEM_E_BAD_ID + 100) return set_err(h, SDEM_E_BAD_ID, "duplicate particle id" + at);
-      return set_err(h, SDEM_E_ARG, "particle type outside 1..nT" + at);
-    }
+    CK(cudaMemcpyAsync(h->h_chk, scal + S_STATUS, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     if (usrmark) CK(cudaMemcpyAsync(h->usrmark, usrmark, sizeof(int) * n, cudaMemcpyHostToDevice, st));
     else CK(cudaMemsetAsync(h->usrmark, 0, sizeof(int) * n, st));
     // (x, y, z, r) per particle is also the device record
@@ -2998,10 +2992,14 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
     int rs = ensure_stage(h, per * n);
     if (rs) return rs;
     double* sp = h->stage;
-    auto put = [&](const double* src, int levels, dbl4* const* dst) -> int {
+    int f = 0;
+    auto put = [&](const double* src, int levels, dbl4* const* dst) {
       if (src) CK(cudaMemcpyAsync(sp, src, sizeof(double) * 3 * levels * (size_t)n, cudaMemcpyHostToDevice, st));
-      for (int k = 0; k < levels; k++) k_unpack3<<<grid_for(n), kThreads, 0, st>>>(dst[k], src ? sp : nullptr, n, levels, k);
+      CK(cudaEventRecord(h->ev_xfer[f], st));
+      CK(cudaStreamWaitEvent(s2, h->ev_xfer[f], 0));
+      for (int k = 0; k < levels; k++) k_unpack3<<<grid_for(n), kThreads, 0, s2>>>(dst[k], src ? sp : nullptr, n, levels, k);
       sp += 3 * (size_t)levels * n;
+      f++;
       return 0;
     };
     dbl4* th[1] = {h->theta};
@@ -3011,6 +3009,8 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
     rc |= put(rotVel, c.rsize, h->rv);
     rc |= put(rotAcc, c.rsize, h->ra);
     if (rc) return rc;
+    CK(cudaEventRecord(h->ev_xfer[5], s2));
+    CK(cudaStreamWaitEvent(st, h->ev_xfer[5], 0));
     k_tag_vel<<<grid_for(n), kThreads, 0, st>>>(h->vel[0], h->gid, h->ptype, n);
   }
   // history reset: both buffers empty; near-wall list refreshed at the next step
@@ -3030,6 +3030,18 @@ int sdem_upload_particles(sdem_h* h, int n, const int* id, const int* ptype, con
   CK(cudaMemsetAsync(h->ull, 0, sizeof(unsigned long long) * 10, st));
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
+  if (n > 0) std::memcpy(chk, h->h_chk, sizeof chk);
+  if (chk[0] != 0) {
+    h->n_host = 0;   // the handle holds no valid particle set now
+    h->stepped = false;
+    drop_graph(h);
+    const int zs[S_SIZE] = {0};   // no particles, status cleared
+    CK(cudaMemcpy(scal, zs, sizeof zs, cudaMemcpyHostToDevice));
+    const std::string at = " (particle index " + std::to_string(chk[1]) + ")";
+    if (chk[0] == SDEM_E_BAD_ID) return set_err(h, SDEM_E_BAD_ID, "particle id outside 1..max_gid" + at);
+    if (chk[0] == SDEM_E_BAD_ID + 100) return set_err(h, SDEM_E_BAD_ID, "duplicate particle id" + at);
+    return set_err(h, SDEM_E_ARG, "particle type outside 1..nT" + at);
+  }
   // the captured step graphs bake in launch sizes from the particle count
   // (and nothing else that an upload changes): they stay valid for a new
   // particle set of the same size
@@ -3290,30 +3302,43 @@ int sdem_download_particles(sdem_h* h, int* n_out, int* id, int* ptype, int* usr
   CK(cudaMemcpy(&n, h->scal + S_N, sizeof n, cudaMemcpyDeviceToHost));
   if (n_out) *n_out = n;
   const sdem_cfg& c = h->cfg;
-  cudaStream_t st = h->stream;
+  cudaStream_t st = h->stream, s2 = h->stream2;
   if (n <= 0) return 0;
+  const size_t per = 3 * (size_t)(2 * c.tsize + 2 * c.rsize + 1);
+  rc = ensure_stage(h, per * n);
+  if (rc) return rc;
+  // The staged fields are packed on the second stream while the handle's
+  // stream copies the records that need no packing; each staged field is
+  // copied out once its packing is done, so the copies follow one another.
+  CK(cudaEventRecord(h->ev_xfer[5], st));
+  CK(cudaStreamWaitEvent(s2, h->ev_xfer[5], 0));
+  struct Field {
+    double* dst;
+    int levels;
+    dbl4* const* src;
+  };
+  dbl4* th[1] = {h->theta};
+  const Field fs[5] = {{linVel, c.tsize, h->vel}, {linAcc, c.tsize, h->acc}, {theta, 1, th},
+                       {rotVel, c.rsize, h->rv}, {rotAcc, c.rsize, h->ra}};
+  double* sp = h->stage;
+  for (int f = 0; f < 5; f++) {
+    if (fs[f].dst)
+      for (int k = 0; k < fs[f].levels; k++)
+        k_pack3<<<grid_for(n), kThreads, 0, s2>>>(sp, fs[f].src[k], n, fs[f].levels, k);
+    CK(cudaEventRecord(h->ev_xfer[f], s2));
+    sp += 3 * (size_t)fs[f].levels * n;
+  }
   if (id) CK(cudaMemcpyAsync(id, h->gid, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
   if (ptype) CK(cudaMemcpyAsync(ptype, h->ptype, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
   if (usrmark) CK(cudaMemcpyAsync(usrmark, h->usrmark, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
   if (posR) CK(cudaMemcpyAsync(posR, h->posr, sizeof(dbl4) * n, cudaMemcpyDeviceToHost, st));
-  const size_t per = 3 * (size_t)(2 * c.tsize + 2 * c.rsize + 1);
-  rc = ensure_stage(h, per * n);
-  if (rc) return rc;
-  double* sp = h->stage;
-  auto get = [&](double* dst, int levels, dbl4* const* src) -> int {
-    if (!dst) return 0;
-    for (int k = 0; k < levels; k++) k_pack3<<<grid_for(n), kThreads, 0, st>>>(sp, src[k], n, levels, k);
-    CK(cudaMemcpyAsync(dst, sp, sizeof(double) * 3 * levels * (size_t)n, cudaMemcpyDeviceToHost, st));
-    sp += 3 * (size_t)levels * n;
-    return 0;
-  };
-  dbl4* th[1] = {h->theta};
-  rc = get(linVel, c.tsize, h->vel);
-  rc |= get(linAcc, c.tsize, h->acc);
-  rc |= get(theta, 1, th);
-  rc |= get(rotVel, c.rsize, h->rv);
-  rc |= get(rotAcc, c.rsize, h->ra);
-  if (rc) return rc;
+  sp = h->stage;
+  for (int f = 0; f < 5; f++) {
+    CK(cudaStreamWaitEvent(st, h->ev_xfer[f], 0));
+    if (fs[f].dst)
+      CK(cudaMemcpyAsync(fs[f].dst, sp, sizeof(double) * 3 * fs[f].levels * (size_t)n, cudaMemcpyDeviceToHost, st));
+    sp += 3 * (size_t)fs[f].levels * n;
+  }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
   return 0;
@@ -3901,6 +3926,7 @@ void sdem_destroy(sdem_h* h) {
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
   if (h->h_mirror) cudaFreeHost(h->h_mirror);
+  if (h->h_chk) cudaFreeHost(h->h_chk);
   if (h->stage) cudaFree(h->stage);
   if (h->stream_io) cudaStreamSynchronize(h->stream_io);
   if (h->sn_state) cudaFree(h->sn_state);
@@ -3916,6 +3942,8 @@ void sdem_destroy(sdem_h* h) {
   for (int b = 0; b < 2; b++)
     if (h->ev_step[b]) cudaEventDestroy(h->ev_step[b]);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  for (int k = 0; k < 6; k++)
+    if (h->ev_xfer[k]) cudaEventDestroy(h->ev_xfer[k]);
   for (int k = 0; k < kMaxChunks; k++)
     if (h->ev_chunk[k]) cudaEventDestroy(h->ev_chunk[k]);
   if (h->stream2) cudaStreamDestroy(h->stream2);
