@@ -588,27 +588,33 @@ def sandboxes_arm(args):
 
 def surrogate_arm(args):
     """The learned surrogate (its own line; not the headline): a network
-    trained on plain-DEM trajectories of `--train-beds` sandboxes (2,000-4,000
-    spheres, parameters from seed 5, 15,000 settling steps, then 12 frames a
-    stride of 100 steps apart) for `--train-iters` Adam steps, then on the 1M
+    trained on plain-DEM trajectories of `--train-beds` Hertz sandboxes
+    (`--train-n`/2 to `--train-n` spheres, parameters from seed 5, advanced
+    together by the batched form: 15,000 settling steps, then
+    `--train-frames` frames a stride of 100 steps apart) for
+    `--train-iters` Adam steps, then on the 1M
     Hertz bed: K surrogate strides (graph build, features, forward, stride
     update) against K x 100 plain DEM steps, and a run of the runner with the
     plain-DEM judge every `--judge-every` strides (bounds: 2% relative bed
     height, 5% mean relative wall pressure).  Simulated seconds per wall
     second, host clock around synchronised runs."""
     import torch
-    from sdem_gb300 import beds, surrogate as sg
+    from sdem_gb300 import beds, props, surrogate as sg
     from sdem_gb300.capi import DEMSystem
     torch.cuda.set_device(0)
     S, vscale = 100, 0.05
     t0 = time.perf_counter()
     rng = np.random.default_rng(5)
-    sets = []
-    for k in range(args.train_beds + 1):
-        case = beds.sandbox_case(rng, k, n_lo=2000, n_hi=4000)
-        s = DEMSystem(case)
-        sets.append([sg.to_device(x, case, 1.2e-3, vscale) for x in sg.record_samples(s, case, S, 12, settle=15000)])
+    # Hertz sandboxes (the configuration's material ranges), all advanced
+    # together by the plain path's batched form; the last one is held out
+    cases = [beds.sandbox_case(rng, k, n_lo=args.train_n // 2, n_hi=args.train_n, cf_type=props.CFT_NLIN)
+             for k in range(args.train_beds + 1)]
+    systems = [DEMSystem(c) for c in cases]
+    recorded = sg.record_samples_batch(systems, cases, S, args.train_frames, settle=15000)
+    for s in systems:
         s.close()
+    sets = [[sg.to_device(x, c, 1.2e-3, vscale) for x in xs] for xs, c in zip(recorded, cases)]
+    del recorded
     train, held = [x for ss in sets[:-1] for x in ss], sets[-1]
     t_data = time.perf_counter() - t0
     net = sg.Network(seed=0)
@@ -628,24 +634,34 @@ def surrogate_arm(args):
                                 fallback_strides=args.judge_every, pressure_bound=0.05)
     K = max(1, args.strides)
     start = (runner.posR.clone(), runner.vel.clone(), runner.omega.clone())
+
+    def reset():
+        # every timed stride starts from the plain DEM's state: the cost of a
+        # stride on the bed itself, not on whatever an untrained rollout makes
+        runner.posR.copy_(start[0])
+        runner.vel.copy_(start[1])
+        runner.omega.copy_(start[2])
+
     runner._surrogate_stride(runner.posR, runner.vel, runner.omega)     # warm-up
-    phases, E = surrogate_phases(runner, net, sg, torch)
+    phases, E = surrogate_phases(runner, net, sg, torch, reset)
     # the same forward on the warp-level mma.sync kernel, for comparison
     assert net.lib.sdem_sg_set_tensor_path(0) == 0
-    phases_mma, _ = surrogate_phases(runner, net, sg, torch)
+    phases_mma, _ = surrogate_phases(runner, net, sg, torch, reset)
     assert net.lib.sdem_sg_set_tensor_path(1) == 0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    t_sur = 0.0
     for _ in range(K):
+        reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         runner._surrogate_stride(runner.posR, runner.vel, runner.omega)
-    torch.cuda.synchronize()
-    t_sur = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        t_sur += time.perf_counter() - t0
     t0 = time.perf_counter()
     dem.step(K * S)
     dem.counters()
     t_plain = time.perf_counter() - t0
     # the judged run starts again from the plain state the timing started from
-    runner.posR, runner.vel, runner.omega = start
+    reset()
     runner.edge_ref = None
     h = S * case.opts.dt
     t_sim0 = runner.t
@@ -675,7 +691,9 @@ def surrogate_arm(args):
                            "bed_height_rel_err": stats["errors"],
                            "wall_pressure_rel_err": stats["pressure_errors"],
                            "bounds": {"bed_height": runner.bound, "wall_pressure": runner.pressure_bound}},
-            "training": {"beds": args.train_beds, "samples": len(train), "iters": args.train_iters,
+            "training": {"beds": args.train_beds, "spheres_per_bed": [c.particles.n for c in cases[:-1]],
+                         "frames_per_bed": args.train_frames, "generator": "sdem_batch (one graph per group)",
+                         "samples": len(train), "iters": args.train_iters,
                          "loss_first10": float(np.mean(losses[:10])), "loss_last10": float(np.mean(losses[-10:])),
                          "heldout_mse": mse, "heldout_mse_free_flight": mse_free, "data_s": t_data,
                          "train_s": t_train},
@@ -778,14 +796,15 @@ def measured_bf16_tflops():
         return 1900.0
 
 
-def surrogate_phases(runner, net, sg, torch, reps: int = 3):
-    """Median CUDA-event times (ms) of the parts of one surrogate stride on
-    the runner's state (graph build, node features, forward, stride update)
-    and the edge count."""
+def surrogate_phases(runner, net, sg, torch, reset, reps: int = 3):
+    """Median CUDA-event times (ms) of the parts of one surrogate stride
+    (graph build, node features, forward, stride update) from the state
+    reset() restores, and the edge count."""
     import ctypes
     out = {"graph": [], "features": [], "forward": [], "update": []}
     E = 0
     for _ in range(reps):
+        reset()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
         ev[0].record()
         g = sg.build_graph(runner.posR, runner.grid, sender_order=False)
@@ -833,7 +852,9 @@ def main():
                     help="sandboxes: batch steps before timing")
     ap.add_argument("--sandbox-layout", default="deposited", choices=["deposited", "lattice"],
                     help="sandboxes: deposited beds in contact (default) or the falling lattice")
-    ap.add_argument("--train-beds", type=int, default=3)
+    ap.add_argument("--train-beds", type=int, default=16)
+    ap.add_argument("--train-n", type=int, default=50000, help="spheres per training bed (half to all)")
+    ap.add_argument("--train-frames", type=int, default=12)
     ap.add_argument("--train-iters", type=int, default=300)
     ap.add_argument("--strides", type=int, default=5)
     ap.add_argument("--judge-every", type=int, default=5)

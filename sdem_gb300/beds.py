@@ -678,14 +678,15 @@ def fixed_floor_case(n: int, seed: int, **kw) -> Case:
 
 
 def sandbox_case(rng: np.random.Generator, index: int, n_lo: int = 2000, n_hi: int = 50000,
-                 layout: str = "lattice") -> Case:
+                 layout: str = "lattice", cf_type: Optional[int] = None) -> Case:
     """One sandbox of the batched workload: n ~ U{n_lo..n_hi} spheres with d
     uniform in [0.8, 1.2] mm (five types, density 2500 kg/m^3), sliding
     friction U(0.1, 0.5), restitution U(0.5, 0.95), linear spring-dashpot or
     Hertz-Mindlin by a coin flip, dt = 2e-6 s, AB2; a jittered simple-cubic
     lattice (pitch 1.3 d_max) filling a box of aspect ratios x:y:z = a:1:b with
     a, b ~ U(0.5, 2), five infinite walls, velocities U(-0.05, 0.05) m/s.  The
-    parameters are drawn from `rng` in a fixed order.  layout="deposited"
+    parameters are drawn from `rng` in a fixed order (cf_type, when given,
+    replaces the coin flip's model after the flip).  layout="deposited"
     puts the same spheres, on the same footprint, as a bed already in
     contact: deposited_positions (column grid spacing 1.1 d_max, jitter
     0.04 d_max), each sphere resting on its support without overlap, at
@@ -694,6 +695,8 @@ def sandbox_case(rng: np.random.Generator, index: int, n_lo: int = 2000, n_hi: i
     mu = float(rng.uniform(0.1, 0.5))
     e_n = float(rng.uniform(0.5, 0.95))
     cf = props.CFT_LSD if rng.uniform() < 0.5 else props.CFT_NLIN
+    if cf_type is not None:
+        cf = cf_type
     a, b = float(rng.uniform(0.5, 2.0)), float(rng.uniform(0.5, 2.0))
     seed = int(rng.integers(0, 2**31 - 1))
     ntypes = 5

@@ -591,6 +591,11 @@ def targets(v0, v1, w0, w1, r, h: float, gravity) -> np.ndarray:
     return np.concatenate([a, al], axis=1).astype(np.float32)
 
 
+def _frame(system):
+    st = system.state()
+    return st.posR.copy(), st.linVel[:, 0, :].copy(), st.rotVel[:, 0, :].copy(), st.id.copy()
+
+
 def record_samples(system, case, stride: int, frames: int, settle: int = 0) -> List[Sample]:
     """Runs the plain DEM (a DEMSystem of `case`) and turns consecutive
     stride frames into samples (frames - 3 of them)."""
@@ -600,8 +605,38 @@ def record_samples(system, case, stride: int, frames: int, settle: int = 0) -> L
     for k in range(frames):
         if k:
             system.step(stride)
-        st = system.state()
-        snaps.append((st.posR.copy(), st.linVel[:, 0, :].copy(), st.rotVel[:, 0, :].copy(), st.id.copy()))
+        snaps.append(_frame(system))
+    return samples_from_frames(snaps, case, stride)
+
+
+def record_samples_batch(systems, cases, stride: int, frames: int, settle: int = 0,
+                         group_size: int = 0) -> List[List[Sample]]:
+    """record_samples for many beds at once: the plain path's batched form
+    (capi.DEMBatch, one captured graph per group of beds) advances all of
+    them through the settling and from frame to frame; each bed's frames
+    are downloaded between batch steps.  Even step counts keep the batch's
+    two-step graphs whole."""
+    from .capi import DEMBatch
+    if stride % 2 or settle % 2:
+        raise ValueError("record_samples_batch: stride and settle must be even")
+    b = DEMBatch(systems, group_size=group_size)
+    snaps = [[] for _ in systems]
+    try:
+        if settle:
+            b.step(settle)
+        for k in range(frames):
+            if k:
+                b.step(stride)
+            for i, s in enumerate(systems):
+                snaps[i].append(_frame(s))
+    finally:
+        b.close()
+    return [samples_from_frames(sn, c, stride) for sn, c in zip(snaps, cases)]
+
+
+def samples_from_frames(snaps, case, stride: int) -> List[Sample]:
+    """Samples from consecutive frames (posR, v, omega, id) a stride apart."""
+    frames = len(snaps)
     h = stride * case.opts.dt
     out = []
     for k in range(2, frames - 1):

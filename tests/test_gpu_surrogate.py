@@ -305,3 +305,23 @@ def test_runner_judges_and_falls_back(sg_lib):
         for a in range(3):
             assert np.all(p[:, a] >= box.lo[a]) and np.all(p[:, a] <= box.hi[a])
         s.close()
+
+
+def test_batched_recording_equals_single_beds(sg_lib):
+    # training frames recorded through the batched form (one graph per group
+    # of beds) are the frames of each bed stepped alone, bit for bit
+    from sdem_gb300 import props
+    rng = np.random.default_rng(7)
+    cases = [beds.sandbox_case(rng, k, n_lo=800, n_hi=1600, cf_type=props.CFT_NLIN) for k in range(3)]
+    systems = [DEMSystem(c) for c in cases]
+    batched = sg.record_samples_batch(systems, cases, stride=20, frames=5, settle=200, group_size=2)
+    for s in systems:
+        s.close()
+    for c, got in zip(cases, batched):
+        s = DEMSystem(c)
+        want = sg.record_samples(s, c, 20, 5, settle=200)
+        s.close()
+        assert len(got) == len(want) == 2
+        for a, b in zip(got, want):
+            for f in ("posR", "vel", "omega", "target"):
+                np.testing.assert_array_equal(getattr(a, f), getattr(b, f))
