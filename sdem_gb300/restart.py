@@ -20,7 +20,9 @@ it (:731-844, :296-377), for the standalone build (no CFDDEM block):
 
 The reference numbers TanDel records in the order of its contact container's
 slots (CL_Prepare_Restart, Prtcl_CL_and_CF.f90:344-359), an artefact of its
-free list; this writer numbers them in order of first listing.  Its reader
+free list; this writer numbers them in order of first listing, one record per
+contact (the two listings of a pair of local spheres share it; contacts with
+periodic images have their own).  Its reader
 resolves the indices either way, so files interoperate; byte equality with a
 file the reference wrote holds up to that numbering.
 """
@@ -63,7 +65,13 @@ def write_restart(path: str, p: Particles, contacts: Optional[tuple], tsize: int
     for k in range(len(owner)):
         g = int(ids[owner[k]])
         q = int(partner[k])
-        key = (g, q) if q > base_wall_id else (min(g, q), max(g, q))
+        # A pair of local spheres is listed under both, with one record; a
+        # contact with a periodic image is listed under its local sphere only,
+        # and two spheres can each touch the other's image (two records under
+        # the same two ids).  Listings share a record when their ids and their
+        # history agree bit for bit.
+        h = np.array([tand[k, 0], tand[k, 1], tand[k, 2], vrel[k]], np.float64).tobytes()
+        key = (g, q) if q > base_wall_id else (min(g, q), max(g, q), h)
         if key not in index:
             index[key] = len(recs) + 1
             recs.append((tand[k, 0], tand[k, 1], tand[k, 2], vrel[k]))
@@ -87,8 +95,14 @@ def read_restart(path: str, tsize: int, rsize: int, radius_of_type: np.ndarray,
                  dom_min=None, dom_max=None) -> Tuple[Particles, tuple]:
     """Returns (particles, contacts) as PIO_Read_Restart + PIO_RestartCL build them
     on one rank: particles outside [dom_min, dom_max) are skipped, the radius
-    comes from the type (Prtcl_IOAndVisu.f90:809)."""
-    raw = np.fromfile(path, dtype=np.uint8)
+    comes from the type (Prtcl_IOAndVisu.f90:809).  A path ending in .gz is
+    read through gzip."""
+    if path.endswith(".gz"):
+        import gzip
+        with gzip.open(path, "rb") as f:
+            raw = np.frombuffer(f.read(), dtype=np.uint8)
+    else:
+        raw = np.fromfile(path, dtype=np.uint8)
     off = 0
 
     def take(dtype, count):
