@@ -284,7 +284,8 @@ int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatch
  * it (1..8; default 3).  Results are bit-identical for every value (every
  * order that matters is fixed by sort positions); only the speed changes,
  * which sdem_gb300/tune.py measures.  0 keeps a value; a change makes the
- * next step capture its graphs again. */
+ * next step capture its graphs again.  sdem_get_launch reports even chunks
+ * as first_chunk_percent 0. */
 int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm, int first_chunk_percent);
 int sdem_get_launch(sdem_h* h, int* pipeline_chunks, int* force_blocks_per_sm, int* first_chunk_percent);
 
