@@ -2152,7 +2152,7 @@ struct sdem_h {
   GRec* gorder = nullptr;
   // second stream and events of the chunked search/force pipeline
   cudaStream_t stream2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_chunk[kMaxChunks] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_rows = nullptr, ev_chunk[kMaxChunks] = {};
   int nchunk = kChunks;                  // launch shape (sdem_set_launch); results do not depend on it
   int force_bps = kForceBlocksPerSM;
   int first_pct = 0;                     // percent of the targets in the first chunk (0: even chunks)
@@ -2505,11 +2505,19 @@ int enqueue_step(sdem_h* h) {
     k_wall_force<<<std::max(1, h->num_sms * 2), kThreads, 0, st>>>(d);
   } else {
     k_wall_force<<<std::max(1, h->num_sms * 2), kThreads, 0, s2>>>(d);
-    cudaEventRecord(h->ev_join, s2);
     for (int k = 0; k < nchunk; k++) {
       const int a = cut(k), b = cut(k + 1);
       cudaStreamWaitEvent(st, h->ev_chunk[k], 0);
       scan(h, h->row_cnt + a, b - a, h->row_off + a, k ? h->row_off + a : nullptr);
+      if (k == nchunk - 1) {
+        // every row offset is known: the gather order (which needs them and
+        // the wall contacts, not the forces) is built on the second stream
+        // beside the last forces
+        cudaEventRecord(h->ev_rows, st);
+        cudaStreamWaitEvent(s2, h->ev_rows, 0);
+        k_degree_scatter<<<grid_for(n), kThreads, 0, s2>>>(d);
+        cudaEventRecord(h->ev_join, s2);
+      }
       k_row_fill<<<grid_for(std::max(b - a, 1)), kThreads, 0, st>>>(d, a, b);
       if (h->gcap > 0 || h->nfix > 0) k_force<true><<<h->num_sms * h->force_bps, kThreads, 0, st>>>(d, a, b);
       else k_force<false><<<h->num_sms * h->force_bps, kThreads, 0, st>>>(d, a, b);
@@ -2517,7 +2525,7 @@ int enqueue_step(sdem_h* h) {
     cudaStreamWaitEvent(st, h->ev_join, 0);
   }
   mark(PH_GATHER);
-  k_degree_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
+  if (s2 == st) k_degree_scatter<<<grid_for(n), kThreads, 0, st>>>(d);
   k_gather<<<grid_for(n), kThreads, 0, st>>>(d);
   k_integrate<<<grid_for(n), kThreads, 0, st>>>(d);
   mark(PH_DELETE);
@@ -2672,6 +2680,7 @@ int sdem_create(const sdem_cfg* cfg, sdem_h** out) {
   CK(cudaEventCreateWithFlags(&h->ev_snap_done, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&h->ev_rows, cudaEventDisableTiming));
   for (int k = 0; k < 6; k++) CK(cudaEventCreateWithFlags(&h->ev_xfer[k], cudaEventDisableTiming));
   for (int k = 0; k < kMaxChunks; k++) CK(cudaEventCreateWithFlags(&h->ev_chunk[k], cudaEventDisableTiming));
   int N = c.n_capacity;
@@ -3942,6 +3951,7 @@ void sdem_destroy(sdem_h* h) {
   for (int b = 0; b < 2; b++)
     if (h->ev_step[b]) cudaEventDestroy(h->ev_step[b]);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->ev_rows) cudaEventDestroy(h->ev_rows);
   for (int k = 0; k < 6; k++)
     if (h->ev_xfer[k]) cudaEventDestroy(h->ev_xfer[k]);
   for (int k = 0; k < kMaxChunks; k++)
