@@ -31,7 +31,9 @@
 //
 // Search, row offsets, row fill and forces run in chunks of target sort
 // positions on two streams, so that the search of one chunk (integer and
-// memory work) overlaps the force kernel of the one before (FP64 work).
+// memory work) overlaps the force kernel of the one before (FP64 work); wall
+// detection, wall forces and the gather order follow the searches on the
+// second stream, beside the forces.
 //   k_gather                           per particle, sums its contact records in the reference's scatter
 //                                      order (a deterministic gather; records signed for the row's
 //                                      target, moments scaled by the particle's own radius), then its
