@@ -279,13 +279,16 @@ int sdem_selftest_fp64(long long n, unsigned long long seed, long long* mismatch
 /* ---- launch shape (no counterpart in the reference) -------------------------
  * The step's search/force pipeline runs in pipeline_chunks chunks of target
  * sort positions (1..4; default 2), the first of them holding
- * first_chunk_percent percent of the targets (10..90; -1: even chunks, the
- * default), and the force kernel with force_blocks_per_sm blocks per SM in
- * it (1..8; default 3).  Results are bit-identical for every value (every
+ * first_chunk_percent percent of the targets (10..90; -1: the default split,
+ * where the first chunk holds as many whole waves of resident search blocks
+ * as fit in an even share when that trims the share by a quarter at most,
+ * else an even share, and the other chunks share the rest evenly), and
+ * the force kernel with force_blocks_per_sm blocks per SM in it (1..8;
+ * default 3).  Results are bit-identical for every value (every
  * order that matters is fixed by sort positions); only the speed changes,
  * which sdem_gb300/tune.py measures.  0 keeps a value; a change makes the
- * next step capture its graphs again.  sdem_get_launch reports even chunks
- * as first_chunk_percent 0. */
+ * next step capture its graphs again.  sdem_get_launch reports the default
+ * split as first_chunk_percent 0. */
 int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm, int first_chunk_percent);
 int sdem_get_launch(sdem_h* h, int* pipeline_chunks, int* force_blocks_per_sm, int* first_chunk_percent);
 

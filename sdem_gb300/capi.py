@@ -370,12 +370,13 @@ class DEMSystem:
 
     def set_launch(self, pipeline_chunks: int = 0, force_blocks_per_sm: int = 0, first_chunk_percent: int = 0) -> None:
         """sdem_set_launch: the step's launch shape (results do not depend on
-        it); first_chunk_percent -1 restores even chunks, 0 keeps a value."""
+        it); first_chunk_percent -1 restores the default split (a first chunk
+        of whole search waves), 0 keeps a value."""
         self._check(self.lib.sdem_set_launch(self.h, int(pipeline_chunks), int(force_blocks_per_sm),
                                              int(first_chunk_percent)))
 
     def get_launch(self) -> tuple:
-        """(pipeline_chunks, force_blocks_per_sm, first_chunk_percent; 0 = even)."""
+        """(pipeline_chunks, force_blocks_per_sm, first_chunk_percent; 0 = the default split)."""
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         self._check(self.lib.sdem_get_launch(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value

@@ -80,6 +80,7 @@ constexpr int kDegBuckets = 64;   // gather-order buckets by number of contact r
 #endif
 constexpr int kChunks = SDEM_PIPELINE_CHUNKS;   // search/force pipeline chunks per step (default)
 constexpr int kMaxChunks = 4;                   // most chunks sdem_set_launch accepts
+constexpr int kSearchBlocksPerSM = 6;           // k_search's register budget: resident blocks of kThreads
 constexpr int kForceBlocksPerSM = 3;            // k_force blocks per SM in the pipeline (default)
 #ifndef SDEM_FORCE_MIN_BLOCKS
 #define SDEM_FORCE_MIN_BLOCKS 3    // k_force blocks of 256 threads per SM its register budget allows
@@ -679,7 +680,7 @@ __global__ void k_cellorder(Dev d) {
 // Six blocks per SM (40 registers): the walk is latency bound, and the extra
 // resident warps measured faster than the unconstrained 60-register build.
 template <bool kHier>
-__global__ void __launch_bounds__(kThreads, 6) k_search(Dev d, int s_begin, int s_end) {
+__global__ void __launch_bounds__(kThreads, kSearchBlocksPerSM) k_search(Dev d, int s_begin, int s_end) {
   int s = s_begin + blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = *d.nt;
   const int nloc = *d.n;
@@ -2157,7 +2158,7 @@ struct sdem_h {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_rows = nullptr, ev_chunk[kMaxChunks] = {};
   int nchunk = kChunks;                  // launch shape (sdem_set_launch); results do not depend on it
   int force_bps = kForceBlocksPerSM;
-  int first_pct = 0;                     // percent of the targets in the first chunk (0: even chunks)
+  int first_pct = 0;                     // percent of the targets in the first chunk (0: whole search waves)
   int cur = 0;  // buffer written by the next step
   // device scalars
   int* scal = nullptr;  // n, status[2], iter, next_update, out_cnt, counters_out[8]
@@ -2471,9 +2472,19 @@ int enqueue_step(sdem_h* h) {
   cudaStream_t s2 = ev ? st : h->stream2;
   // chunk boundaries on scan tiles, so that each chunk's row scan moves whole
   // aligned tiles
-  // (the first chunk may take first_pct percent of the targets, the others
-  // share the rest evenly: a short first search starts the forces sooner)
-  const long long first = (nchunk > 1 && h->first_pct > 0) ? (long long)na * h->first_pct / 100 : -1;
+  // The first chunk's search runs alone, before any force: by default it
+  // takes as many whole waves of resident search blocks as fit in an even
+  // share, when that trims the share by a quarter at most, so that its last
+  // wave is full (a partial last wave takes a whole wave's time); or
+  // first_pct percent of the targets.  The other chunks share the rest
+  // evenly.
+  long long first = -1;
+  if (nchunk > 1) {
+    const long long wave = (long long)h->num_sms * kSearchBlocksPerSM * kThreads;
+    const long long share = na / nchunk, whole = share / wave * wave;
+    if (h->first_pct > 0) first = (long long)na * h->first_pct / 100;
+    else if (whole > 0 && 4 * (share - whole) <= share) first = whole;
+  }
   auto cut = [&](int k) {
     if (k == 0) return 0;
     if (k == nchunk) return na;
@@ -3874,7 +3885,7 @@ int sdem_set_launch(sdem_h* h, int pipeline_chunks, int force_blocks_per_sm, int
   if (pipeline_chunks < 0 || pipeline_chunks > kMaxChunks || force_blocks_per_sm < 0 || force_blocks_per_sm > 8 ||
       first_chunk_percent < -1 || first_chunk_percent > 90 || (first_chunk_percent > 0 && first_chunk_percent < 10))
     return set_err(h, SDEM_E_ARG, "sdem_set_launch: pipeline_chunks in 1..4, force_blocks_per_sm in 1..8, "
-                                  "first_chunk_percent in 10..90 or -1 for even chunks (0 keeps)");
+                                  "first_chunk_percent in 10..90 or -1 for the default split (0 keeps)");
   const int nc = pipeline_chunks ? pipeline_chunks : h->nchunk;
   const int fb = force_blocks_per_sm ? force_blocks_per_sm : h->force_bps;
   const int fp = first_chunk_percent == 0 ? h->first_pct : (first_chunk_percent < 0 ? 0 : first_chunk_percent);

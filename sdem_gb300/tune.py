@@ -41,7 +41,7 @@ CACHE_DIR = os.path.join(os.path.dirname(HERE), ".tunecache")
 
 CHUNKS = (1, 2, 3, 4)
 FORCE_BLOCKS = (2, 3, 4)
-FIRST_CHUNK = (-1, 25, 35)        # percent of the targets in the first chunk (-1: even chunks)
+FIRST_CHUNK = (-1, 25, 35)        # percent of the targets in the first chunk (-1: whole search waves)
 CELL_FACTORS = (1.0, 1.25, 1.5)
 GROUP_SIZES = (16, 32, 64, 128)
 
