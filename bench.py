@@ -274,13 +274,15 @@ def reference_arm(args):
 STATE_FIELDS = ("id", "ptype", "usrmark", "posR", "linVel", "linAcc", "theta", "rotVel", "rotAcc")
 
 
-def e2e_run(case, K, pinned: bool, barrier, shape=None):
+def e2e_run(case, K, pinned: bool, barrier, shape=None, reps: int = 3):
     """The metric through the C ABI with host buffers: upload of the state,
     K x (sdem_step_async(h,1) + the step's counters read back), download of
     the state.  pinned: page-locked host arrays; else ordinary (pageable)
     numpy arrays, what a Fortran caller's arrays are unless it registers
     them.  The arrays have been through one untimed upload and download
-    first.  Returns (elapsed s, h2d bytes, d2h bytes)."""
+    first.  The run is timed `reps` times (each from its own upload of the
+    same state); returns (median elapsed s, h2d bytes, d2h bytes, all
+    elapsed s)."""
     import torch
     from sdem_gb300 import beds
     from sdem_gb300.capi import DEMSystem
@@ -303,24 +305,26 @@ def e2e_run(case, K, pinned: bool, barrier, shape=None):
     # freshly allocated host pages pays their one-time mapping, not the path
     sys2.upload(st)
     sys2.state(out=out_buf)
-    barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sys2.upload(st)
-    sys2.step_async(1)
-    for k in range(1, K + 1):
-        if k < K:
-            sys2.step_async(1)          # step k+1 is queued ...
-            sys2.counters_lagged()      # ... while step k's counters are read
-        else:
-            sys2.counters()
-    out = sys2.state(out=out_buf)
-    torch.cuda.synchronize()
-    el = time.perf_counter() - t0
+    els = []
+    for _ in range(reps):
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sys2.upload(st)
+        sys2.step_async(1)
+        for k in range(1, K + 1):
+            if k < K:
+                sys2.step_async(1)          # step k+1 is queued ...
+                sys2.counters_lagged()      # ... while step k's counters are read
+            else:
+                sys2.counters()
+        out = sys2.state(out=out_buf)
+        torch.cuda.synchronize()
+        els.append(time.perf_counter() - t0)
     h2d = sum(getattr(st, f).nbytes for f in STATE_FIELDS)
     d2h = sum(getattr(out, f).nbytes for f in STATE_FIELDS) + K * 4 * 9
     sys2.close()
-    return el, h2d, d2h
+    return statistics.median(els), h2d, d2h, els
 
 
 def fp64_step_model(C: float, n: int, pw: float) -> float:
@@ -420,14 +424,16 @@ def our_arm(args):
         Ke = args.e2e_steps
         runs = {}
         for pinned in (True, False):
-            el, h2d, d2h = e2e_run(case, Ke, pinned, barrier, shape)
+            el, h2d, d2h, els = e2e_run(case, Ke, pinned, barrier, shape)
             _, el, _ = replicas.aggregate(el, n, Ke, device="cuda")
             runs[pinned] = {"value": n_all * Ke / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / Ke),
-                            "d2h_bytes_per_step": int(d2h / Ke), "steps": Ke}
+                            "d2h_bytes_per_step": int(d2h / Ke), "steps": Ke,
+                            "runs_ms": [round(x * 1e3, 3) for x in els]}
         e2e = dict(runs[True], note="upload of the state from page-locked host memory, K x (sdem_step_async(h,1) "
                    "+ the counters of each step read back: sdem_counters_lagged while the next step runs, "
                    "sdem_counters after the last), download of the state into page-locked host memory; the "
-                   "host arrays went through one untimed upload and download first")
+                   "host arrays went through one untimed upload and download first; median of three timed "
+                   "runs (runs_ms, rank 0's)")
         e2e_pageable = dict(runs[False], note="the same with ordinary (pageable) host arrays, as an unmodified "
                             "Fortran caller passes them")
 
