@@ -720,6 +720,76 @@ def surrogate_arm(args):
     dem.close()
 
 
+def transfers_arm(args):
+    """The host side of the end-to-end figure (its own line): the host link's
+    copy bandwidth (260 MiB from page-locked memory, one stream against four)
+    and the library's upload and download of the 1M bed's state
+    (sdem_upload_particles / sdem_download_particles, page-locked and pageable
+    host arrays, median of 5 after one untimed transfer).  Host clock around
+    synchronised calls."""
+    import torch
+    from sdem_gb300 import beds
+    from sdem_gb300.capi import DEMSystem
+    torch.cuda.set_device(0)
+    N = 260 * 2**20
+    hbuf = torch.empty(N, dtype=torch.uint8, pin_memory=True)
+    hbuf.fill_(1)
+    dbuf = torch.empty(N, dtype=torch.uint8, device="cuda")
+    streams = [torch.cuda.Stream() for _ in range(4)]
+
+    def copy_rate(ns, h2d):
+        parts = [(i * N // ns, (i + 1) * N // ns) for i in range(ns)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for (a, b), st in zip(parts, streams):
+            with torch.cuda.stream(st):
+                if h2d:
+                    dbuf[a:b].copy_(hbuf[a:b], non_blocking=True)
+                else:
+                    hbuf[a:b].copy_(dbuf[a:b], non_blocking=True)
+        torch.cuda.synchronize()
+        return N / (time.perf_counter() - t0) / 1e9
+
+    link = {}
+    for h2d in (True, False):
+        for ns in (1, 4):
+            copy_rate(ns, h2d)
+            link[f"{'h2d' if h2d else 'd2h'}_{ns}_streams_gbs"] = max(copy_rate(ns, h2d) for _ in range(5))
+    case, _ = make_case("hertz_poly_1m_deposited", args.n or 1_000_000, 2)
+    s = DEMSystem(case)
+    s.step(2)
+    st0 = s.state()
+    out = {}
+    for pinned in (True, False):
+        st = pinned_particles(st0) if pinned else st0
+        cap = s.cfg.n_capacity
+        buf = (pinned_particles(st0, rows=cap) if pinned else
+               beds.Particles(*(np.zeros((cap,) + getattr(st0, f).shape[1:], dtype=getattr(st0, f).dtype)
+                                for f in STATE_FIELDS)))
+        s.upload(st)
+        s.state(out=buf)
+        up, down = [], []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.upload(st)
+            t1 = time.perf_counter()
+            s.state(out=buf)
+            t2 = time.perf_counter()
+            up.append((t1 - t0) * 1e3)
+            down.append((t2 - t1) * 1e3)
+        key = "page_locked" if pinned else "pageable"
+        out[key] = {"upload_ms": statistics.median(up), "download_ms": statistics.median(down),
+                    "bytes_each_way": int(sum(getattr(st, f).nbytes for f in STATE_FIELDS))}
+    s.close()
+    line = {"metric": "host transfers of the 1M bed's state", "unit": "ms", "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "transfers", "particles": case.particles.n}, "host_link": link,
+            "state_transfers": out,
+            "note": "host clock around synchronised calls; the state arrays went through one untimed upload "
+                    "and download first"}
+    print(json.dumps(line), flush=True)
+
+
 def surrogate_gemm_arm(args):
     """The surrogate's GEMM alone (its own line): the first edge layer of the
     network's forward -- E rows gathered from node latents twice plus the
@@ -856,10 +926,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shape")
     ap.add_argument("--workload", default="hertz_poly_1m",
-                    choices=[*WORKLOADS, "sandboxes", "surrogate", "surrogate_gemm"],
+                    choices=[*WORKLOADS, "sandboxes", "surrogate", "surrogate_gemm", "transfers"],
                     help="hertz_poly_1m (the headline), hertz_poly_1m_deposited, lsd_mono_20k, hopper_4m; "
                          "sandboxes: the batched workload; surrogate: the learned surrogate against the plain "
-                         "DEM (each its own line)")
+                         "DEM; transfers: the host link and the state's upload and download (each its own line)")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--contact-steps", type=int, default=1000,
                     help="sandboxes: batch steps before timing")
@@ -876,6 +946,8 @@ def main():
         args.warmup = 3
     if args.workload == "sandboxes":
         sandboxes_arm(args)
+    elif args.workload == "transfers":
+        transfers_arm(args)
     elif args.workload == "surrogate_gemm":
         surrogate_gemm_arm(args)
     elif args.workload == "surrogate":
