@@ -1,7 +1,7 @@
 """ctypes driver of the CPU oracle (oracle/sdem_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
-baseline leg of bench.py as the checker.  The product never imports it.
+baseline leg of bench.py, to check the GPU path.  The product never imports it.
 
 OracleSystem mirrors sdem_gb300.capi.DEMSystem (same constructor, step, state,
 forces, contacts, counters), so a test runs one Case through both.

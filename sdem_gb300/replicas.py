@@ -1,5 +1,5 @@
 """Replica runs across GPUs: one independent bed per rank, no collective on the
-data path (the bed does not shard across GPUs in this build).  Only the timing
+data path (one bed is not split across GPUs).  Only the timing
 is reduced: barrier before and after the timed region, max of the elapsed time
 and sum of the particles over ranks."""
 from __future__ import annotations

@@ -16,7 +16,7 @@ from tests.helpers import assert_same_contact_sets, compare_history, force_scale
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-12   # forces, torques and contact history (spec bar)
+RTOL = 1e-12   # forces, torques and contact history (the parity bar)
 
 
 def cloud(**kw):
