@@ -1,9 +1,9 @@
 /*
  * sdem_oracle.c -- CPU restatement of sDEM's per-step particle hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the GB300
- * kernels: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
- * leg may load it.  No product code path calls it.
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the GB300 kernels are
+ * compared with: only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg may load it.  No product code path calls it.
  *
  * It restates, single-threaded and in the reference's own order of operations,
  * the Fortran routines of GongZheng-Justin/sDEM (src/DEM/...):

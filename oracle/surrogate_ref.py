@@ -1,5 +1,5 @@
 """CPU statement of the learned surrogate (test infrastructure only: the
-checker of libsdem_surrogate.so, never called by the product path).
+oracle libsdem_surrogate.so is compared with, never called by the product path).
 
 The surrogate has no counterpart in the reference; this module restates the
 library's contract (include/sdem_surrogate.h) in numpy:

@@ -16,7 +16,7 @@ SRC = os.path.join(HERE, "csrc", "fp64_int_check.cpp")
 
 
 @pytest.fixture(scope="module")
-def checker(tmp_path_factory):
+def fpi_check(tmp_path_factory):
     gxx = shutil.which("g++")
     if not gxx:
         pytest.skip("no g++")
@@ -26,7 +26,7 @@ def checker(tmp_path_factory):
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3])
-def test_integer_binary64_matches_ieee(checker, seed):
-    r = subprocess.run([checker, str(seed), "400000"], capture_output=True, text=True)
+def test_integer_binary64_matches_ieee(fpi_check, seed):
+    r = subprocess.run([fpi_check, str(seed), "400000"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout[-2000:]
     assert r.stdout.startswith("ok ")
