@@ -173,3 +173,45 @@ def test_rebound_on_fixed_sphere():
     v = s.state().linVel[0, 0]
     assert e < v[1] / 0.2 < e + 0.1, v
     assert abs(v[0]) < 1e-12 and abs(v[2]) < 1e-12
+
+
+def test_hertz_static_normal_force():
+    # two Hertz spheres at rest pressed by delta: no damping (no relative
+    # velocity) and no spring history, so the force is K delta^1.5 with
+    # K = 4/3 E* sqrt(R*), E* = E / (2 (1 - nu^2)), R* = r / 2 (equal spheres)
+    E, nu, d, delta = 5e7, 0.3, 1e-3, 3e-6
+    case = two_sphere_case(props.CFT_NLIN, 0.0, e_n=0.8, E=E)
+    mid = 0.005
+    case.particles.posR[0, 0] = mid - (d - delta) / 2
+    case.particles.posR[1, 0] = mid + (d - delta) / 2
+    s = OracleSystem(case)
+    s.step(1)
+    F, T = s.forces()
+    assert s.counters()["pp"] == 1
+    K = 4.0 / 3.0 * (E / (2.0 * (1.0 - nu * nu))) * math.sqrt(d / 4.0)
+    want = K * delta ** 1.5
+    assert F[0, 0] == pytest.approx(-want, rel=1e-10) and F[1, 0] == pytest.approx(want, rel=1e-10)
+    assert np.abs(F[:, 1:]).max() == 0.0 and np.abs(T).max() == 0.0
+
+
+def test_hertz_elastic_impact_peak_overlap():
+    # restitution 1 (no damping): a head-on impact reaches the Hertz maximum
+    # overlap (15 m* v^2 / (16 E* sqrt(R*)))^(2/5) and leaves at the speed it came
+    E, nu, d, v = 5e7, 0.3, 1e-3, 0.2
+    case = two_sphere_case(props.CFT_NLIN, v, e_n=1.0, mu=0.0, E=E, dt=1e-8)
+    s = OracleSystem(case)
+    m = 2500.0 * math.pi / 6.0 * d ** 3
+    Es = E / (2.0 * (1.0 - nu * nu))
+    want = (15.0 * (m / 2.0) * (2.0 * v) ** 2 / (16.0 * Es * math.sqrt(d / 4.0))) ** 0.4
+    peak, touched = 0.0, False
+    for _ in range(4000):
+        s.step(5)
+        st = s.state()
+        ov = d - (st.posR[1, 0] - st.posR[0, 0])
+        peak = max(peak, ov)
+        touched = touched or ov > 0
+        if touched and ov < 0:
+            break
+    assert peak == pytest.approx(want, rel=2e-3), (peak, want)
+    st = s.state()
+    assert (st.linVel[1, 0, 0] - st.linVel[0, 0, 0]) / (2 * v) == pytest.approx(1.0, abs=2e-3)
