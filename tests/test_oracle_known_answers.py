@@ -215,3 +215,37 @@ def test_hertz_elastic_impact_peak_overlap():
     assert peak == pytest.approx(want, rel=2e-3), (peak, want)
     st = s.state()
     assert (st.linVel[1, 0, 0] - st.linVel[0, 0, 0]) / (2 * v) == pytest.approx(1.0, abs=2e-3)
+
+
+def test_lsd_static_normal_force():
+    # linear spring-dashpot at rest: VelRel_Init = max(|v_rn|, 0.01) = 0.01, so
+    # the stiffness is Kn 0.01^0.4 and the force Kn 0.01^0.4 delta
+    d, delta = 1e-3, 2e-6
+    case = two_sphere_case(props.CFT_LSD, 0.0, e_n=0.9)
+    mid = 0.005
+    case.particles.posR[0, 0] = mid - (d - delta) / 2
+    case.particles.posR[1, 0] = mid + (d - delta) / 2
+    s = OracleSystem(case)
+    s.step(1)
+    F, _ = s.forces()
+    kn = abs(case.tables.bpp.reshape(1, 1, props.BP_SIZE)[0, 0, 2])
+    want = kn * 0.01 ** 0.4 * delta
+    assert F[0, 0] == pytest.approx(-want, rel=1e-10) and F[1, 0] == pytest.approx(want, rel=1e-10)
+
+
+def test_hertz_wall_static_force():
+    # a sphere at rest pressed into an infinite floor by delta: the wall's
+    # radius is infinite, so R* = r, and E* = 1 / ((1-nu^2)/E + (1-nu_w^2)/E_w)
+    E, nu, d, delta = 5e7, 0.3, 1e-3, 4e-6
+    walls = box_walls((0.0, 0.0, 0.0), (0.01, 0.01, 0.01))
+    case = two_sphere_case(props.CFT_NLIN, 0.0, e_n=0.8, E=E, walls=walls)
+    p = case.particles.take(np.array([0]))
+    p.posR[0, :3] = (0.005, d / 2 - delta, 0.005)
+    s = OracleSystem(beds.Case("wall", case.opts, case.tables, walls, p))
+    s.step(1)
+    F, T = s.forces()
+    assert s.counters()["pw"] == 1
+    Es = 1.0 / (2.0 * (1.0 - nu * nu) / E)
+    want = 4.0 / 3.0 * Es * math.sqrt(d / 2.0) * delta ** 1.5
+    assert F[0, 1] == pytest.approx(want, rel=1e-10)
+    assert abs(F[0, 0]) == 0.0 and abs(F[0, 2]) == 0.0 and np.abs(T).max() == 0.0
