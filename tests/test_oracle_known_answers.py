@@ -249,3 +249,27 @@ def test_hertz_wall_static_force():
     want = 4.0 / 3.0 * Es * math.sqrt(d / 2.0) * delta ** 1.5
     assert F[0, 1] == pytest.approx(want, rel=1e-10)
     assert abs(F[0, 0]) == 0.0 and abs(F[0, 2]) == 0.0 and np.abs(T).max() == 0.0
+
+
+def test_rolling_resistance_torque_on_a_spinning_sphere():
+    # a sphere pressed into the floor and spinning about the floor's normal:
+    # the contact point does not slide (omega is parallel to n), so the only
+    # torque is the rolling resistance -mu_r |f_n| R* w_hat (CT_Model 1,
+    # Prtcl_ContactForce_inc.f90), with R* = r against a wall
+    E, nu, d, delta, mur, w = 5e7, 0.3, 1e-3, 4e-6, 0.1, 30.0
+    c = (0.3, 0.3, mur, 0.8, 0.8)
+    t = props.build_tables(props.CFT_NLIN, [d], [2500.0], [E], [nu], c, [E], [nu], c)
+    o = beds.Options(dt=1e-8, minpoint=(0, 0, 0), maxpoint=(0.01, 0.01, 0.01), gravity=(0.0, 0.0, 0.0),
+                     cf_type=props.CFT_NLIN, pi_method=2, pri_method=2)
+    walls = box_walls((0.0, 0.0, 0.0), (0.01, 0.01, 0.01))
+    p = beds.new_particles(np.array([[0.005, d / 2 - delta, 0.005]]), np.array([1]), t.radius,
+                           np.zeros((1, 3)), o.tsize, o.rsize)
+    p.rotVel[:, :, 1] = w
+    s = OracleSystem(beds.Case("spin", o, t, walls, p))
+    s.step(1)
+    F, T = s.forces()
+    Es = 1.0 / (2.0 * (1.0 - nu * nu) / E)
+    fn = 4.0 / 3.0 * Es * math.sqrt(d / 2.0) * delta ** 1.5
+    assert F[0, 1] == pytest.approx(fn, rel=1e-10) and abs(F[0, 0]) == 0.0 and abs(F[0, 2]) == 0.0
+    assert T[0, 1] == pytest.approx(-mur * fn * d / 2.0, rel=1e-10)
+    assert abs(T[0, 0]) == 0.0 and abs(T[0, 2]) == 0.0
