@@ -273,3 +273,20 @@ def test_rolling_resistance_torque_on_a_spinning_sphere():
     assert F[0, 1] == pytest.approx(fn, rel=1e-10) and abs(F[0, 0]) == 0.0 and abs(F[0, 2]) == 0.0
     assert T[0, 1] == pytest.approx(-mur * fn * d / 2.0, rel=1e-10)
     assert abs(T[0, 0]) == 0.0 and abs(T[0, 2]) == 0.0
+
+
+@pytest.mark.parametrize("cf", [props.CFT_NLIN, props.CFT_LSD])
+def test_pair_forces_cancel_in_a_cloud(cf):
+    # without walls and gravity every force is a pair force, added to one
+    # sphere and subtracted from the other: the forces of a dense moving
+    # cloud sum to zero up to the rounding of each sphere's own sum
+    import dataclasses
+    case = beds.lattice_cloud_case(800, seed=41, cf_type=cf, ntypes=5)
+    opts = dataclasses.replace(case.opts, gravity=(0.0, 0.0, 0.0))
+    s = OracleSystem(beds.Case("cloud", opts, case.tables, WallSet(), case.particles))
+    for _ in range(3):
+        s.step(1)
+        F, _ = s.forces()
+        assert s.counters()["pp"] > 50 and s.counters()["pw"] == 0
+        total = np.array([math.fsum(F[:, k]) for k in range(3)])
+        assert np.abs(total).max() <= 1e-13 * np.abs(F).sum(), total
