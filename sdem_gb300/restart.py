@@ -58,24 +58,51 @@ def write_restart(path: str, p: Particles, contacts: Optional[tuple], tsize: int
     ncv = np.bincount(owner, minlength=n).astype(np.int32) if len(owner) else np.zeros(n, np.int32)
     if len(ncv) and ncv.max(initial=0) > NCV_LIMIT:
         raise RestartError("CL_Count_Cntctlink: so big ncv (more than 20 contacts on one particle)")
-    ids = p.id
-    index = {}
-    pairs = np.zeros((len(owner), 2), np.int32)
-    recs = []
-    for k in range(len(owner)):
-        g = int(ids[owner[k]])
-        q = int(partner[k])
-        # A pair of local spheres is listed under both, with one record; a
-        # contact with a periodic image is listed under its local sphere only,
-        # and two spheres can each touch the other's image (two records under
-        # the same two ids).  Listings share a record when their ids and their
-        # history agree bit for bit.
-        h = np.array([tand[k, 0], tand[k, 1], tand[k, 2], vrel[k]], np.float64).tobytes()
-        key = (g, q) if q > base_wall_id else (min(g, q), max(g, q), h)
-        if key not in index:
-            index[key] = len(recs) + 1
-            recs.append((tand[k, 0], tand[k, 1], tand[k, 2], vrel[k]))
-        pairs[k] = (q, index[key])
+    # A pair of local spheres is listed under both, with one record; a
+    # contact with a periodic image is listed under its local sphere only,
+    # and two spheres can each touch the other's image (two records under
+    # the same two ids).  Listings share a record when their ids and their
+    # history agree bit for bit; records are numbered in order of first
+    # listing.
+    g = np.asarray(p.id, np.int64)[owner] if len(owner) else np.zeros(0, np.int64)
+    q = partner.astype(np.int64)
+    wall = q > base_wall_id
+    a = np.where(wall, g, np.minimum(g, q))
+    b = np.where(wall, q, np.maximum(g, q))
+    hist = np.ascontiguousarray(np.concatenate([tand.reshape(-1, 3), vrel.reshape(-1, 1)], axis=1),
+                                dtype=np.float64).view(np.int64)
+    # listings grouped by the two ids (stable: a group's first entry is its
+    # earliest listing), then split where the history differs; two ids are
+    # listed at most twice in a valid list, and longer runs take the general
+    # grouping over ids and history together
+    ab = (a << 32) | (b & 0xFFFFFFFF)
+    o = np.argsort(ab, kind="stable")
+    sab = ab[o]
+    run_start = np.ones(len(o), bool)
+    if len(o) > 1:
+        run_start[1:] = sab[1:] != sab[:-1]
+    starts = np.flatnonzero(run_start)
+    if len(o) and np.diff(np.append(starts, len(o))).max() > 2:
+        keys = np.ascontiguousarray(np.concatenate([a[:, None], b[:, None], hist], axis=1))
+        kv = keys.view(np.dtype((np.void, keys.shape[1] * keys.itemsize))).ravel()
+        _, first, inverse = np.unique(kv, return_index=True, return_inverse=True)
+        group_of = inverse.ravel()
+    else:
+        new_group = run_start.copy()
+        if len(o) > 1:
+            new_group[1:] |= np.any(hist[o][1:] != hist[o][:-1], axis=1)
+        gid = np.cumsum(new_group) - 1
+        first = o[new_group]
+        group_of = np.empty(len(o), np.int64)
+        group_of[o] = gid
+    rank = np.empty(len(first), np.int64)
+    rank[np.argsort(first, kind="stable")] = np.arange(len(first))
+    index = rank[group_of] + 1                    # 1-based record of each listing
+    pairs = np.stack([partner.astype(np.int32), index.astype(np.int32)], axis=1) if len(owner) else \
+        np.zeros((0, 2), np.int32)
+    firsts = np.sort(first)
+    recs = np.concatenate([tand.reshape(-1, 3)[firsts], vrel.reshape(-1)[firsts, None]], axis=1) if len(owner) \
+        else np.zeros((0, 4))
     nreal3 = 2 * (1 + tsize + rsize) - 1
     with open(path, "wb") as f:
         np.array([n, len(owner)], dtype=np.int32).tofile(f)
@@ -88,7 +115,7 @@ def write_restart(path: str, p: Particles, contacts: Optional[tuple], tsize: int
         np.ascontiguousarray(blk, dtype=np.float64).tofile(f)
         ncv.tofile(f)
         pairs.tofile(f)
-        np.array(recs, dtype=np.float64).reshape(-1, 4).tofile(f)
+        np.ascontiguousarray(recs, dtype=np.float64).reshape(-1, 4).tofile(f)
 
 
 def read_restart(path: str, tsize: int, rsize: int, radius_of_type: np.ndarray,
@@ -132,15 +159,13 @@ def read_restart(path: str, tsize: int, rsize: int, radius_of_type: np.ndarray,
     parts = Particles(id=ints[sel, 0].copy(), ptype=ints[sel, 1].copy(), usrmark=ints[sel, 2].copy(), posR=posR,
                       linVel=blk[sel, :t0].copy(), linAcc=blk[sel, t0:t1].copy(), theta=blk[sel, t1].copy(),
                       rotVel=blk[sel, t2:t2 + rsize].copy(), rotAcc=blk[sel, t2 + rsize:t2 + 2 * rsize].copy())
-    start = np.concatenate([[0], np.cumsum(ncv)[:-1]]).astype(np.int64)
-    own, par, td, vr = [], [], [], []
-    for new_i, i in enumerate(sel):
-        for k in range(start[i], start[i] + ncv[i]):
-            q, j = int(pairs[k, 0]), int(pairs[k, 1])
-            own.append(new_i)
-            par.append(q)
-            td.append(tan[j - 1, :3])
-            vr.append(tan[j - 1, 3])
-    contacts = (np.array(own, np.int32), np.array(par, np.int32), np.array(td, np.float64).reshape(-1, 3),
-                np.array(vr, np.float64))
+    # every listing with its owner's position in the file; the kept owners
+    # are renumbered in order
+    owner_all = np.repeat(np.arange(n, dtype=np.int64), ncv.astype(np.int64))
+    new_index = np.full(n, -1, np.int64)
+    new_index[sel] = np.arange(len(sel))
+    keep_l = new_index[owner_all] >= 0
+    rec = pairs[keep_l, 1].astype(np.int64) - 1
+    contacts = (new_index[owner_all[keep_l]].astype(np.int32), pairs[keep_l, 0].astype(np.int32),
+                np.ascontiguousarray(tan[rec, :3]), np.ascontiguousarray(tan[rec, 3]))
     return parts, contacts
