@@ -68,3 +68,52 @@ def test_ncv_limit(tmp_path):
     partner = np.arange(2, 23, dtype=np.int32)
     with pytest.raises(restart.RestartError):
         restart.write_restart(str(tmp_path / "x"), p, (owner, partner, np.zeros((21, 3)), np.zeros(21)), 2, 2)
+
+
+def _records_by_loop(ids, owner, partner, tand, vrel, base_wall_id):
+    """The record numbering stated listing by listing: a new record for each
+    (ids, history) not seen before, in order of first listing."""
+    index, recs, pairs = {}, [], []
+    for k in range(len(owner)):
+        g, q = int(ids[owner[k]]), int(partner[k])
+        h = np.array([*tand[k], vrel[k]], np.float64).tobytes()
+        key = (g, q) if q > base_wall_id else (min(g, q), max(g, q), h)
+        if key not in index:
+            index[key] = len(recs) + 1
+            recs.append((*tand[k], vrel[k]))
+        pairs.append((q, index[key]))
+    return np.array(pairs, np.int32), np.array(recs, np.float64).reshape(-1, 4)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_writer_numbers_records_as_the_listing_order(tmp_path, mixed):
+    # the vectorised writer against the listing-by-listing statement: local
+    # pairs (two listings, one record), wall contacts, mutual contacts with
+    # periodic images (two listings under the same ids, two histories), and a
+    # run of four listings under one pair of ids
+    case, o = stepped_case()
+    st = o.state()
+    owner, partner, tand, vrel = (np.asarray(a) for a in o.contacts())
+    if mixed:
+        extra_o = np.array([0, 1, 0, 1], np.int32)
+        extra_q = np.array([st.id[1], st.id[0], st.id[1], st.id[0]], np.int32)
+        extra_t = np.array([[1e-7, 0, 0], [2e-7, 0, 0], [1e-7, 0, 0], [3e-7, 0, 0]])
+        extra_v = np.array([0.1, 0.2, 0.1, 0.3])
+        owner = np.concatenate([owner, extra_o])
+        partner = np.concatenate([partner, extra_q])
+        tand = np.concatenate([tand, extra_t])
+        vrel = np.concatenate([vrel, extra_v])
+    path = str(tmp_path / "r")
+    restart.write_restart(path, st, (owner, partner, tand, vrel), case.opts.tsize, case.opts.rsize,
+                          case.opts.base_wall_id)
+    order = np.argsort(owner, kind="stable")
+    want_pairs, want_recs = _records_by_loop(st.id, owner[order], partner[order], tand[order], vrel[order],
+                                             case.opts.base_wall_id)
+    raw = np.fromfile(path, dtype=np.uint8)
+    n, nct = np.frombuffer(raw, np.int32, count=2)
+    nreal3 = 2 * (1 + case.opts.tsize + case.opts.rsize) - 1
+    off = 8 + 24 * n + 12 * n + 24 * nreal3 * n + 4 * n
+    pairs = np.frombuffer(raw, np.int32, count=2 * nct, offset=off).reshape(-1, 2)
+    recs = np.frombuffer(raw, np.float64, offset=off + 8 * nct).reshape(-1, 4)
+    np.testing.assert_array_equal(pairs, want_pairs)
+    np.testing.assert_array_equal(recs, want_recs)
