@@ -24,6 +24,12 @@ GOLDEN = {
     # hierarchical search over three levels of cells
     "hrchl_poly3": (lambda: beds.scaled(beds.lattice_cloud_case(400, seed=205, ntypes=9, d_lo=0.3e-3, d_hi=1.2e-3,
                                                                 nn=0.9e-3), cs_method=2), 30),
+    # a rough floor of fixed spheres, linear spring-dashpot, forward Euler
+    "lsd_fe_fixed": (lambda: beds.fixed_floor_case(400, 206, cf_type=props.CFT_LSD, ntypes=3, pi=1, pri=1), 30),
+    # Adams-Bashforth 3, rolling resistance scaled by the relative speed
+    # (CT_Model 2), the rotation update from the angular velocity (no quirk)
+    "hertz_ab3_ct2": (lambda: beds.scaled(beds.lattice_cloud_case(400, seed=207, pi=3, pri=3), ct_model=2,
+                                          quirk_ab2_rot=0), 30),
 }
 
 CHAIN = (1, 10)   # steps after the input file whose state is stored

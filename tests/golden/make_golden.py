@@ -43,7 +43,7 @@ def main() -> None:
         # the chain starts from the file, as a restarted run does
         p, c = restart.read_restart(os.path.join(HERE, file_name(name, pre)), case.opts.tsize, case.opts.rsize,
                                     case.tables.radius)
-        o2 = OracleSystem(beds.Case(case.name, case.opts, case.tables, case.walls, p, contacts=c))
+        o2 = OracleSystem(beds.Case(case.name, case.opts, case.tables, case.walls, p, contacts=c, fixed=case.fixed))
         done = 0
         for k in CHAIN:
             o2.step(k - done)

@@ -23,7 +23,7 @@ def start(name: str):
     maker, pre = GOLDEN[name]
     base = maker()
     p, c = load(name, pre, base)
-    return beds.Case(base.name, base.opts, base.tables, base.walls, p, contacts=c), pre
+    return beds.Case(base.name, base.opts, base.tables, base.walls, p, contacts=c, fixed=base.fixed), pre
 
 
 def forces(name: str, itime: int):
