@@ -32,7 +32,7 @@ from typing import Optional, Tuple
 
 import numpy as np
 
-from .beds import Particles
+from .beds import FixedSpheres, Particles
 
 NCV_LIMIT = 20   # CL_Count_Cntctlink aborts above this (Prtcl_CL_and_CF.f90:641,648)
 
@@ -169,3 +169,45 @@ def read_restart(path: str, tsize: int, rsize: int, radius_of_type: np.ndarray,
     contacts = (new_index[owner_all[keep_l]].astype(np.int32), pairs[keep_l, 0].astype(np.int32),
                 np.ascontiguousarray(tan[rec, :3]), np.ascontiguousarray(tan[rec, 3]))
     return parts, contacts
+
+
+# FixedSpheresCoord.dat: per fixed sphere x, y, z, diameter (float64) and its
+# type (int32), 36 bytes, packed (the MPI struct of PIO_ReadFixedCoord)
+FIXED_RECORD = np.dtype([("pos", "<f8", (3,)), ("diam", "<f8"), ("ptype", "<i4")])
+
+
+def write_fixed_coords(path: str, pos: np.ndarray, ptype: np.ndarray, radius_of_type: np.ndarray) -> None:
+    """FixedSpheresCoord.dat for the fixed spheres at `pos` of types `ptype`
+    (1-based; the diameter written is twice the type's radius)."""
+    rec = np.zeros(len(pos), FIXED_RECORD)
+    rec["pos"] = pos
+    rec["ptype"] = ptype
+    rec["diam"] = 2.0 * np.asarray(radius_of_type)[np.asarray(ptype) - 1]
+    rec.tofile(path)
+
+
+def read_fixed_coords(path: str, num_prtcl_fix: int, num_prtcl: int, radius_of_type: np.ndarray,
+                      dom_min, dom_max) -> FixedSpheres:
+    """PIO_ReadFixedCoord (Prtcl_IOAndVisu.f90:163-291) on one rank: the
+    fixed spheres of the file, numbered file position + numPrtcl (above
+    every moving id), the radius from the type.  The checks of the reference
+    raise RestartError: a file whose size is not numPrtclFix records ("file
+    byte wrong"), a diameter that differs from its type's by more than 1e-6
+    relative ("Diameter not coordinate"), a sphere outside [dom_min, dom_max)
+    (nfix_sum /= numPrtclFix)."""
+    import os
+    if os.path.getsize(path) != FIXED_RECORD.itemsize * num_prtcl_fix:
+        raise RestartError("PIO_ReadFixedCoord: file byte wrong")
+    rec = np.fromfile(path, dtype=FIXED_RECORD)
+    ptype = rec["ptype"].astype(np.int32)
+    radius = np.asarray(radius_of_type, np.float64)[ptype - 1]
+    if np.any(np.abs(2.0 * radius / rec["diam"] - 1.0) > 1.0e-6):
+        raise RestartError("PIO_ReadFixedCoord: Diameter not coordinate")
+    pos = rec["pos"].astype(np.float64)
+    inside = np.ones(len(rec), bool)
+    for k in range(3):
+        inside &= (pos[:, k] >= dom_min[k]) & (pos[:, k] < dom_max[k])
+    if not inside.all():
+        raise RestartError("PIO_ReadFixedCoord: nfix_sum /= numPrtclFix")
+    ids = (np.arange(1, len(rec) + 1) + num_prtcl).astype(np.int32)
+    return FixedSpheres(id=ids, ptype=ptype, pos=pos)

@@ -117,3 +117,28 @@ def test_writer_numbers_records_as_the_listing_order(tmp_path, mixed):
     recs = np.frombuffer(raw, np.float64, offset=off + 8 * nct).reshape(-1, 4)
     np.testing.assert_array_equal(pairs, want_pairs)
     np.testing.assert_array_equal(recs, want_recs)
+
+
+def test_fixed_coords_file(tmp_path):
+    # FixedSpheresCoord.dat in the reference's record layout: positions,
+    # diameters and types round-trip, ids continue above the moving ones, and
+    # the reader refuses what PIO_ReadFixedCoord aborts on
+    case = beds.fixed_floor_case(300, 61)
+    fx = case.fixed
+    path = str(tmp_path / "FixedSpheresCoord.dat")
+    restart.write_fixed_coords(path, fx.pos, fx.ptype, case.tables.radius)
+    assert (tmp_path / "FixedSpheresCoord.dat").stat().st_size == 36 * fx.n
+    got = restart.read_fixed_coords(path, fx.n, 1000, case.tables.radius, case.opts.minpoint, case.opts.maxpoint)
+    np.testing.assert_array_equal(got.pos, fx.pos)
+    np.testing.assert_array_equal(got.ptype, fx.ptype)
+    np.testing.assert_array_equal(got.id, np.arange(1001, 1001 + fx.n))
+    with pytest.raises(restart.RestartError, match="file byte wrong"):
+        restart.read_fixed_coords(path, fx.n + 1, 1000, case.tables.radius, case.opts.minpoint, case.opts.maxpoint)
+    bad = np.fromfile(path, dtype=restart.FIXED_RECORD)
+    bad["diam"][0] *= 1.001
+    bad.tofile(path)
+    with pytest.raises(restart.RestartError, match="Diameter not coordinate"):
+        restart.read_fixed_coords(path, fx.n, 1000, case.tables.radius, case.opts.minpoint, case.opts.maxpoint)
+    restart.write_fixed_coords(path, fx.pos + np.array([1.0, 0.0, 0.0]), fx.ptype, case.tables.radius)
+    with pytest.raises(restart.RestartError, match="numPrtclFix"):
+        restart.read_fixed_coords(path, fx.n, 1000, case.tables.radius, case.opts.minpoint, case.opts.maxpoint)
