@@ -25,6 +25,17 @@ def cloud(**kw):
     return beds.lattice_cloud_case(**base)
 
 
+def moving_floor(case, v=(0.2, 0.0, 0.05)):
+    """The case with its floor (the first box wall) moving tangentially at v,
+    the wall's translational velocity of G_add_PlaneWall."""
+    import dataclasses
+    from sdem_gb300.geometry import WallSet
+    ws = WallSet(walls=[w.copy() for w in case.walls.walls], flags=[f.copy() for f in case.walls.flags])
+    assert ws.walls[0][13] == 1.0     # the floor's normal is +y
+    ws.walls[0][16:19] = v
+    return dataclasses.replace(case, walls=ws)
+
+
 CASES = {
     "hertz_ab2": lambda: cloud(),
     "lsd_ab2": lambda: cloud(seed=12, cf_type=props.CFT_LSD, ntypes=3),
@@ -33,6 +44,9 @@ CASES = {
     "lsd_fe": lambda: cloud(seed=15, cf_type=props.CFT_LSD, pi=1, pri=1),
     "hertz_ct2_noquirk": lambda: beds.scaled(cloud(seed=16), ct_model=2, quirk_ab2_rot=0),
     "mono_one_type": lambda: cloud(seed=17, ntypes=1, nn=0.995e-3),
+    # a floor moving tangentially (the wall velocity in the force law and in
+    # the near-wall refresh)
+    "hertz_moving_floor": lambda: moving_floor(cloud(seed=18)),
     # periodic images (PC_Comm_For_Cntct, FineSearch3, ContactForce_PPG)
     "periodic_xyz": lambda: beds.periodic_lattice_case(800, 31, (1, 1, 1)),
     "periodic_y": lambda: beds.periodic_lattice_case(800, 32, (0, 1, 0)),
@@ -88,7 +102,7 @@ def test_one_step_from_identical_inputs(gpu_lib, name):
 
 
 @pytest.mark.parametrize("name", ["hertz_ab2", "lsd_ab2", "hertz_finite_walls", "periodic_xyz", "periodic_xz",
-                                  "hopper", "fixed_floor", "hrchl_hopper", "hrchl_poly3"])
+                                  "hopper", "fixed_floor", "hrchl_hopper", "hrchl_poly3", "hertz_moving_floor"])
 def test_twenty_steps_resynchronised(gpu_lib, name):
     """A chain of single steps, each from the oracle's state and contact list
     (restart-file style), so chaos cannot hide or create a mismatch."""

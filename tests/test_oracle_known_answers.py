@@ -290,3 +290,24 @@ def test_pair_forces_cancel_in_a_cloud(cf):
         assert s.counters()["pp"] > 50 and s.counters()["pw"] == 0
         total = np.array([math.fsum(F[:, k]) for k in range(3)])
         assert np.abs(total).max() <= 1e-13 * np.abs(F).sum(), total
+
+
+def test_moving_floor_drags_a_resting_sphere():
+    # a floor moving along x at v (the wall's translational velocity,
+    # G_add_PlaneWall's t_vel): the first step's spring is the relative
+    # tangential displacement -v dt, so the sphere feels Kt sqrt(delta) v dt
+    # along +x (Kt = 16/3 G* sqrt(R*) of the wall pair) besides the normal load
+    E, nu, d, delta, v, dt = 5e7, 0.3, 1e-3, 4e-6, 0.05, 1e-7
+    walls = box_walls((0.0, 0.0, 0.0), (0.01, 0.01, 0.01))
+    walls.walls[0][16:19] = (v, 0.0, 0.0)                    # the floor (y = 0) moves along x
+    case = two_sphere_case(props.CFT_NLIN, 0.0, e_n=0.8, mu=0.5, E=E, walls=walls, dt=dt)
+    p = case.particles.take(np.array([0]))
+    p.posR[0, :3] = (0.005, d / 2 - delta, 0.005)
+    s = OracleSystem(beds.Case("conveyor", case.opts, case.tables, walls, p))
+    s.step(1)
+    F, _ = s.forces()
+    G = E / (2.0 * (1.0 + nu))
+    Gs = 1.0 / (2.0 * (2.0 - nu) / G)
+    kt = 16.0 / 3.0 * Gs * math.sqrt(d / 2.0)
+    assert F[0, 0] == pytest.approx(kt * math.sqrt(delta) * v * dt, rel=1e-10)
+    assert F[0, 1] > 0.0 and abs(F[0, 2]) == 0.0
