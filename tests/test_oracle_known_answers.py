@@ -311,3 +311,21 @@ def test_moving_floor_drags_a_resting_sphere():
     kt = 16.0 / 3.0 * Gs * math.sqrt(d / 2.0)
     assert F[0, 0] == pytest.approx(kt * math.sqrt(delta) * v * dt, rel=1e-10)
     assert F[0, 1] > 0.0 and abs(F[0, 2]) == 0.0
+
+
+def test_forward_euler_free_fall_closed_form():
+    # FE (PI_Method 1): x_{k+1} = x_k + v_k dt, v_{k+1} = v_k + a dt, so
+    # v_n = v0 + n a dt and x_n = x0 + n v0 dt + a dt^2 n (n - 1) / 2
+    t = props.build_tables(1, [1e-3], [2500.0], [1e7], [0.3], (0.3, 0.3, 0.1, 0.9, 0.9), [1e7], [0.3],
+                           (0.3, 0.3, 0.1, 0.9, 0.9))
+    o = beds.Options(dt=1e-4, minpoint=(0, 0, 0), maxpoint=(1, 1, 1), pi_method=1, pri_method=1)
+    p = beds.new_particles(np.array([[0.5, 0.9, 0.5]]), np.array([1]), t.radius, np.array([[0.0, 0.1, 0.0]]),
+                           o.tsize, o.rsize)
+    s = OracleSystem(beds.Case("fall_fe", o, t, WallSet(), p))
+    n = 100
+    s.step(n)
+    st = s.state()
+    a, dt = -9.81, 1e-4
+    assert st.linVel[0, 0, 1] == pytest.approx(0.1 + n * a * dt, rel=1e-12)
+    assert st.posR[0, 1] == pytest.approx(0.9 + n * 0.1 * dt + a * dt * dt * n * (n - 1) / 2, rel=1e-12)
+    assert st.linAcc[0, 0, 1] == pytest.approx(a, rel=1e-15)
