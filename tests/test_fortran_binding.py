@@ -113,3 +113,22 @@ def test_patch_inserts_only_and_calls_the_driver():
     public = set(re.findall(r"\b(gpu_\w+)", re.search(r"public ::(.*?)\n\s*\n", drv, flags=re.S).group(1)))
     called = set(re.findall(r"call (gpu_\w+)", body))
     assert called and called <= public, called - public
+
+
+def test_patch_applies_to_the_published_file(tmp_path):
+    # the insertion points exist as the patch expects them in the
+    # reference's Prtcl_DEMSystem.f90 (a dry run of patch on a copy; skipped
+    # where the reference's sources or the patch tool are absent)
+    import shutil
+    import subprocess
+    import pytest
+    src = os.environ.get("SDEM_REFERENCE_SRC", "/root/reference/src/DEM")
+    target = os.path.join(src, "Prtcl_DEMSystem.f90")
+    if not os.path.exists(target) or shutil.which("patch") is None:
+        pytest.skip("no reference source or no patch tool here")
+    shutil.copy(target, tmp_path / "Prtcl_DEMSystem.f90")
+    with open(os.path.join(FDIR, "Prtcl_DEMSystem_gpu.patch")) as f:
+        r = subprocess.run(["patch", "-p0", "--dry-run"], stdin=f, cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = r.stdout.lower()
+    assert "failed" not in out and "fuzz" not in out and "offset" not in out, r.stdout
