@@ -35,3 +35,20 @@ def test_cfg_struct_layout_matches_header():
     assert cfg.cntct_list_size == 6 and cfg.base_wall_id == 10000000 and cfg.wall_max_update_iter == 100
     assert cfg.dt == 1.0e-5 and tuple(cfg.gravity) == (0.0, -9.81, 0.0) and cfg.wall_neighbor_ratio == 2.0
     assert cfg.quirk_ab2_rot == 1 and cfg.cs_ratio == 1.0
+
+
+def test_headers_compile_as_c_and_cxx(tmp_path):
+    # a C or C++ host includes the headers as they are (no CUDA headers needed)
+    import shutil
+    import subprocess
+    import pytest
+    for cc, lang in (("gcc", "c"), ("g++", "c++")):
+        exe = shutil.which(cc)
+        if exe is None:
+            pytest.skip(f"no {cc}")
+        for h in ("sdem_gpu.h", "sdem_surrogate.h"):
+            src = tmp_path / f"use_{h}.{'c' if lang == 'c' else 'cpp'}"
+            src.write_text(f'#include "{os.path.join(ROOT, "include", h)}"\nint main(void) {{ return 0; }}\n')
+            r = subprocess.run([exe, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", lang, str(src)],
+                               capture_output=True, text=True)
+            assert r.returncode == 0, (cc, h, r.stderr)
