@@ -1,8 +1,6 @@
 """The autotuner's host logic without a GPU: the choice is the fastest
 measured candidate (ties keep the first), size classes separate beds that
 must be tuned apart, and choices are cached by class."""
-import numpy as np
-
 from sdem_gb300 import beds, tune
 
 
